@@ -1,0 +1,115 @@
+/* hvm_gb300.h — C ABI of the GB300-native HVM2 evaluator (libhvm_gb300.so).
+ *
+ * Plain C types only: pointers, sizes and fixed-width integers. Every entry
+ * point names the reference interface it replaces or extends.
+ */
+#ifndef HVM_GB300_H
+#define HVM_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- Drop-in entry point ---------------------------------------------------
+ *
+ * Replaces the reference's CUDA runtime entry point
+ *   `extern "C" void hvm_cu(u32* book_buffer)`      (src/hvm.cu:2320)
+ * bound from Rust as
+ *   `extern "C" { fn hvm_cu(book_buffer: *const u32); }`  (src/main.rs:17-20)
+ * `book_buffer` is the serialized Book (src/hvm.rs:957-1003). The call loads
+ * the book, normalises `@main`, and prints on stdout, as the reference does:
+ *   Result: <tree>
+ *   - ITRS: <interactions>
+ *   - LEAK: <redexes moved between threads through the global ring>
+ *   - TIME: <seconds>s
+ *   - MIPS: <million interactions per second>
+ * A book the loader rejects prints "failed to load book" on stderr and
+ * returns (src/hvm.cu:2325-2328); a device error prints a message on stderr
+ * and exits with EXIT_FAILURE (src/hvm.cu:2360-2367).
+ */
+void hvm_cu(const uint32_t* book_buffer);
+
+/* ---- Front-end ---------------------------------------------------------------
+ *
+ * Replaces `ast::Book::parse(code).build().to_buffer(&mut buf)`
+ * (src/main.rs:87-92; src/ast.rs:44-634; src/hvm.rs:957-1003), which the
+ * reference runs in Rust before calling `hvm_cu`.
+ * Writes the book buffer into `out` (capacity `out_cap_words` u32 words) and
+ * its length into `*out_words`; call with `out == NULL` to query the length.
+ * Returns 0, or 1 (parse error), 2 (build error: missing `@main`, unbound
+ * reference), 3 (output too small); `err` receives the message.
+ */
+int hvm_gb300_book_from_text(const char* text, uint32_t* out, size_t out_cap_words,
+                             size_t* out_words, char* err, size_t err_cap);
+
+/* Canonical form of one printed tree (the text after "Result:"): variables
+ * renamed x0, x1, ... in first-occurrence order and numbers as their 29-bit
+ * Numb word, the comparison the reference's test harness makes
+ * (tests/run.rs:112-147). Returns 0, 1 on a parse error, 3 if `out` is too
+ * small; `out == NULL` queries the length. */
+int hvm_gb300_canonical_tree(const char* text, char* out, size_t out_cap, size_t* out_len,
+                             char* err, size_t err_cap);
+
+/* ---- Handle API ----------------------------------------------------------------
+ *
+ * Re-entrant form of `hvm_cu` for callers that run many nets, read results
+ * programmatically, or time the evaluator: it splits the reference's
+ * book_load -> gnet_create -> boot -> do_run_io -> print sequence
+ * (src/hvm.cu:2320-2397, src/run.cu:857-925) into separate calls.
+ */
+typedef struct hvm_gb300_runtime hvm_gb300_runtime;
+
+typedef struct {
+  int32_t device;             /* CUDA device ordinal */
+  uint32_t threads_per_block; /* multiple of 32 */
+  uint32_t stack_cap;         /* redexes per thread in the shared-memory LIFO */
+  uint32_t blocks_per_sm;     /* 0 = as many as fit */
+  uint32_t node_log2;         /* node space 2^k words (k <= 29, the port width) */
+  uint32_t vars_log2;         /* var space 2^k words (k <= 29) */
+  uint32_t ring_log2;         /* global redex ring 2^k entries */
+  uint32_t max_turns;         /* 0 = unbounded; else fail after this many turns */
+} hvm_gb300_config;
+
+typedef struct {
+  uint64_t itrs;          /* interactions, counted as the reference counts them */
+  uint64_t leak;          /* redexes that went through the global ring */
+  uint64_t turns;         /* evaluator turns run */
+  uint64_t retries;       /* availability re-tries */
+  uint64_t rule_hist[8];  /* interactions per rule: LINK CALL VOID ERAS ANNI COMM OPER SWIT */
+  double seconds;         /* wall time inside normalisation */
+  uint32_t threads, grid, block;
+} hvm_gb300_stats;
+
+/* Fills `cfg` with the defaults used by `hvm_cu`. */
+void hvm_gb300_default_config(hvm_gb300_config* cfg);
+
+/* Creates a runtime on `cfg->device` (NULL = defaults) and allocates its net.
+ * Returns 0; on failure *out may still hold a runtime whose error text says why. */
+int hvm_gb300_create(const hvm_gb300_config* cfg, hvm_gb300_runtime** out);
+
+/* Loads a book buffer (`words` = its length in u32, or 0 if unknown). Same
+ * limits as the reference's C loader (src/hvm.c:1408-1453). */
+int hvm_gb300_load_book(hvm_gb300_runtime* rt, const uint32_t* book_buffer, size_t words);
+
+/* Clears the net, boots `@main ~ ROOT`, normalises, and runs the readback
+ * expansion of the IO loop (which can add interactions). `stats` may be NULL. */
+int hvm_gb300_run(hvm_gb300_runtime* rt, hvm_gb300_stats* stats);
+
+/* The normal form at ROOT in the reference's printed format (without the
+ * "Result: " prefix). `out == NULL` queries the length (excluding the NUL). */
+int hvm_gb300_result(hvm_gb300_runtime* rt, char* out, size_t cap, size_t* len);
+
+/* Last error message of `rt` ("" if none). */
+const char* hvm_gb300_error(const hvm_gb300_runtime* rt);
+
+/* Frees the runtime and its device memory. */
+void hvm_gb300_destroy(hvm_gb300_runtime* rt);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* HVM_GB300_H */

@@ -1,0 +1,228 @@
+"""GB300-native HVM2 evaluator: Python host binding.
+
+Mirrors the reference's surface for the `hvm run-cu` path:
+  * `book_from_text(code)`  -- `ast::Book::parse(code).build().to_buffer()`
+                               (src/ast.rs, src/hvm.rs:957-1003)
+  * `hvm_cu(book)`          -- `extern "C" hvm_cu(u32*)` (src/hvm.cu:2320),
+                               printing the reference's output lines
+  * `Runtime`               -- the re-entrant handle API of include/hvm_gb300.h
+
+Everything computes through `libhvm_gb300.so` (sm_103a CUDA). There is no CPU
+fallback: if the library is missing the import of `lib()` raises.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+from dataclasses import dataclass, field
+
+import numpy as np
+
+PKG_DIR = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(PKG_DIR, "libhvm_gb300.so")
+CLI_PATH = os.path.join(PKG_DIR, "hvm")
+
+_lib = None
+
+
+class HvmError(RuntimeError):
+    pass
+
+
+class Config(ctypes.Structure):
+    _fields_ = [
+        ("device", ctypes.c_int32),
+        ("threads_per_block", ctypes.c_uint32),
+        ("stack_cap", ctypes.c_uint32),
+        ("blocks_per_sm", ctypes.c_uint32),
+        ("node_log2", ctypes.c_uint32),
+        ("vars_log2", ctypes.c_uint32),
+        ("ring_log2", ctypes.c_uint32),
+        ("max_turns", ctypes.c_uint32),
+    ]
+
+
+class _Stats(ctypes.Structure):
+    _fields_ = [
+        ("itrs", ctypes.c_uint64),
+        ("leak", ctypes.c_uint64),
+        ("turns", ctypes.c_uint64),
+        ("retries", ctypes.c_uint64),
+        ("rule_hist", ctypes.c_uint64 * 8),
+        ("seconds", ctypes.c_double),
+        ("threads", ctypes.c_uint32),
+        ("grid", ctypes.c_uint32),
+        ("block", ctypes.c_uint32),
+    ]
+
+
+RULE_NAMES = ("LINK", "CALL", "VOID", "ERAS", "ANNI", "COMM", "OPER", "SWIT")
+
+# Every symbol include/hvm_gb300.h declares.
+EXPORTED_SYMBOLS = (
+    "hvm_cu",
+    "hvm_gb300_book_from_text",
+    "hvm_gb300_canonical_tree",
+    "hvm_gb300_default_config",
+    "hvm_gb300_create",
+    "hvm_gb300_load_book",
+    "hvm_gb300_run",
+    "hvm_gb300_result",
+    "hvm_gb300_error",
+    "hvm_gb300_destroy",
+)
+
+
+def lib() -> ctypes.CDLL:
+    """Loads libhvm_gb300.so (built in-tree by build.py); raises if absent."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(LIB_PATH):
+        raise HvmError(f"{LIB_PATH} is missing: build it with `python lambdavm-rust_gb300/build.py` "
+                       "or `python -c 'import __graft_entry__ as g; g.build()'`")
+    L = ctypes.CDLL(LIB_PATH)
+    u32p = ctypes.POINTER(ctypes.c_uint32)
+    L.hvm_cu.argtypes = [u32p]
+    L.hvm_cu.restype = None
+    L.hvm_gb300_book_from_text.argtypes = [ctypes.c_char_p, u32p, ctypes.c_size_t,
+                                           ctypes.POINTER(ctypes.c_size_t), ctypes.c_char_p, ctypes.c_size_t]
+    L.hvm_gb300_canonical_tree.argtypes = [ctypes.c_char_p, ctypes.c_char_p, ctypes.c_size_t,
+                                           ctypes.POINTER(ctypes.c_size_t), ctypes.c_char_p, ctypes.c_size_t]
+    L.hvm_gb300_default_config.argtypes = [ctypes.POINTER(Config)]
+    L.hvm_gb300_default_config.restype = None
+    L.hvm_gb300_create.argtypes = [ctypes.POINTER(Config), ctypes.POINTER(ctypes.c_void_p)]
+    L.hvm_gb300_load_book.argtypes = [ctypes.c_void_p, u32p, ctypes.c_size_t]
+    L.hvm_gb300_run.argtypes = [ctypes.c_void_p, ctypes.POINTER(_Stats)]
+    L.hvm_gb300_result.argtypes = [ctypes.c_void_p, ctypes.c_char_p, ctypes.c_size_t,
+                                   ctypes.POINTER(ctypes.c_size_t)]
+    L.hvm_gb300_error.argtypes = [ctypes.c_void_p]
+    L.hvm_gb300_error.restype = ctypes.c_char_p
+    L.hvm_gb300_destroy.argtypes = [ctypes.c_void_p]
+    L.hvm_gb300_destroy.restype = None
+    _lib = L
+    return L
+
+
+def book_from_text(code: str) -> np.ndarray:
+    """Parses `.hvm` text into the reference's u32 book buffer."""
+    L = lib()
+    n = ctypes.c_size_t()
+    err = ctypes.create_string_buffer(4096)
+    data = code.encode()
+    rc = L.hvm_gb300_book_from_text(data, None, 0, ctypes.byref(n), err, len(err))
+    if rc:
+        raise HvmError(err.value.decode())
+    buf = np.zeros(n.value, dtype=np.uint32)
+    rc = L.hvm_gb300_book_from_text(data, buf.ctypes.data_as(ctypes.POINTER(ctypes.c_uint32)),
+                                    n.value, ctypes.byref(n), err, len(err))
+    if rc:
+        raise HvmError(err.value.decode())
+    return buf
+
+
+def canonical(tree_text: str) -> str:
+    """Canonical form of a printed tree: vars renamed by first occurrence,
+    numbers as 29-bit words (bit-exact comparison, f24 included)."""
+    L = lib()
+    n = ctypes.c_size_t()
+    err = ctypes.create_string_buffer(4096)
+    data = tree_text.encode()
+    rc = L.hvm_gb300_canonical_tree(data, None, 0, ctypes.byref(n), err, len(err))
+    if rc:
+        raise HvmError(err.value.decode())
+    out = ctypes.create_string_buffer(n.value + 1)
+    rc = L.hvm_gb300_canonical_tree(data, out, n.value + 1, ctypes.byref(n), err, len(err))
+    if rc:
+        raise HvmError(err.value.decode())
+    return out.value.decode()
+
+
+@dataclass
+class RunStats:
+    itrs: int
+    leak: int
+    turns: int
+    retries: int
+    seconds: float
+    threads: int
+    grid: int
+    block: int
+    rule_hist: dict = field(default_factory=dict)
+
+    @property
+    def mips(self) -> float:
+        return self.itrs / self.seconds / 1e6 if self.seconds > 0 else float("nan")
+
+
+class Runtime:
+    """One GPU net (include/hvm_gb300.h handle API)."""
+
+    def __init__(self, device: int = 0, **overrides):
+        L = lib()
+        cfg = Config()
+        L.hvm_gb300_default_config(ctypes.byref(cfg))
+        cfg.device = device
+        for k, v in overrides.items():
+            if not hasattr(cfg, k):
+                raise TypeError(f"unknown config field {k}")
+            setattr(cfg, k, v)
+        self.config = cfg
+        h = ctypes.c_void_p()
+        rc = L.hvm_gb300_create(ctypes.byref(cfg), ctypes.byref(h))
+        self._h = h
+        if rc:
+            msg = L.hvm_gb300_error(h).decode() if h else "create failed"
+            self.close()
+            raise HvmError(msg)
+
+    def _check(self, rc: int) -> None:
+        if rc:
+            raise HvmError(lib().hvm_gb300_error(self._h).decode())
+
+    def load(self, book) -> None:
+        if isinstance(book, str):
+            book = book_from_text(book)
+        buf = np.ascontiguousarray(np.asarray(book, dtype=np.uint32))
+        self._book = buf
+        self._check(lib().hvm_gb300_load_book(self._h, buf.ctypes.data_as(ctypes.POINTER(ctypes.c_uint32)),
+                                              buf.size))
+
+    def run(self) -> RunStats:
+        st = _Stats()
+        self._check(lib().hvm_gb300_run(self._h, ctypes.byref(st)))
+        return RunStats(itrs=st.itrs, leak=st.leak, turns=st.turns, retries=st.retries, seconds=st.seconds,
+                        threads=st.threads, grid=st.grid, block=st.block,
+                        rule_hist={RULE_NAMES[i]: int(st.rule_hist[i]) for i in range(8)})
+
+    def result(self) -> str:
+        n = ctypes.c_size_t()
+        self._check(lib().hvm_gb300_result(self._h, None, 0, ctypes.byref(n)))
+        out = ctypes.create_string_buffer(n.value + 1)
+        self._check(lib().hvm_gb300_result(self._h, out, n.value + 1, ctypes.byref(n)))
+        return out.value.decode()
+
+    def close(self) -> None:
+        if getattr(self, "_h", None):
+            lib().hvm_gb300_destroy(self._h)
+            self._h = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def run_text(code: str, device: int = 0, **cfg) -> tuple[str, RunStats]:
+    """Parses, loads and normalises `code`; returns (result tree text, stats)."""
+    with Runtime(device=device, **cfg) as rt:
+        rt.load(code)
+        st = rt.run()
+        return rt.result(), st

@@ -1,0 +1,79 @@
+"""Builds the native parts of the package in-tree.
+
+  libhvm_gb300.so   the C-ABI library (front-end + sm_103a evaluator + runtime)
+  hvm               the command-line driver (`hvm run-cu FILE`, `hvm gen-cu FILE`)
+
+Compiled for sm_103a only (`-gencode arch=compute_103a,code=sm_103a`), with
+translation units built in parallel. Runs the same on x86_64 (cross-compile,
+no GPU needed) and on the aarch64 GPU host.
+"""
+from __future__ import annotations
+
+import os
+import subprocess
+import sys
+from concurrent.futures import ThreadPoolExecutor
+
+PKG = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(PKG)
+CSRC = os.path.join(PKG, "csrc")
+INCLUDE = os.path.join(ROOT, "include")
+BUILD = os.path.join(PKG, "_build")
+LIB = os.path.join(PKG, "libhvm_gb300.so")
+CLI = os.path.join(PKG, "hvm")
+
+NVCC = os.environ.get("NVCC", "nvcc")
+ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
+CXXFLAGS = ["-O3", "-std=c++17", "-I" + INCLUDE, "-I" + CSRC]
+
+LIB_SOURCES = ["frontend.cpp", "runtime.cu"]
+
+
+def _run(cmd: list[str]) -> None:
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError("build failed:\n" + " ".join(cmd) + "\n" + r.stdout + r.stderr)
+
+
+def _stale(target: str, deps: list[str]) -> bool:
+    if not os.path.exists(target):
+        return True
+    t = os.path.getmtime(target)
+    return any(os.path.getmtime(d) > t for d in deps)
+
+
+def _headers() -> list[str]:
+    hs = [os.path.join(CSRC, f) for f in os.listdir(CSRC) if f.endswith((".h", ".cuh"))]
+    return hs + [os.path.join(INCLUDE, f) for f in os.listdir(INCLUDE) if f.endswith(".h")]
+
+
+def _compile(src: str) -> str:
+    path = os.path.join(CSRC, src)
+    obj = os.path.join(BUILD, src + ".o")
+    if _stale(obj, [path] + _headers()):
+        if src.endswith(".cu"):
+            _run([NVCC, *ARCH, "-lineinfo", *CXXFLAGS, "-Xcompiler", "-fPIC", "-c", path, "-o", obj])
+        else:
+            _run([NVCC, *CXXFLAGS, "-Xcompiler", "-fPIC", "-c", path, "-o", obj])
+    return obj
+
+
+def build(verbose: bool = False) -> str:
+    """Compiles the library and the CLI if any source changed; returns the library path."""
+    os.makedirs(BUILD, exist_ok=True)
+    with ThreadPoolExecutor(max_workers=max(2, len(LIB_SOURCES))) as ex:
+        objs = list(ex.map(_compile, LIB_SOURCES))
+    if _stale(LIB, objs):
+        _run([NVCC, *ARCH, "-shared", "-o", LIB, *objs, "-lcudart"])
+    cli_src = os.path.join(CSRC, "hvm_cli.cpp")
+    if os.path.exists(cli_src) and _stale(CLI, [cli_src, LIB] + _headers()):
+        _run([NVCC, *CXXFLAGS, "-o", CLI, cli_src, "-L" + PKG, "-lhvm_gb300",
+              "-Xlinker", "-rpath=$ORIGIN"])
+    if verbose:
+        print("built", LIB)
+    return LIB
+
+
+if __name__ == "__main__":
+    build(verbose=True)
+    sys.exit(0)

@@ -1,0 +1,353 @@
+// evaluator.cuh — device side of the GB300 HVM2 evaluator: net memory
+// access, allocation, the lock-free linker and the eight interaction rules.
+//
+// The rules, the linker and the interaction count follow the reference
+// semantics exactly (src/hvm.c:784-1122; src/hvm.cu:999-1420), because the
+// normal form and the total interaction count must equal `hvm run-c`'s. What
+// differs is the GB300 execution model around them:
+//   * every net word lives in HBM and is touched only at L2 (ld.cg/st.cg and
+//     atomics), so no SM ever reads a stale L1 copy of a shared word;
+//   * a thread publishes freshly created nodes/vars with one gpu-scope fence
+//     before its first link, instead of the reference's per-access
+//     availability re-tries (the re-try path is kept as a safety net);
+//   * redexes live in a per-thread LIFO in shared memory; overflow and the
+//     end-of-turn remainder go to one global ring (see runtime.cu);
+//   * allocation scans a per-thread slice of the node/var space for free
+//     (zero) words, as the reference does (src/hvm.cu:880-912), with a bound
+//     on the scan that turns exhaustion into an error status instead of a
+//     spin.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+#include "hvm_defs.h"
+
+namespace hvm {
+
+// Device status codes (0 = running / ok). Written once, first error wins.
+enum : uint32_t {
+  ST_OK = 0,
+  ST_OOM_NODES = 1,     // a thread's node slice has no free word
+  ST_OOM_VARS = 2,      // a thread's var slice has no free word
+  ST_RING_FULL = 3,     // the global redex ring overflowed
+  ST_LINK_UNSET = 4,    // a link met a var word that was never created
+  ST_LINK_LIMIT = 5,    // a substitution chain exceeded the iteration bound
+  ST_BAD_REF = 6,       // a REF to a definition the book does not have
+};
+
+// One book definition on the device. Pairs for a def are stored at
+// book[off .. off+rbag_len) (redexes) then book[off+rbag_len ..) (nodes).
+struct DefHdr {
+  uint32_t node_len, rbag_len, vars_len, safe;
+  uint32_t root, off, pad0, pad1;
+};
+
+// Control block of one net. Hot atomics sit on separate 128-byte lines.
+struct alignas(128) Ctl {
+  unsigned long long head;          // next dynamically claimable ring index
+  unsigned long long pad_h[15];
+  unsigned long long tail;          // next free ring index
+  unsigned long long pad_t[15];
+  unsigned long long base;          // first ring index of this turn's input
+  unsigned long long in_end;        // one past the last input index
+  unsigned long long itrs;          // counted interactions (all turns)
+  unsigned long long leak;          // redexes that went through the ring
+  unsigned long long retries;       // availability re-tries (diagnostic)
+  unsigned long long turns;         // completed turns
+  unsigned long long pending;       // redexes left after the last turn
+  unsigned int blocks_done;
+  unsigned int status;
+  unsigned int err_info;
+  unsigned int static_per_thread;   // ring items each thread takes at turn start
+  unsigned int budget;              // interactions per thread per turn
+  unsigned int chunk;               // items per dynamic claim
+  unsigned int policy;              // 0 = fixed policy
+  unsigned int pad_c[1];
+  unsigned long long hist[8];       // interactions per rule (diagnostic)
+};
+
+// Everything a turn kernel needs; passed by value.
+struct Dev {
+  Pair* node;                 // node words, 2^k entries
+  Port* vars;                 // var words, 2^k entries (ROOT_VAR is the last)
+  Pair* ring;                 // global redex ring
+  unsigned long long ring_mask;
+  uint32_t node_slice, vars_slice;   // words per thread slice
+  uint32_t* ncur;             // per-thread allocation cursors (persist across turns)
+  uint32_t* vcur;
+  uint32_t* nloc;             // CALL scratch: [max_def_nodes][nthreads]
+  uint32_t* vloc;             // CALL scratch: [max_def_vars][nthreads]
+  uint32_t nthreads;
+  uint32_t ndefs;
+  const DefHdr* defs;
+  const Pair* book;
+  Ctl* ctl;
+};
+
+// ---- memory access -----------------------------------------------------------
+
+__device__ __forceinline__ Pair nload(const Dev& d, uint32_t i) {
+  return (Pair)__ldcg((const unsigned long long*)&d.node[i]);
+}
+__device__ __forceinline__ void nstore(const Dev& d, uint32_t i, Pair p) {
+  __stcg((unsigned long long*)&d.node[i], (unsigned long long)p);
+}
+__device__ __forceinline__ Port vload(const Dev& d, uint32_t i) { return __ldcg(&d.vars[i]); }
+__device__ __forceinline__ void vstore(const Dev& d, uint32_t i, Port p) { __stcg(&d.vars[i], p); }
+__device__ __forceinline__ Port vexch(const Dev& d, uint32_t i, Port p) { return atomicExch(&d.vars[i], p); }
+
+__device__ __forceinline__ void set_status(const Dev& d, uint32_t code, uint32_t info) {
+  if (atomicCAS(&d.ctl->status, 0u, code) == 0u) d.ctl->err_info = info;
+}
+
+// ---- per-thread state ----------------------------------------------------------
+
+struct TState {
+  Pair* stk;                  // this thread's LIFO in shared memory (stride = blockDim.x)
+  uint32_t stride;
+  uint32_t len, cap;
+  uint32_t gid;
+  uint32_t node_base, vars_base;
+  uint32_t ncur, vcur;
+  unsigned long long base;    // ring index of this turn's first input (overflow check)
+  unsigned long long itrs, leak, retries;
+  unsigned long long hist[8];
+  bool dead;                  // set after a fatal status: stop interacting
+};
+
+// Spills one redex to the global ring (available to every thread next turn).
+__device__ __forceinline__ void ring_push(const Dev& d, TState& t, Pair r) {
+  unsigned long long at = atomicAdd(&d.ctl->tail, 1ull);
+  if (at - t.base > d.ring_mask) { set_status(d, ST_RING_FULL, 0); t.dead = true; return; }
+  d.ring[at & d.ring_mask] = r;
+  t.leak++;
+}
+
+__device__ __forceinline__ void push(const Dev& d, TState& t, Pair r) {
+  if (t.len < t.cap) {
+    t.stk[(size_t)t.len * t.stride] = r;
+    t.len++;
+  } else {
+    ring_push(d, t, r);
+  }
+}
+
+// ---- allocation (src/hvm.cu:880-912, src/hvm.c:713-755) ------------------------
+
+// Returns a free node word of this thread's slice, or 0 when `budget` scans
+// found none. `budget` bounds the scans of one allocation batch, so a batch
+// can never wrap around its slice and hand out the same word twice.
+__device__ __forceinline__ uint32_t alloc_node(const Dev& d, TState& t, uint32_t& budget) {
+  while (budget > 0) {
+    budget--;
+    uint32_t at = t.node_base + t.ncur;
+    if (++t.ncur == d.node_slice) t.ncur = 0;
+    if (at != 0 && nload(d, at) == 0) return at;
+  }
+  return 0;
+}
+
+__device__ __forceinline__ uint32_t alloc_var(const Dev& d, TState& t, uint32_t& budget) {
+  while (budget > 0) {
+    budget--;
+    uint32_t at = t.vars_base + t.vcur;
+    if (++t.vcur == d.vars_slice) t.vcur = 0;
+    if (at != 0 && vload(d, at) == 0) return at;
+  }
+  return 0;
+}
+
+// ---- linking (src/hvm.c:784-840) ----------------------------------------------
+
+// Follows a var chain, consuming every resolved var on the way.
+__device__ __forceinline__ Port enter(const Dev& d, Port p) {
+  while (get_tag(p) == VAR) {
+    Port v = vexch(d, get_val(p), NONE);
+    if (v == NONE || v == 0) break;
+    vstore(d, get_val(p), 0);
+    p = v;
+  }
+  return p;
+}
+
+// Atomically wires A ~ B: publishes a substitution, or makes a redex when
+// both sides are non-vars.
+__device__ void link(const Dev& d, TState& t, Port A, Port B) {
+  for (uint32_t guard = 0; guard < (1u << 24); guard++) {
+    if (get_tag(A) != VAR && get_tag(B) == VAR) { Port x = A; A = B; B = x; }
+    if (get_tag(A) != VAR) { push(d, t, new_pair(A, B)); return; }
+    B = enter(d, B);
+    Port prev = vexch(d, get_val(A), B);
+    if (prev == NONE) return;
+    if (prev == 0) { set_status(d, ST_LINK_UNSET, get_val(A)); t.dead = true; return; }
+    vstore(d, get_val(A), 0);
+    A = prev;
+  }
+  set_status(d, ST_LINK_LIMIT, 0);
+  t.dead = true;
+}
+
+// ---- interactions (src/hvm.c:852-1122) -----------------------------------------
+
+enum : int { IR_DONE = 0, IR_RETRY = 1, IR_FATAL = 2 };
+
+// Publishes this thread's node/var creations before they become reachable
+// from another thread through a link.
+__device__ __forceinline__ void publish() { __threadfence(); }
+
+__device__ __forceinline__ int rule_eras(const Dev& d, TState& t, Port a, Port b) {
+  Pair B = nload(d, get_val(b));
+  if (B == 0) return IR_RETRY;
+  nstore(d, get_val(b), 0);
+  link(d, t, a, get_fst(B));
+  link(d, t, a, get_snd(B));
+  return IR_DONE;
+}
+
+__device__ __forceinline__ int rule_anni(const Dev& d, TState& t, Port a, Port b) {
+  Pair A = nload(d, get_val(a));
+  Pair B = nload(d, get_val(b));
+  if (A == 0 || B == 0) return IR_RETRY;
+  nstore(d, get_val(a), 0);
+  nstore(d, get_val(b), 0);
+  link(d, t, get_fst(A), get_fst(B));
+  link(d, t, get_snd(A), get_snd(B));
+  return IR_DONE;
+}
+
+__device__ __forceinline__ int rule_comm(const Dev& d, TState& t, Port a, Port b) {
+  uint32_t nb = d.node_slice, vb = d.vars_slice;
+  uint32_t n0 = alloc_node(d, t, nb), n1 = alloc_node(d, t, nb);
+  uint32_t n2 = alloc_node(d, t, nb), n3 = alloc_node(d, t, nb);
+  if (!n3) { set_status(d, ST_OOM_NODES, t.gid); return IR_FATAL; }
+  uint32_t v0 = alloc_var(d, t, vb), v1 = alloc_var(d, t, vb);
+  uint32_t v2 = alloc_var(d, t, vb), v3 = alloc_var(d, t, vb);
+  if (!v3) { set_status(d, ST_OOM_VARS, t.gid); return IR_FATAL; }
+  Pair A = nload(d, get_val(a));
+  Pair B = nload(d, get_val(b));
+  if (A == 0 || B == 0) return IR_RETRY;
+  nstore(d, get_val(a), 0);
+  nstore(d, get_val(b), 0);
+  vstore(d, v0, NONE); vstore(d, v1, NONE); vstore(d, v2, NONE); vstore(d, v3, NONE);
+  nstore(d, n0, new_pair(new_port(VAR, v0), new_port(VAR, v1)));
+  nstore(d, n1, new_pair(new_port(VAR, v2), new_port(VAR, v3)));
+  nstore(d, n2, new_pair(new_port(VAR, v0), new_port(VAR, v2)));
+  nstore(d, n3, new_pair(new_port(VAR, v1), new_port(VAR, v3)));
+  publish();
+  link(d, t, new_port(get_tag(b), n0), get_fst(A));
+  link(d, t, new_port(get_tag(b), n1), get_snd(A));
+  link(d, t, new_port(get_tag(a), n2), get_fst(B));
+  link(d, t, new_port(get_tag(a), n3), get_snd(B));
+  return IR_DONE;
+}
+
+__device__ __forceinline__ int rule_oper(const Dev& d, TState& t, Port a, Port b) {
+  uint32_t nb = d.node_slice;
+  uint32_t n0 = alloc_node(d, t, nb);
+  if (!n0) { set_status(d, ST_OOM_NODES, t.gid); return IR_FATAL; }
+  Pair B = nload(d, get_val(b));
+  if (B == 0) return IR_RETRY;
+  nstore(d, get_val(b), 0);
+  Port b1 = get_fst(B);
+  Port b2 = enter(d, get_snd(B));
+  if (get_tag(b1) == NUM) {
+    link(d, t, new_port(NUM, operate(get_val(a), get_val(b1))), b2);
+  } else {
+    nstore(d, n0, new_pair(a, b2));
+    publish();
+    link(d, t, b1, new_port(OPR, n0));
+  }
+  return IR_DONE;
+}
+
+__device__ __forceinline__ int rule_swit(const Dev& d, TState& t, Port a, Port b) {
+  uint32_t nb = d.node_slice;
+  uint32_t n0 = alloc_node(d, t, nb), n1 = alloc_node(d, t, nb);
+  if (!n1) { set_status(d, ST_OOM_NODES, t.gid); return IR_FATAL; }
+  Pair B = nload(d, get_val(b));
+  if (B == 0) return IR_RETRY;
+  nstore(d, get_val(b), 0);
+  uint32_t n = get_u24(get_val(a));
+  if (n == 0) {
+    nstore(d, n0, new_pair(get_snd(B), new_port(ERA, 0)));
+  } else {
+    nstore(d, n0, new_pair(new_port(ERA, 0), new_port(CON, n1)));
+    nstore(d, n1, new_pair(new_port(NUM, new_u24(n - 1)), get_snd(B)));
+  }
+  publish();
+  link(d, t, new_port(CON, n0), get_fst(B));
+  return IR_DONE;
+}
+
+__device__ __forceinline__ Port relocate(const Dev& d, const TState& t, Port p) {
+  Tag tag = get_tag(p);
+  if (tag >= CON) return new_port(tag, d.nloc[(size_t)get_val(p) * d.nthreads + t.gid]);
+  if (tag == VAR) return new_port(VAR, d.vloc[(size_t)get_val(p) * d.nthreads + t.gid]);
+  return p;
+}
+
+__device__ int rule_call(const Dev& d, TState& t, Port a, Port b) {
+  uint32_t fid = get_val(a) & 0xFFFFFFFu;
+  if (fid >= d.ndefs) { set_status(d, ST_BAD_REF, fid); return IR_FATAL; }
+  const DefHdr h = d.defs[fid];
+  // Copy optimisation: a safe REF meeting a DUP is duplicated like an eraser.
+  if (h.safe && get_tag(b) == DUP) return rule_eras(d, t, a, b);
+  uint32_t nb = d.node_slice, vb = d.vars_slice;
+  for (uint32_t i = 0; i < h.node_len; i++) {
+    uint32_t at = alloc_node(d, t, nb);
+    if (!at) { set_status(d, ST_OOM_NODES, t.gid); return IR_FATAL; }
+    d.nloc[(size_t)i * d.nthreads + t.gid] = at;
+  }
+  for (uint32_t i = 0; i < h.vars_len; i++) {
+    uint32_t at = alloc_var(d, t, vb);
+    if (!at) { set_status(d, ST_OOM_VARS, t.gid); return IR_FATAL; }
+    d.vloc[(size_t)i * d.nthreads + t.gid] = at;
+  }
+  for (uint32_t i = 0; i < h.vars_len; i++) vstore(d, d.vloc[(size_t)i * d.nthreads + t.gid], NONE);
+  const Pair* nodes = d.book + h.off + h.rbag_len;
+  for (uint32_t i = 0; i < h.node_len; i++) {
+    Pair p = __ldg((const unsigned long long*)&nodes[i]);
+    nstore(d, d.nloc[(size_t)i * d.nthreads + t.gid],
+           new_pair(relocate(d, t, get_fst(p)), relocate(d, t, get_snd(p))));
+  }
+  publish();
+  const Pair* rbag = d.book + h.off;
+  for (uint32_t i = 0; i < h.rbag_len; i++) {
+    Pair p = __ldg((const unsigned long long*)&rbag[i]);
+    link(d, t, relocate(d, t, get_fst(p)), relocate(d, t, get_snd(p)));
+  }
+  link(d, t, relocate(d, t, h.root), b);
+  return IR_DONE;
+}
+
+// One interaction on redex `r` (src/hvm.c:1073-1122). Returns the rule run,
+// or -1 when the redex was pushed back for a re-try.
+__device__ __forceinline__ int interact(const Dev& d, TState& t, Pair r) {
+  Port a = get_fst(r), b = get_snd(r);
+  Rule rule = get_rule(a, b);
+  if (get_tag(a) == REF && b == ROOT) {
+    rule = CALL;
+  } else if (should_swap(a, b)) {
+    Port x = a; a = b; b = x;
+  }
+  int rc;
+  switch (rule) {
+    case LINK: link(d, t, a, b); rc = IR_DONE; break;
+    case CALL: rc = rule_call(d, t, a, b); break;
+    case VOID: rc = IR_DONE; break;
+    case ERAS: rc = rule_eras(d, t, a, b); break;
+    case ANNI: rc = rule_anni(d, t, a, b); break;
+    case COMM: rc = rule_comm(d, t, a, b); break;
+    case OPER: rc = rule_oper(d, t, a, b); break;
+    default:   rc = rule_swit(d, t, a, b); break;
+  }
+  if (rc == IR_RETRY) {
+    push(d, t, r);
+    t.retries++;
+    return -1;
+  }
+  if (rc == IR_FATAL) { t.dead = true; return -1; }
+  if (rule != LINK) { t.itrs++; t.hist[rule]++; }
+  return rule;
+}
+
+}  // namespace hvm

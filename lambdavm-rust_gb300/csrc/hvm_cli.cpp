@@ -1,0 +1,69 @@
+// hvm_cli.cpp — command-line driver with the reference's `run-cu` surface
+// (src/main.rs:22-65, 93-96): `hvm run-cu FILE` parses the `.hvm` file,
+// serializes the Book and calls the C ABI `hvm_cu(book_buffer)`.
+// `hvm book FILE OUT` writes the serialized book buffer to OUT (the bytes the
+// reference passes across its C ABI), for feeding other runtimes.
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <fstream>
+#include <sstream>
+#include <string>
+#include <vector>
+
+#include "hvm_gb300.h"
+
+static std::string read_file(const char* path) {
+  std::ifstream f(path, std::ios::binary);
+  if (!f) {
+    fprintf(stderr, "Unable to read file: %s\n", path);
+    exit(1);
+  }
+  std::stringstream ss;
+  ss << f.rdbuf();
+  return ss.str();
+}
+
+static std::vector<uint32_t> to_buffer(const std::string& code) {
+  size_t words = 0;
+  char err[1024];
+  int rc = hvm_gb300_book_from_text(code.c_str(), nullptr, 0, &words, err, sizeof err);
+  if (rc != 0) {
+    fprintf(stderr, "%s\n", err);
+    exit(101);
+  }
+  std::vector<uint32_t> buf(words);
+  hvm_gb300_book_from_text(code.c_str(), buf.data(), buf.size(), &words, err, sizeof err);
+  return buf;
+}
+
+static void usage() {
+  fprintf(stderr,
+          "HVM2 on GB300\n"
+          "usage:\n"
+          "  hvm run-cu <file.hvm>       evaluate @main on the GPU\n"
+          "  hvm book <file.hvm> <out>   write the serialized book buffer\n");
+  exit(2);
+}
+
+int main(int argc, char** argv) {
+  if (argc < 3) usage();
+  std::string cmd = argv[1];
+  if (cmd == "run-cu") {
+    std::vector<uint32_t> buf = to_buffer(read_file(argv[2]));
+    hvm_cu(buf.data());
+    return 0;
+  }
+  if (cmd == "book" && argc == 4) {
+    std::vector<uint32_t> buf = to_buffer(read_file(argv[2]));
+    FILE* f = fopen(argv[3], "wb");
+    if (!f || fwrite(buf.data(), 4, buf.size(), f) != buf.size()) {
+      fprintf(stderr, "cannot write %s\n", argv[3]);
+      return 1;
+    }
+    fclose(f);
+    return 0;
+  }
+  usage();
+  return 2;
+}

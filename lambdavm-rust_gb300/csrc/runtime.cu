@@ -1,0 +1,719 @@
+// runtime.cu — GB300 HVM2 runtime: turn kernel, fixed scheduling policy,
+// host normalise/expand loop, readback, and the C ABI (`hvm_cu` and the
+// handle API declared in include/hvm_gb300.h).
+//
+// Execution model (sm_103a, one GPU):
+//   * One turn = one launch of `turn_kernel` over a grid sized to the SMs
+//     (every resident block runs once). A thread takes its share of the
+//     turn's input redexes from the global ring, then runs up to `budget`
+//     interactions from its shared-memory LIFO, claiming more input from the
+//     ring when its LIFO drains. Whatever is left, plus overflow, goes back to
+//     the ring tail for the next turn. This replaces the reference's
+//     evaluator/inbetween launch pair and its two blocking D2H copies per turn
+//     (src/hvm.cu:1810-1839): the last block to finish computes the next
+//     turn's input range and policy on the device, and the host only polls
+//     the control block after a batch of turns.
+//   * Termination: a turn that leaves no redex in the ring ends the
+//     normalisation (the reference stops when the global bag is empty).
+//   * The readback (`expand`, the lambda-encoded constructor walk of the IO
+//     loop, src/run.cu:67-97 / src/hvm.cu:1861-1893) runs on the host over
+//     single-word reads, and the final tree is serialised by one gather
+//     kernel instead of a device printf (src/hvm.cu:2290-2297).
+#include <cuda_runtime.h>
+#include <chrono>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "hvm_defs.h"
+#include "evaluator.cuh"
+#include "hvm_gb300.h"
+
+namespace hvm {
+
+static const char* status_text(uint32_t s) {
+  switch (s) {
+    case ST_OK: return "ok";
+    case ST_OOM_NODES: return "out of node memory";
+    case ST_OOM_VARS: return "out of var memory";
+    case ST_RING_FULL: return "redex ring overflow";
+    case ST_LINK_UNSET: return "link met an uninitialised var";
+    case ST_LINK_LIMIT: return "substitution chain too long";
+    case ST_BAD_REF: return "reference to a missing definition";
+    default: return "unknown device error";
+  }
+}
+
+// ---- turn kernel -------------------------------------------------------------------
+
+__device__ __forceinline__ unsigned long long ldcg64(const unsigned long long* p) { return __ldcg(p); }
+
+__device__ __forceinline__ bool claim(const Dev& d, TState& t, unsigned long long in_end, uint32_t chunk) {
+  if (ldcg64(&d.ctl->head) >= in_end) return false;
+  unsigned long long h = atomicAdd(&d.ctl->head, (unsigned long long)chunk);
+  if (h >= in_end) return false;
+  unsigned long long e = h + chunk < in_end ? h + chunk : in_end;
+  for (unsigned long long i = h; i < e; i++) {
+    push(d, t, (Pair)__ldcg((const unsigned long long*)&d.ring[i & d.ring_mask]));
+  }
+  return true;
+}
+
+__device__ __forceinline__ unsigned long long warp_sum(unsigned long long v) {
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xFFFFFFFFu, v, o);
+  return v;
+}
+
+// Fixed work-distribution policy (the GB300 counterpart of the reference's
+// SEED/GROW/WORK modes, src/hvm.cu:1509-1548): while the ring holds fewer
+// redexes than threads, turns are short so that fresh redexes are spread over
+// more threads every turn; once every thread has work, turns are long.
+__device__ void fixed_policy(Ctl* c, unsigned long long pending, uint32_t nthreads, uint32_t cap) {
+  uint32_t s, budget, chunk;
+  if (pending < nthreads) {
+    s = 1;
+    chunk = 1;
+    budget = pending * 64 < nthreads ? 32 : (pending * 8 < nthreads ? 128 : 512);
+  } else {
+    unsigned long long per = pending / nthreads;
+    s = (uint32_t)(per < cap / 2 ? per : cap / 2);
+    if (s == 0) s = 1;
+    chunk = 2;
+    budget = 4096;
+  }
+  c->static_per_thread = s;
+  c->budget = budget;
+  c->chunk = chunk;
+}
+
+__global__ void turn_kernel(Dev d, uint32_t cap) {
+  extern __shared__ unsigned long long smem_stack[];
+  Ctl* c = d.ctl;
+  const unsigned long long base = ldcg64(&c->base);
+  const unsigned long long in_end = ldcg64(&c->in_end);
+  if (base == in_end) return;  // normal form reached: nothing to do
+  if (__ldcg(&c->status) != 0) return;
+  const uint32_t s = __ldcg(&c->static_per_thread);
+  const uint32_t budget = __ldcg(&c->budget);
+  const uint32_t chunk = __ldcg(&c->chunk);
+
+  TState t;
+  t.stk = (Pair*)smem_stack + threadIdx.x;
+  t.stride = blockDim.x;
+  t.len = 0;
+  t.cap = cap;
+  t.gid = blockIdx.x * blockDim.x + threadIdx.x;
+  t.node_base = t.gid * d.node_slice;
+  t.vars_base = t.gid * d.vars_slice;
+  t.ncur = d.ncur[t.gid];
+  t.vcur = d.vcur[t.gid];
+  t.base = base;
+  t.itrs = t.leak = t.retries = 0;
+  for (int i = 0; i < 8; i++) t.hist[i] = 0;
+  t.dead = false;
+
+  // Static share of the input: items base + gid + k*N, k < s.
+  for (uint32_t k = 0; k < s; k++) {
+    unsigned long long at = base + t.gid + (unsigned long long)k * d.nthreads;
+    if (at >= in_end) break;
+    push(d, t, (Pair)__ldcg((const unsigned long long*)&d.ring[at & d.ring_mask]));
+  }
+
+  for (uint32_t left = budget; left > 0 && !t.dead; left--) {
+    if (t.len == 0 && !claim(d, t, in_end, chunk)) break;
+    t.len--;
+    Pair r = t.stk[(size_t)t.len * t.stride];
+    interact(d, t, r);
+  }
+
+  d.ncur[t.gid] = t.ncur;
+  d.vcur[t.gid] = t.vcur;
+
+  // Flush the LIFO to the ring tail, one atomic per warp.
+  __syncwarp();
+  const unsigned lane = threadIdx.x & 31;
+  uint32_t n = t.len, incl = n;
+  for (int o = 1; o < 32; o <<= 1) {
+    uint32_t y = __shfl_up_sync(0xFFFFFFFFu, incl, o);
+    if (lane >= (unsigned)o) incl += y;
+  }
+  uint32_t total = __shfl_sync(0xFFFFFFFFu, incl, 31);
+  unsigned long long wbase = 0;
+  if (lane == 31 && total) wbase = atomicAdd(&c->tail, (unsigned long long)total);
+  wbase = __shfl_sync(0xFFFFFFFFu, wbase, 31);
+  if (total) {
+    unsigned long long my = wbase + incl - n;
+    if (wbase + total - base > d.ring_mask + 1) {
+      if (lane == 0) set_status(d, ST_RING_FULL, 1);
+    } else {
+      for (uint32_t i = 0; i < n; i++) d.ring[(my + i) & d.ring_mask] = t.stk[(size_t)i * t.stride];
+      t.leak += n;
+    }
+  }
+
+  // Counters: one atomic per warp.
+  unsigned long long v;
+  v = warp_sum(t.itrs);    if (lane == 0 && v) atomicAdd(&c->itrs, v);
+  v = warp_sum(t.leak);    if (lane == 0 && v) atomicAdd(&c->leak, v);
+  v = warp_sum(t.retries); if (lane == 0 && v) atomicAdd(&c->retries, v);
+  for (int i = 0; i < 8; i++) {
+    v = warp_sum(t.hist[i]);
+    if (lane == 0 && v) atomicAdd(&c->hist[i], v);
+  }
+
+  // The last block to finish closes the turn and picks the next one.
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    __threadfence();
+    unsigned prev = atomicAdd(&c->blocks_done, 1u);
+    if (prev == gridDim.x - 1) {
+      __threadfence();
+      unsigned long long head = ldcg64(&c->head), tail = ldcg64(&c->tail);
+      unsigned long long nb = head < in_end ? head : in_end;
+      unsigned long long pending = tail - nb;
+      c->base = nb;
+      c->in_end = tail;
+      c->pending = pending;
+      c->turns += 1;
+      fixed_policy(c, pending, d.nthreads, cap);
+      unsigned long long take = (unsigned long long)c->static_per_thread * d.nthreads;
+      c->head = nb + (take < pending ? take : pending);
+      c->blocks_done = 0;
+      __threadfence();
+    }
+  }
+}
+
+// Starts a normalisation from `redex` (src/hvm.cu:1488-1497): sets ROOT to
+// NONE and makes `redex` the only input of the next turn.
+__global__ void boot_kernel(Dev d, Pair redex, uint32_t cap) {
+  Ctl* c = d.ctl;
+  d.vars[ROOT_VAR] = NONE;
+  unsigned long long at = c->tail;
+  d.ring[at & d.ring_mask] = redex;
+  c->base = at;
+  c->in_end = at + 1;
+  c->tail = at + 1;
+  c->pending = 1;
+  c->blocks_done = 0;
+  fixed_policy(c, 1, d.nthreads, cap);
+  c->head = at + 1;
+  __threadfence();
+}
+
+// Serialises the tree reachable from `root` in breadth-first order:
+// out[k] is a port with its var chain resolved; for a node port, kids[k] is
+// the index of its first child (the second child follows it). One block.
+__global__ void gather_kernel(Dev d, Port root, Port* out, uint32_t* kids, uint32_t cap, uint32_t* info) {
+  __shared__ uint32_t next, lo, hi, overflow;
+  auto resolve = [&](Port p) -> Port {
+    for (uint32_t g = 0; g < (1u << 20) && get_tag(p) == VAR; g++) {
+      Port v = __ldcg(&d.vars[get_val(p)]);
+      if (v == NONE || v == 0) break;
+      p = v;
+    }
+    return p;
+  };
+  if (threadIdx.x == 0) {
+    out[0] = resolve(root);
+    next = 1; lo = 0; hi = 1; overflow = 0;
+  }
+  __syncthreads();
+  while (lo < hi && !overflow) {
+    for (uint32_t k = lo + threadIdx.x; k < hi; k += blockDim.x) {
+      Port p = out[k];
+      if (is_nod(p)) {
+        uint32_t pos = atomicAdd(&next, 2u);
+        if (pos + 2 > cap) { overflow = 1; continue; }
+        Pair nd = (Pair)__ldcg((const unsigned long long*)&d.node[get_val(p)]);
+        out[pos] = resolve(get_fst(nd));
+        out[pos + 1] = resolve(get_snd(nd));
+        kids[k] = pos;
+      }
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) { lo = hi; hi = next < cap ? next : cap; }
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) { info[0] = next < cap ? next : cap; info[1] = overflow; }
+}
+
+// ---- host runtime ----------------------------------------------------------------
+
+#define CK(x) do { cudaError_t e_ = (x); if (e_ != cudaSuccess) { return fail(std::string(#x) + ": " + cudaGetErrorString(e_)); } } while (0)
+
+struct HostDef {
+  std::string name;
+  bool safe;
+  uint32_t rbag_len, node_len, vars_len;
+  Port root;
+  std::vector<Pair> rbag, node;
+};
+
+class Runtime {
+ public:
+  hvm_gb300_config cfg;
+  std::string err;
+  std::vector<HostDef> defs;
+  Dev d{};
+  Ctl* ctl = nullptr;
+  void* mem_node = nullptr; void* mem_vars = nullptr; void* mem_ring = nullptr;
+  void* mem_cur = nullptr; void* mem_scratch = nullptr;
+  void* mem_defs = nullptr; void* mem_book = nullptr;
+  Port* g_out = nullptr; uint32_t* g_kids = nullptr; uint32_t* g_info = nullptr;
+  uint32_t gather_cap = 0;
+  uint32_t grid = 0, block = 0, cap = 0;
+  size_t smem = 0;
+  uint32_t max_def_nodes = 1, max_def_vars = 1;
+  int sms = 0;
+  double norm_seconds = 0;
+  uint64_t norm_calls = 0;
+
+  ~Runtime() { release(); }
+
+  int fail(const std::string& m) { if (err.empty()) err = m; return -1; }
+
+  void release() {
+    void* ps[] = {mem_node, mem_vars, mem_ring, mem_cur, mem_scratch, mem_defs, mem_book, g_out, g_kids, g_info, ctl};
+    for (void* p : ps) if (p) cudaFree(p);
+    mem_node = mem_vars = mem_ring = mem_cur = mem_scratch = mem_defs = mem_book = nullptr;
+    g_out = nullptr; g_kids = nullptr; g_info = nullptr; ctl = nullptr;
+  }
+
+  int init(const hvm_gb300_config* c) {
+    hvm_gb300_default_config(&cfg);
+    if (c) cfg = *c;
+    CK(cudaSetDevice(cfg.device));
+    CK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, cfg.device));
+    block = cfg.threads_per_block;
+    cap = cfg.stack_cap;
+    if (block == 0 || block % 32 || block > 1024) return fail("threads_per_block must be a multiple of 32 in [32, 1024]");
+    if (cap == 0) return fail("stack_cap must be positive");
+    if (cfg.node_log2 < 10 || cfg.node_log2 > 29 || cfg.vars_log2 < 10 || cfg.vars_log2 > 29)
+      return fail("node_log2/vars_log2 must be in [10, 29]");
+    smem = (size_t)block * cap * sizeof(Pair);
+    CK(cudaFuncSetAttribute(turn_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    int per_sm = 0;
+    CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, turn_kernel, (int)block, smem));
+    if (per_sm <= 0) return fail("turn kernel does not fit on an SM with this block size / stack capacity");
+    if (cfg.blocks_per_sm && (int)cfg.blocks_per_sm < per_sm) per_sm = (int)cfg.blocks_per_sm;
+    grid = (uint32_t)(per_sm * sms);
+    uint32_t nthreads = grid * block;
+
+    uint64_t n_nodes = 1ull << cfg.node_log2, n_vars = 1ull << cfg.vars_log2;
+    // Slices exclude word 0 and the ROOT var at the top of the var space.
+    d.node_slice = (uint32_t)((n_nodes - 1) / nthreads);
+    d.vars_slice = (uint32_t)((n_vars - 2) / nthreads);
+    if (d.node_slice < 4 || d.vars_slice < 4) return fail("node/var space too small for the thread count");
+    d.nthreads = nthreads;
+
+    // The ROOT var is index 0x1FFFFFFF: the var array always spans 2^29 words
+    // of address space, but only the slices and ROOT are ever touched.
+    CK(cudaMalloc(&mem_node, n_nodes * sizeof(Pair)));
+    size_t vars_words = (size_t)1 << 29;
+    CK(cudaMalloc(&mem_vars, vars_words * sizeof(Port)));
+    uint64_t ring_len = 1ull << cfg.ring_log2;
+    CK(cudaMalloc(&mem_ring, ring_len * sizeof(Pair)));
+    CK(cudaMalloc(&mem_cur, 2ull * nthreads * sizeof(uint32_t)));
+    CK(cudaMalloc((void**)&ctl, sizeof(Ctl)));
+    d.node = (Pair*)mem_node;
+    d.vars = (Port*)mem_vars;
+    d.ring = (Pair*)mem_ring;
+    d.ring_mask = ring_len - 1;
+    d.ncur = (uint32_t*)mem_cur;
+    d.vcur = d.ncur + nthreads;
+    d.ctl = ctl;
+    return reset_net();
+  }
+
+  // Clears the whole net (node/var words, ring, cursors, counters).
+  int reset_net() {
+    CK(cudaMemset(mem_node, 0, (1ull << cfg.node_log2) * sizeof(Pair)));
+    // Only the slices and the ROOT word of the var space are used.
+    CK(cudaMemset(mem_vars, 0, ((size_t)d.vars_slice * d.nthreads + 1) * sizeof(Port)));
+    CK(cudaMemset((char*)mem_vars + (size_t)ROOT_VAR * sizeof(Port), 0, sizeof(Port)));
+    CK(cudaMemset(mem_cur, 0, 2ull * d.nthreads * sizeof(uint32_t)));
+    CK(cudaMemset(ctl, 0, sizeof(Ctl)));
+    std::vector<uint32_t> one(d.nthreads, 1);  // cursors start past word 0 like the reference
+    CK(cudaMemcpy(d.ncur, one.data(), d.nthreads * sizeof(uint32_t), cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(d.vcur, one.data(), d.nthreads * sizeof(uint32_t), cudaMemcpyHostToDevice));
+    norm_seconds = 0;
+    norm_calls = 0;
+    return 0;
+  }
+
+  // Parses the book buffer (src/hvm.c:1408-1453 limits and messages).
+  int load_book(const uint32_t* w, size_t words) {
+    defs.clear();
+    if (!w) return fail("null book buffer");
+    size_t at = 0;
+    auto need = [&](size_t k) { return words == 0 || at + k <= words; };
+    if (!need(1)) return fail("failed to load book");
+    uint32_t ndefs = w[at++];
+    if (ndefs == 0 || ndefs > MAX_DEFS) return fail("failed to load book");
+    defs.resize(ndefs);
+    std::vector<bool> seen(ndefs, false);
+    for (uint32_t k = 0; k < ndefs; k++) {
+      if (!need(DEF_HEADER_WORDS)) return fail("failed to load book");
+      uint32_t fid = w[at++];
+      if (fid >= ndefs) return fail("failed to load book");
+      HostDef& h = defs[fid];
+      char name[257];
+      memcpy(name, &w[at], 256);
+      name[256] = 0;
+      h.name = name;
+      at += 64;
+      h.safe = w[at++] != 0;
+      h.rbag_len = w[at++];
+      h.node_len = w[at++];
+      h.vars_len = w[at++];
+      if (h.rbag_len > DEF_RBAG_LEN) return fail("def '" + h.name + "' has too many redexes: " + std::to_string(h.rbag_len));
+      if (h.node_len > DEF_NODE_LEN) return fail("def '" + h.name + "' has too many nodes: " + std::to_string(h.node_len));
+      h.root = w[at++];
+      if (!need(2ull * (h.rbag_len + h.node_len))) return fail("failed to load book");
+      h.rbag.resize(h.rbag_len);
+      h.node.resize(h.node_len);
+      for (uint32_t i = 0; i < h.rbag_len; i++, at += 2) h.rbag[i] = new_pair(w[at], w[at + 1]);
+      for (uint32_t i = 0; i < h.node_len; i++, at += 2) h.node[i] = new_pair(w[at], w[at + 1]);
+      seen[fid] = true;
+    }
+    return upload_book();
+  }
+
+  int upload_book() {
+    std::vector<DefHdr> hdr(defs.size());
+    std::vector<Pair> flat;
+    max_def_nodes = 1;
+    max_def_vars = 1;
+    for (size_t f = 0; f < defs.size(); f++) {
+      HostDef& h = defs[f];
+      hdr[f] = DefHdr{h.node_len, h.rbag_len, h.vars_len, h.safe ? 1u : 0u, h.root, (uint32_t)flat.size(), 0, 0};
+      flat.insert(flat.end(), h.rbag.begin(), h.rbag.end());
+      flat.insert(flat.end(), h.node.begin(), h.node.end());
+      if (h.node_len > max_def_nodes) max_def_nodes = h.node_len;
+      if (h.vars_len > max_def_vars) max_def_vars = h.vars_len;
+    }
+    if (flat.empty()) flat.push_back(0);
+    if (mem_defs) cudaFree(mem_defs);
+    if (mem_book) cudaFree(mem_book);
+    if (mem_scratch) cudaFree(mem_scratch);
+    mem_defs = mem_book = mem_scratch = nullptr;
+    CK(cudaMalloc(&mem_defs, hdr.size() * sizeof(DefHdr)));
+    CK(cudaMalloc(&mem_book, flat.size() * sizeof(Pair)));
+    CK(cudaMemcpy(mem_defs, hdr.data(), hdr.size() * sizeof(DefHdr), cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(mem_book, flat.data(), flat.size() * sizeof(Pair), cudaMemcpyHostToDevice));
+    CK(cudaMalloc(&mem_scratch, (size_t)(max_def_nodes + max_def_vars) * d.nthreads * sizeof(uint32_t)));
+    d.defs = (const DefHdr*)mem_defs;
+    d.book = (const Pair*)mem_book;
+    d.ndefs = (uint32_t)defs.size();
+    d.nloc = (uint32_t*)mem_scratch;
+    d.vloc = d.nloc + (size_t)max_def_nodes * d.nthreads;
+    return 0;
+  }
+
+  int read_ctl(Ctl& h) {
+    CK(cudaMemcpy(&h, ctl, sizeof(Ctl), cudaMemcpyDeviceToHost));
+    return 0;
+  }
+
+  int boot(Pair redex) {
+    boot_kernel<<<1, 1>>>(d, redex, cap);
+    CK(cudaGetLastError());
+    return 0;
+  }
+
+  // Runs turns until the ring is empty (src/hvm.cu:1810-1839).
+  int normalize() {
+    auto t0 = std::chrono::steady_clock::now();
+    uint32_t batch = 4;
+    uint64_t turns_run = 0;
+    Ctl h;
+    for (;;) {
+      for (uint32_t i = 0; i < batch; i++) turn_kernel<<<grid, block, smem>>>(d, cap);
+      CK(cudaGetLastError());
+      turns_run += batch;
+      if (read_ctl(h)) return -1;
+      if (h.status) return fail(std::string("device error: ") + status_text(h.status) + " (info " + std::to_string(h.err_info) + ")");
+      if (h.base == h.in_end) break;
+      if (cfg.max_turns && turns_run >= cfg.max_turns) return fail("turn budget exhausted before normal form");
+      if (batch < 64) batch *= 2;
+    }
+    norm_seconds += std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+    norm_calls++;
+    return 0;
+  }
+
+  // Single-word device accessors for the host-side readback walk.
+  Port vars_load(uint32_t i) { Port v = 0; cudaMemcpy(&v, d.vars + i, sizeof(Port), cudaMemcpyDeviceToHost); return v; }
+  void vars_store(uint32_t i, Port v) { cudaMemcpy(d.vars + i, &v, sizeof(Port), cudaMemcpyHostToDevice); }
+  Pair node_load(uint32_t i) { Pair v = 0; cudaMemcpy(&v, d.node + i, sizeof(Pair), cudaMemcpyDeviceToHost); return v; }
+
+  // Read-only chase (src/hvm.c:781-790).
+  Port peek(Port p) {
+    while (get_tag(p) == VAR) {
+      Port v = vars_load(get_val(p));
+      if (v == NONE || v == 0) break;
+      p = v;
+    }
+    return p;
+  }
+
+  // Normalises every REF met by the readback (src/hvm.c:1233-1243).
+  int expand(Port p, Port* out) {
+    Port saved = vars_load(ROOT_VAR);
+    Port got = peek(p);
+    while (get_tag(got) == REF) {
+      if (boot(new_pair(got, ROOT)) || normalize()) return -1;
+      got = peek(vars_load(ROOT_VAR));
+    }
+    vars_store(ROOT_VAR, saved);
+    *out = got;
+    return 0;
+  }
+
+  struct Ctr { uint32_t tag; uint32_t nargs; Port args[16]; };
+
+  // Lambda-encoded constructor readback (src/run.c:65-97).
+  int read_ctr(Port p, Ctr& c) {
+    c.tag = (uint32_t)-1;
+    c.nargs = 0;
+    Port lam, app, arg;
+    if (expand(p, &lam)) return -1;
+    if (get_tag(lam) != CON) return 0;
+    Pair lam_n = node_load(get_val(lam));
+    if (expand(get_fst(lam_n), &app)) return -1;
+    if (get_tag(app) != CON) return 0;
+    Pair app_n = node_load(get_val(app));
+    if (expand(get_fst(app_n), &arg)) return -1;
+    if (get_tag(arg) != NUM) return 0;
+    c.tag = get_u24(get_val(arg));
+    for (;;) {
+      if (expand(get_snd(app_n), &app)) return -1;
+      if (get_tag(app) != CON) break;
+      app_n = node_load(get_val(app));
+      if (expand(get_fst(app_n), &arg)) return -1;
+      if (c.nargs < 16) c.args[c.nargs] = arg;
+      c.nargs++;
+    }
+    return 0;
+  }
+
+  // boot @main ~ ROOT, then the IO loop without IO builtins (src/run.cu:857-925).
+  int run_main() {
+    if (defs.empty()) return fail("no book loaded");
+    if (reset_net()) return -1;
+    if (boot(new_pair(new_port(REF, 0), ROOT))) return -1;
+    for (;;) {
+      if (normalize()) return -1;
+      Ctr c;
+      if (read_ctr(peek(ROOT), c)) return -1;
+      if (c.nargs < 1 || get_tag(c.args[0]) != CON) break;
+      Pair magic = node_load(get_val(c.args[0]));
+      if (get_val(get_fst(magic)) != new_u24(0xD0CA11) || get_val(get_snd(magic)) != new_u24(0xFF1FF1)) break;
+      if (c.tag == 1) fprintf(stderr, "IO calls are not supported by this runtime\n");
+      break;
+    }
+    return 0;
+  }
+
+  // Serialises the tree at ROOT and prints it in the reference's format
+  // (src/hvm.c:1535-1699).
+  int result_text(std::string& s) {
+    if (!g_info) {
+      gather_cap = 1u << 24;
+      CK(cudaMalloc((void**)&g_out, gather_cap * sizeof(Port)));
+      CK(cudaMalloc((void**)&g_kids, gather_cap * sizeof(uint32_t)));
+      CK(cudaMalloc((void**)&g_info, 2 * sizeof(uint32_t)));
+    }
+    gather_kernel<<<1, 1024>>>(d, ROOT, g_out, g_kids, gather_cap, g_info);
+    CK(cudaGetLastError());
+    uint32_t info[2];
+    CK(cudaMemcpy(info, g_info, sizeof(info), cudaMemcpyDeviceToHost));
+    if (info[1]) return fail("result tree larger than the readback buffer");
+    std::vector<Port> out(info[0]);
+    std::vector<uint32_t> kids(info[0]);
+    CK(cudaMemcpy(out.data(), g_out, info[0] * sizeof(Port), cudaMemcpyDeviceToHost));
+    CK(cudaMemcpy(kids.data(), g_kids, info[0] * sizeof(uint32_t), cudaMemcpyDeviceToHost));
+    s.clear();
+    // Iterative pre-order print; values < 0x100 on the stack are literal chars.
+    std::vector<uint64_t> stack;
+    stack.push_back(0);
+    const uint64_t CHAR = 1ull << 40;
+    char buf[64];
+    while (!stack.empty()) {
+      uint64_t top = stack.back();
+      stack.pop_back();
+      if (top & CHAR) { s.push_back((char)(top & 0xFF)); continue; }
+      uint32_t k = (uint32_t)top;
+      Port p = out[k];
+      Tag tag = get_tag(p);
+      switch (tag) {
+        case CON: case DUP: case OPR: case SWI: {
+          static const char* open[] = {"(", "{", "$(", "?("};
+          static const char close[] = {')', '}', ')', ')'};
+          s += open[tag - CON];
+          stack.push_back(CHAR | (uint64_t)(unsigned char)close[tag - CON]);
+          stack.push_back(kids[k] + 1);
+          stack.push_back(CHAR | (uint64_t)' ');
+          stack.push_back(kids[k]);
+          break;
+        }
+        case ERA: s += "*"; break;
+        case VAR: snprintf(buf, sizeof buf, "x%x", get_val(p)); s += buf; break;
+        case NUM: print_numb(get_val(p), s); break;
+        case REF: {
+          uint32_t fid = get_val(p) & 0xFFFFFFFu;
+          s += "@";
+          s += fid < defs.size() ? defs[fid].name : std::string("?");
+          break;
+        }
+      }
+    }
+    return 0;
+  }
+
+  static void print_numb(Numb w, std::string& s) {
+    static const char* syms[] = {
+      "[u24]", "[i24]", "[f24]", "[+]", "[-]", "[:-]", "[*]", "[/]", "[:/]", "[%]", "[:%]",
+      "[=]", "[!]", "[<]", "[>]", "[&]", "[|]", "[^]", "[<<]", "[:<<]", "[>>]", "[:>>]"};
+    static const char* ops[] = {
+      "+", "-", ":-", "*", "/", ":/", "%", ":%", "=", "!", "<", ">", "&", "|", "^", "<<", ":<<", ">>", ":>>"};
+    char b[64];
+    uint32_t t = get_typ(w);
+    if (t == TY_SYM) {
+      uint32_t k = get_sym(w);
+      s += (k >= 1 && k <= 22) ? syms[k - 1] : "[?]";
+    } else if (t == TY_U24) {
+      snprintf(b, sizeof b, "%u", get_u24(w)); s += b;
+    } else if (t == TY_I24) {
+      snprintf(b, sizeof b, "%+d", get_i24(w)); s += b;
+    } else if (t == TY_F24) {
+      float f = get_f24(w);
+      if (isinf(f)) s += signbit(f) ? "-inf" : "+inf";
+      else if (isnan(f)) s += "+NaN";
+      else { snprintf(b, sizeof b, "%.7e", f); s += b; }
+    } else {
+      snprintf(b, sizeof b, "[%s0x%07X]", (t >= OP_ADD && t <= FP_SHR) ? ops[t - OP_ADD] : "?", get_u24(w));
+      s += b;
+    }
+  }
+
+  int stats(hvm_gb300_stats* st) {
+    Ctl h;
+    if (read_ctl(h)) return -1;
+    memset(st, 0, sizeof(*st));
+    st->itrs = h.itrs;
+    st->leak = h.leak;
+    st->turns = h.turns;
+    st->retries = h.retries;
+    for (int i = 0; i < 8; i++) st->rule_hist[i] = h.hist[i];
+    st->seconds = norm_seconds;
+    st->threads = d.nthreads;
+    st->grid = grid;
+    st->block = block;
+    return 0;
+  }
+};
+
+}  // namespace hvm
+
+// ---- C ABI ---------------------------------------------------------------------------
+
+struct hvm_gb300_runtime {
+  hvm::Runtime rt;
+};
+
+extern "C" void hvm_gb300_default_config(hvm_gb300_config* c) {
+  memset(c, 0, sizeof(*c));
+  c->device = 0;
+  c->threads_per_block = 128;
+  c->stack_cap = 64;
+  c->blocks_per_sm = 0;
+  c->node_log2 = 29;
+  c->vars_log2 = 29;
+  c->ring_log2 = 26;
+  c->max_turns = 0;
+}
+
+extern "C" int hvm_gb300_create(const hvm_gb300_config* cfg, hvm_gb300_runtime** out) {
+  if (!out) return -1;
+  *out = nullptr;
+  hvm_gb300_runtime* r = new hvm_gb300_runtime();
+  int rc = r->rt.init(cfg);
+  *out = r;
+  return rc;
+}
+
+extern "C" void hvm_gb300_destroy(hvm_gb300_runtime* r) { delete r; }
+
+extern "C" const char* hvm_gb300_error(const hvm_gb300_runtime* r) {
+  return r ? r->rt.err.c_str() : "null runtime";
+}
+
+extern "C" int hvm_gb300_load_book(hvm_gb300_runtime* r, const uint32_t* book, size_t words) {
+  if (!r) return -1;
+  r->rt.err.clear();
+  return r->rt.load_book(book, words);
+}
+
+extern "C" int hvm_gb300_run(hvm_gb300_runtime* r, hvm_gb300_stats* stats) {
+  if (!r) return -1;
+  r->rt.err.clear();
+  if (r->rt.run_main()) return -1;
+  if (stats && r->rt.stats(stats)) return -1;
+  return 0;
+}
+
+extern "C" int hvm_gb300_result(hvm_gb300_runtime* r, char* out, size_t cap, size_t* len) {
+  if (!r) return -1;
+  std::string s;
+  if (r->rt.result_text(s)) return -1;
+  if (len) *len = s.size();
+  if (out) {
+    if (cap <= s.size()) { r->rt.fail("result buffer too small"); return -2; }
+    memcpy(out, s.data(), s.size());
+    out[s.size()] = 0;
+  }
+  return 0;
+}
+
+// Drop-in for the reference's CUDA entry point (src/hvm.cu:2320-2397): loads
+// the book, normalises @main and prints `Result:`, `- ITRS`, `- LEAK`,
+// `- TIME` and `- MIPS` on stdout.
+extern "C" void hvm_cu(const uint32_t* book_buffer) {
+  hvm_gb300_runtime* r = nullptr;
+  if (hvm_gb300_create(nullptr, &r) != 0) {
+    fprintf(stderr, "Failed to initialise the GB300 runtime: %s\n", r ? hvm_gb300_error(r) : "?");
+    hvm_gb300_destroy(r);
+    exit(EXIT_FAILURE);
+  }
+  if (hvm_gb300_load_book(r, book_buffer, 0) != 0) {
+    fprintf(stderr, "%s\n", hvm_gb300_error(r));
+    fprintf(stderr, "failed to load book\n");
+    hvm_gb300_destroy(r);
+    return;
+  }
+  auto t0 = std::chrono::steady_clock::now();
+  hvm_gb300_stats st;
+  if (hvm_gb300_run(r, &st) != 0) {
+    fprintf(stderr, "Failed to run the net: %s\n", hvm_gb300_error(r));
+    hvm_gb300_destroy(r);
+    exit(EXIT_FAILURE);
+  }
+  double secs = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+  std::string s;
+  if (r->rt.result_text(s) != 0) {
+    fprintf(stderr, "Failed to read back the result: %s\n", hvm_gb300_error(r));
+    hvm_gb300_destroy(r);
+    exit(EXIT_FAILURE);
+  }
+  printf("Result: %s\n", s.c_str());
+  printf("- ITRS: %llu\n", (unsigned long long)st.itrs);
+  printf("- LEAK: %llu\n", (unsigned long long)st.leak);
+  printf("- TIME: %.2fs\n", secs);
+  printf("- MIPS: %.2f\n", (double)st.itrs / secs / 1000000.0);
+  fflush(stdout);
+  hvm_gb300_destroy(r);
+}

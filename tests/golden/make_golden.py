@@ -1,0 +1,120 @@
+"""Generates the golden fixtures of the parity tests (run here, where the
+reference sources exist; the fixtures travel, the reference does not).
+
+  reference_programs.json  every non-IO `.hvm` program of the reference's test
+                           suite (tests/programs/**, examples/**) with
+                           - the snapshot's expected `Result:` line
+                             (tests/snapshots/*.snap, produced by `hvm run`),
+                           - the `Result:` line and `- ITRS:` count printed
+                             by the reference's own C runtime (`hvm run-c`,
+                             built in place by oracle/Makefile as
+                             oracle/_ref/hvm_ref) on this repository's book
+                             buffer.
+  configs.json             the same two fields for the seeded benchmark
+                           workloads (lambdavm-rust_gb300/workloads.py), with
+                           large results stored as a SHA-256 of their
+                           canonical form.
+
+Usage: python tests/golden/make_golden.py [--reference /root/reference]
+"""
+from __future__ import annotations
+
+import argparse
+import glob
+import hashlib
+import importlib
+import json
+import os
+import re
+import subprocess
+import sys
+import tempfile
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, ROOT)
+H = importlib.import_module("lambdavm-rust_gb300")
+W = importlib.import_module("lambdavm-rust_gb300.workloads")
+REF_BIN = os.path.join(ROOT, "oracle", "_ref", "hvm_ref")
+
+
+def run_ref(code: str) -> dict:
+    buf = H.book_from_text(code)
+    with tempfile.NamedTemporaryFile(suffix=".bin", delete=False) as f:
+        buf.tofile(f.name)
+        path = f.name
+    try:
+        r = subprocess.run([REF_BIN, path], capture_output=True, text=True, timeout=3600)
+    finally:
+        os.unlink(path)
+    res = re.search(r"^Result: (.*)$", r.stdout, re.M)
+    itrs = re.search(r"^- ITRS: (\d+)$", r.stdout, re.M)
+    if r.returncode != 0 or not res or not itrs:
+        raise RuntimeError(f"reference run failed: rc={r.returncode}\n{r.stdout[-2000:]}\n{r.stderr[-2000:]}")
+    return {"result": res.group(1), "itrs": int(itrs.group(1))}
+
+
+def snapshot_result(ref: str, rel: str) -> str | None:
+    key = rel.replace("tests/programs/", "").replace("examples/", "").replace("/", "__")
+    for snap in glob.glob(os.path.join(ref, "tests", "snapshots", "*.snap")):
+        if os.path.basename(snap) in (f"run__file@{key}.snap",):
+            body = open(snap).read().split("---\n", 2)[-1]
+            m = re.search(r"^Result: (.*)$", body, re.M)
+            return m.group(1) if m else body.strip()
+    return None
+
+
+def main() -> None:
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--reference", default="/root/reference")
+    ap.add_argument("--skip-configs", action="store_true")
+    args = ap.parse_args()
+    subprocess.run(["make", "-C", os.path.join(ROOT, "oracle"), "ref", f"REF_SRC={args.reference}/src"], check=True)
+
+    progs = []
+    files = sorted(glob.glob(os.path.join(args.reference, "tests", "programs", "**", "*.hvm"), recursive=True)
+                   + glob.glob(os.path.join(args.reference, "examples", "**", "*.hvm"), recursive=True))
+    for path in files:
+        rel = os.path.relpath(path, args.reference)
+        code = open(path).read()
+        if "@test-io = 1" in code or "@test-skip = 1" in code or "/io/" in rel or "demo_io" in rel:
+            continue  # IO builtins are outside the evaluator path
+        entry = {"name": rel, "code": code, "snapshot": snapshot_result(args.reference, rel)}
+        try:
+            entry.update(run_ref(code))
+        except H.HvmError as e:
+            entry.update({"build_error": str(e)})
+        except RuntimeError as e:
+            entry.update({"ref_error": str(e)})
+        progs.append(entry)
+        print(rel, entry.get("itrs"), entry.get("build_error", ""))
+    with open(os.path.join(HERE, "reference_programs.json"), "w") as f:
+        json.dump(progs, f, indent=1)
+
+    if args.skip_configs:
+        return
+    cases = {
+        "tree_sum_d12": W.tree_sum(12),
+        "tree_sum_d20": W.tree_sum(20),
+        "bitonic_sort_2p8": W.bitonic_sort(8),
+        "bitonic_sort_2p12": W.bitonic_sort(12),
+        "bitonic_sort_2p16": W.bitonic_sort(16),
+        "skewed_fold_2p10": W.skewed_fold(10),
+        "skewed_fold_2p18": W.skewed_fold(18),
+        "countdown_100000": W.countdown(100000),
+    }
+    out = {}
+    for name, code in cases.items():
+        r = run_ref(code)
+        canon = H.canonical(r["result"])
+        entry = {"itrs": r["itrs"], "canonical_sha256": hashlib.sha256(canon.encode()).hexdigest()}
+        if len(r["result"]) <= 4096:
+            entry["result"] = r["result"]
+        out[name] = entry
+        print(name, entry["itrs"])
+    with open(os.path.join(HERE, "configs.json"), "w") as f:
+        json.dump(out, f, indent=1)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,44 @@
+"""The C-ABI library loads and exports every symbol include/hvm_gb300.h
+declares (no device calls: this runs without a GPU)."""
+from __future__ import annotations
+
+import ctypes
+import os
+import re
+import subprocess
+
+from conftest import ROOT
+
+
+def declared_functions() -> set[str]:
+    text = open(os.path.join(ROOT, "include", "hvm_gb300.h")).read()
+    text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+    return set(re.findall(r"\b(hvm_\w+)\s*\(", text))
+
+
+def test_header_matches_exports(hvm):
+    decl = declared_functions()
+    assert decl == set(hvm.EXPORTED_SYMBOLS)
+    L = ctypes.CDLL(hvm.LIB_PATH)
+    for name in decl:
+        assert hasattr(L, name), name
+    nm = subprocess.run(["nm", "-D", "--defined-only", hvm.LIB_PATH], capture_output=True, text=True).stdout
+    exported = set(re.findall(r" T (\w+)$", nm, re.M))
+    assert decl <= exported
+
+
+def test_default_config(hvm):
+    cfg = hvm.Config()
+    hvm.lib().hvm_gb300_default_config(ctypes.byref(cfg))
+    assert cfg.threads_per_block % 32 == 0
+    assert cfg.node_log2 <= 29 and cfg.vars_log2 <= 29
+    assert cfg.stack_cap > 0
+
+
+def test_cli_book_matches_library(hvm, tmp_path):
+    src = tmp_path / "p.hvm"
+    src.write_text("@main = a & @f ~ (1 a)\n@f = (x x)\n")
+    out = tmp_path / "p.bin"
+    subprocess.run([hvm.CLI_PATH, "book", str(src), str(out)], check=True)
+    import numpy as np
+    assert np.array_equal(np.fromfile(out, dtype=np.uint32), hvm.book_from_text(src.read_text()))

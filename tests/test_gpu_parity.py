@@ -1,0 +1,113 @@
+"""Parity of the sm_103a evaluator with the oracle and the reference's
+goldens: bit-exact normal form (canonical tree: structure, REF names, 29-bit
+numbers) and identical interaction count. All calls go through the C ABI."""
+from __future__ import annotations
+
+import hashlib
+import re
+import subprocess
+
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def rt(hvm):
+    r = hvm.Runtime(device=0)
+    yield r
+    r.close()
+
+
+def run(rt, code):
+    rt.load(code)
+    st = rt.run()
+    return rt.result(), st
+
+
+def test_reference_programs(hvm, rt, ref_programs):
+    n = 0
+    for p in ref_programs:
+        if "result" not in p:
+            continue
+        res, st = run(rt, p["code"])
+        assert st.itrs == p["itrs"], p["name"]
+        assert hvm.canonical(res) == hvm.canonical(p["result"]), p["name"]
+        n += 1
+    assert n >= 12
+
+
+@pytest.mark.parametrize("name", ["tree_sum_d12", "bitonic_sort_2p8", "bitonic_sort_2p12",
+                                  "skewed_fold_2p10", "countdown_100000"])
+def test_configs_small(hvm, rt, workloads, config_goldens, name):
+    makers = {
+        "tree_sum_d12": lambda: workloads.tree_sum(12),
+        "bitonic_sort_2p8": lambda: workloads.bitonic_sort(8),
+        "bitonic_sort_2p12": lambda: workloads.bitonic_sort(12),
+        "skewed_fold_2p10": lambda: workloads.skewed_fold(10),
+        "countdown_100000": lambda: workloads.countdown(100000),
+    }
+    res, st = run(rt, makers[name]())
+    g = config_goldens[name]
+    assert st.itrs == g["itrs"]
+    assert hashlib.sha256(hvm.canonical(res).encode()).hexdigest() == g["canonical_sha256"]
+
+
+def test_live_oracle_seeded_nets(hvm, rt, workloads, oracle):
+    # Seeded nets the goldens do not hold: compared with the oracle live.
+    for seed in (1, 2, 3):
+        code = workloads.bitonic_sum(7, seed)
+        want = oracle(code, threads=2)
+        res, st = run(rt, code)
+        assert st.itrs == want["itrs"]
+        assert hvm.canonical(res) == hvm.canonical(want["result"])
+
+
+def test_repeat_runs_identical(hvm, rt, workloads):
+    code = workloads.bitonic_sort(10)
+    outs = {run(rt, code)[0] for _ in range(3)}
+    canon = {hvm.canonical(o) for o in outs}
+    assert len(canon) == 1
+
+
+@pytest.mark.slow
+@pytest.mark.parametrize("name", ["tree_sum_d20", "bitonic_sort_2p16", "skewed_fold_2p18"])
+def test_configs_full(hvm, rt, workloads, config_goldens, name):
+    makers = {
+        "tree_sum_d20": lambda: workloads.tree_sum(20),
+        "bitonic_sort_2p16": lambda: workloads.bitonic_sort(16),
+        "skewed_fold_2p18": lambda: workloads.skewed_fold(18),
+    }
+    res, st = run(rt, makers[name]())
+    g = config_goldens[name]
+    assert st.itrs == g["itrs"]
+    assert hashlib.sha256(hvm.canonical(res).encode()).hexdigest() == g["canonical_sha256"]
+    if name.startswith("bitonic"):
+        # size-independent property: the leaves are the sorted input keys
+        got = [int(x) for x in re.findall(r"\d+", res)]
+        assert got == sorted(workloads.pcg_keys(1 << 16))
+
+
+def test_hvm_cu_cli(hvm, tmp_path, workloads):
+    src = tmp_path / "t.hvm"
+    src.write_text(workloads.tree_sum(10))
+    out = subprocess.run([hvm.CLI_PATH, "run-cu", str(src)], capture_output=True, text=True, check=True).stdout
+    lines = out.strip().splitlines()
+    assert lines[0] == "Result: 1024"
+    assert lines[1] == "- ITRS: 16374"
+    assert lines[2].startswith("- LEAK: ")
+    assert re.match(r"- TIME: \d+\.\d\ds", lines[3])
+    assert lines[4].startswith("- MIPS: ")
+
+
+def test_errors_are_reported_not_hung(hvm, workloads):
+    # A node space too small for the net ends in an error status, not a hang.
+    with hvm.Runtime(device=0, node_log2=15, threads_per_block=32, blocks_per_sm=1) as r:
+        r.load(workloads.tree_sum(18))
+        with pytest.raises(hvm.HvmError, match="out of node memory|ring"):
+            r.run()
+    # A turn budget that ends before the normal form is reported.
+    with hvm.Runtime(device=0, max_turns=1) as r:
+        r.load(workloads.countdown(100000))
+        with pytest.raises(hvm.HvmError, match="turn budget"):
+            r.run()
