@@ -160,7 +160,7 @@ __device__ __forceinline__ uint32_t alloc_var(const Dev& d, TState& t, uint32_t&
 
 // Follows a var chain, consuming every resolved var on the way.
 __device__ __forceinline__ Port enter(const Dev& d, Port p) {
-  while (get_tag(p) == VAR) {
+  for (uint32_t guard = 0; guard < (1u << 24) && get_tag(p) == VAR; guard++) {
     Port v = vexch(d, get_val(p), NONE);
     if (v == NONE || v == 0) break;
     vstore(d, get_val(p), 0);

@@ -379,6 +379,24 @@ class Runtime {
       for (uint32_t i = 0; i < h.node_len; i++, at += 2) h.node[i] = new_pair(w[at], w[at + 1]);
       seen[fid] = true;
     }
+    // Every def-local port must point inside its def and every REF at a def
+    // of this book, so that the device never indexes past its arrays. The
+    // reference does not check; a book from the front-end always passes.
+    for (uint32_t f = 0; f < ndefs; f++) {
+      if (!seen[f]) return fail("failed to load book: missing definition " + std::to_string(f));
+      const HostDef& h = defs[f];
+      auto ok = [&](Port p) {
+        Tag t = get_tag(p);
+        if (t >= CON) return get_val(p) < h.node_len;
+        if (t == VAR) return get_val(p) < h.vars_len;
+        if (t == REF) return (get_val(p) & 0xFFFFFFFu) < ndefs;
+        return true;
+      };
+      bool good = ok(h.root);
+      for (Pair p : h.rbag) good = good && ok(get_fst(p)) && ok(get_snd(p));
+      for (Pair p : h.node) good = good && ok(get_fst(p)) && ok(get_snd(p));
+      if (!good) return fail("failed to load book: def '" + h.name + "' has a port outside the def");
+    }
     return upload_book();
   }
 
@@ -428,7 +446,8 @@ class Runtime {
   int normalize() {
     auto t0 = std::chrono::steady_clock::now();
     uint32_t batch = 4;
-    uint64_t turns_run = 0;
+    uint64_t turns_run = 0, stalled_turns = 0;
+    unsigned long long last_itrs = ~0ull, last_pending = ~0ull;
     Ctl h;
     for (;;) {
       for (uint32_t i = 0; i < batch; i++) turn_kernel<<<grid, block, smem>>>(d, cap);
@@ -438,6 +457,15 @@ class Runtime {
       if (h.status) return fail(std::string("device error: ") + status_text(h.status) + " (info " + std::to_string(h.err_info) + ")");
       if (h.base == h.in_end) break;
       if (cfg.max_turns && turns_run >= cfg.max_turns) return fail("turn budget exhausted before normal form");
+      // A net whose interaction count stops moving while redexes remain is
+      // stuck (e.g. a redex that never becomes available): report it.
+      if (h.itrs == last_itrs && h.pending == last_pending) {
+        if (++stalled_turns > 4096) return fail("no progress: interaction count stalled with redexes pending");
+      } else {
+        stalled_turns = 0;
+      }
+      last_itrs = h.itrs;
+      last_pending = h.pending;
       if (batch < 64) batch *= 2;
     }
     norm_seconds += std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
