@@ -71,6 +71,8 @@ typedef struct {
   uint32_t vars_log2;         /* var space 2^k words (k <= 29) */
   uint32_t ring_log2;         /* global redex ring 2^k entries */
   uint32_t max_turns;         /* 0 = unbounded; else fail after this many turns */
+  uint32_t stop_frac_q8;      /* a turn ends once busy threads < (1 - f/256) x initially busy */
+  uint32_t trace_cap;         /* record up to this many turns (0 = off), see hvm_gb300_trace */
 } hvm_gb300_config;
 
 typedef struct {
@@ -101,6 +103,23 @@ int hvm_gb300_run(hvm_gb300_runtime* rt, hvm_gb300_stats* stats);
 /* The normal form at ROOT in the reference's printed format (without the
  * "Result: " prefix). `out == NULL` queries the length (excluding the NUL). */
 int hvm_gb300_result(hvm_gb300_runtime* rt, char* out, size_t cap, size_t* len);
+
+/* One evaluator turn as recorded on the device (no reference counterpart:
+ * the reference's per-turn state is only visible through printf debugging,
+ * src/hvm.cu:1729-1740). */
+typedef struct {
+  uint64_t t_ns;        /* device clock when the turn closed */
+  uint64_t itrs;        /* cumulative interactions */
+  uint64_t pending;     /* redexes left for the next turn */
+  uint32_t dry;         /* threads that ran out of work */
+  uint32_t stopped;     /* 1 if the turn was ended by the dry rule */
+  uint32_t budget;      /* interactions per thread allowed in the turn */
+  uint32_t per_thread;  /* input redexes each thread took at the start */
+} hvm_gb300_turn;
+
+/* Copies up to `cap` turn records of the last run (needs trace_cap > 0);
+ * `*n` receives how many exist. */
+int hvm_gb300_trace(hvm_gb300_runtime* rt, hvm_gb300_turn* out, size_t cap, size_t* n);
 
 /* Last error message of `rt` ("" if none). */
 const char* hvm_gb300_error(const hvm_gb300_runtime* rt);

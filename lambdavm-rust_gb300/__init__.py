@@ -39,6 +39,20 @@ class Config(ctypes.Structure):
         ("vars_log2", ctypes.c_uint32),
         ("ring_log2", ctypes.c_uint32),
         ("max_turns", ctypes.c_uint32),
+        ("stop_frac_q8", ctypes.c_uint32),
+        ("trace_cap", ctypes.c_uint32),
+    ]
+
+
+class Turn(ctypes.Structure):
+    _fields_ = [
+        ("t_ns", ctypes.c_uint64),
+        ("itrs", ctypes.c_uint64),
+        ("pending", ctypes.c_uint64),
+        ("dry", ctypes.c_uint32),
+        ("stopped", ctypes.c_uint32),
+        ("budget", ctypes.c_uint32),
+        ("per_thread", ctypes.c_uint32),
     ]
 
 
@@ -68,6 +82,7 @@ EXPORTED_SYMBOLS = (
     "hvm_gb300_load_book",
     "hvm_gb300_run",
     "hvm_gb300_result",
+    "hvm_gb300_trace",
     "hvm_gb300_error",
     "hvm_gb300_destroy",
 )
@@ -96,6 +111,8 @@ def lib() -> ctypes.CDLL:
     L.hvm_gb300_run.argtypes = [ctypes.c_void_p, ctypes.POINTER(_Stats)]
     L.hvm_gb300_result.argtypes = [ctypes.c_void_p, ctypes.c_char_p, ctypes.c_size_t,
                                    ctypes.POINTER(ctypes.c_size_t)]
+    L.hvm_gb300_trace.argtypes = [ctypes.c_void_p, ctypes.POINTER(Turn), ctypes.c_size_t,
+                                  ctypes.POINTER(ctypes.c_size_t)]
     L.hvm_gb300_error.argtypes = [ctypes.c_void_p]
     L.hvm_gb300_error.restype = ctypes.c_char_p
     L.hvm_gb300_destroy.argtypes = [ctypes.c_void_p]
@@ -201,6 +218,14 @@ class Runtime:
         out = ctypes.create_string_buffer(n.value + 1)
         self._check(lib().hvm_gb300_result(self._h, out, n.value + 1, ctypes.byref(n)))
         return out.value.decode()
+
+    def trace(self) -> list[dict]:
+        """Per-turn records of the last run (needs trace_cap > 0)."""
+        n = ctypes.c_size_t()
+        self._check(lib().hvm_gb300_trace(self._h, None, 0, ctypes.byref(n)))
+        arr = (Turn * max(1, n.value))()
+        self._check(lib().hvm_gb300_trace(self._h, arr, n.value, ctypes.byref(n)))
+        return [{k: getattr(arr[i], k) for k, _ in Turn._fields_} for i in range(n.value)]
 
     def close(self) -> None:
         if getattr(self, "_h", None):

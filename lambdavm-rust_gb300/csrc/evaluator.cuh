@@ -41,6 +41,15 @@ struct DefHdr {
   uint32_t root, off, pad0, pad1;
 };
 
+// One record per completed turn, written by the turn's last block.
+struct TurnRecord {
+  unsigned long long t_ns;          // %globaltimer when the turn closed
+  unsigned long long itrs;          // cumulative interactions
+  unsigned long long pending;       // redexes in the ring for the next turn
+  unsigned int dry, stopped;        // dry threads at close; 1 if ended by the dry rule
+  unsigned int budget, per_thread;  // the closed turn's budget and static share
+};
+
 // Control block of one net. Hot atomics sit on separate 128-byte lines.
 struct alignas(128) Ctl {
   unsigned long long head;          // next dynamically claimable ring index
@@ -54,6 +63,12 @@ struct alignas(128) Ctl {
   unsigned long long retries;       // availability re-tries (diagnostic)
   unsigned long long turns;         // completed turns
   unsigned long long pending;       // redexes left after the last turn
+  unsigned long long pad_p[7];
+  unsigned int dry;                 // threads that ran out of work this turn
+  unsigned int stop;                // set once enough threads are dry: end the turn
+  unsigned int stop_at;             // dry count that sets `stop`
+  unsigned int stop_frac_q8;        // end a turn once busy < (1 - frac) * initially busy
+  unsigned int pad_s[28];
   unsigned int blocks_done;
   unsigned int status;
   unsigned int err_info;
@@ -63,12 +78,16 @@ struct alignas(128) Ctl {
   unsigned int policy;              // 0 = fixed policy
   unsigned int pad_c[1];
   unsigned long long hist[8];       // interactions per rule (diagnostic)
+  TurnRecord* trace;                // per-turn records (null = off)
+  unsigned int trace_cap;
 };
 
 // Everything a turn kernel needs; passed by value.
 struct Dev {
   Pair* node;                 // node words, 2^k entries
-  Port* vars;                 // var words, 2^k entries (ROOT_VAR is the last)
+  Port* vars;                 // var words, 2^k entries; var v lives at v & vars_mask,
+                              // so ROOT (0x1FFFFFFF) lands on the last word
+  uint32_t vars_mask;
   Pair* ring;                 // global redex ring
   unsigned long long ring_mask;
   uint32_t node_slice, vars_slice;   // words per thread slice
@@ -91,9 +110,9 @@ __device__ __forceinline__ Pair nload(const Dev& d, uint32_t i) {
 __device__ __forceinline__ void nstore(const Dev& d, uint32_t i, Pair p) {
   __stcg((unsigned long long*)&d.node[i], (unsigned long long)p);
 }
-__device__ __forceinline__ Port vload(const Dev& d, uint32_t i) { return __ldcg(&d.vars[i]); }
-__device__ __forceinline__ void vstore(const Dev& d, uint32_t i, Port p) { __stcg(&d.vars[i], p); }
-__device__ __forceinline__ Port vexch(const Dev& d, uint32_t i, Port p) { return atomicExch(&d.vars[i], p); }
+__device__ __forceinline__ Port vload(const Dev& d, uint32_t i) { return __ldcg(&d.vars[i & d.vars_mask]); }
+__device__ __forceinline__ void vstore(const Dev& d, uint32_t i, Port p) { __stcg(&d.vars[i & d.vars_mask], p); }
+__device__ __forceinline__ Port vexch(const Dev& d, uint32_t i, Port p) { return atomicExch(&d.vars[i & d.vars_mask], p); }
 
 __device__ __forceinline__ void set_status(const Dev& d, uint32_t code, uint32_t info) {
   if (atomicCAS(&d.ctl->status, 0u, code) == 0u) d.ctl->err_info = info;

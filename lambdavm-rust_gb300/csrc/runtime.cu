@@ -67,22 +67,30 @@ __device__ __forceinline__ unsigned long long warp_sum(unsigned long long v) {
 }
 
 // Fixed work-distribution policy (the GB300 counterpart of the reference's
-// SEED/GROW/WORK modes, src/hvm.cu:1509-1548): while the ring holds fewer
-// redexes than threads, turns are short so that fresh redexes are spread over
-// more threads every turn; once every thread has work, turns are long.
-__device__ void fixed_policy(Ctl* c, unsigned long long pending, uint32_t nthreads, uint32_t cap) {
+// SEED/GROW/WORK modes, src/hvm.cu:1509-1548). While the ring holds fewer
+// redexes than threads, turns are short so fresh redexes spread over more
+// threads each turn; if the ring stops growing (sequential work), the turn
+// budget doubles so a lone chain is not cut into tiny turns. Once every
+// thread has work, a turn runs until too many threads have run dry (`stop`),
+// and its leftovers are then redistributed evenly.
+__device__ void fixed_policy(Ctl* c, unsigned long long pending, unsigned long long prev_pending,
+                             uint32_t nthreads, uint32_t cap) {
   uint32_t s, budget, chunk;
   if (pending < nthreads) {
     s = 1;
     chunk = 1;
-    budget = pending * 64 < nthreads ? 32 : (pending * 8 < nthreads ? 128 : 512);
+    uint32_t prev = c->budget;
+    budget = (pending <= prev_pending && prev >= 64) ? (prev < (1u << 16) ? prev * 2 : prev) : 64;
   } else {
     unsigned long long per = pending / nthreads;
     s = (uint32_t)(per < cap / 2 ? per : cap / 2);
     if (s == 0) s = 1;
     chunk = 2;
-    budget = 4096;
+    budget = 1u << 16;
   }
+  unsigned long long busy = pending < nthreads ? pending : nthreads;
+  unsigned long long keep = (busy * (256 - c->stop_frac_q8)) >> 8;  // busy threads that keep the turn going
+  c->stop_at = (uint32_t)(nthreads - keep);
   c->static_per_thread = s;
   c->budget = budget;
   c->chunk = chunk;
@@ -91,13 +99,24 @@ __device__ void fixed_policy(Ctl* c, unsigned long long pending, uint32_t nthrea
 __global__ void turn_kernel(Dev d, uint32_t cap) {
   extern __shared__ unsigned long long smem_stack[];
   Ctl* c = d.ctl;
-  const unsigned long long base = ldcg64(&c->base);
-  const unsigned long long in_end = ldcg64(&c->in_end);
-  if (base == in_end) return;  // normal form reached: nothing to do
-  if (__ldcg(&c->status) != 0) return;
-  const uint32_t s = __ldcg(&c->static_per_thread);
-  const uint32_t budget = __ldcg(&c->budget);
-  const uint32_t chunk = __ldcg(&c->chunk);
+  // Turn parameters are read once per block so every thread of the block
+  // takes the same early-exit decision.
+  __shared__ unsigned long long sh_base, sh_end;
+  __shared__ unsigned sh_run, sh_s, sh_budget, sh_chunk, sh_stop_at, blk_dry;
+  if (threadIdx.x == 0) {
+    sh_base = ldcg64(&c->base);
+    sh_end = ldcg64(&c->in_end);
+    sh_run = sh_base != sh_end && __ldcg(&c->status) == 0;  // else: normal form reached, or failed
+    sh_s = __ldcg(&c->static_per_thread);
+    sh_budget = __ldcg(&c->budget);
+    sh_chunk = __ldcg(&c->chunk);
+    sh_stop_at = __ldcg(&c->stop_at);
+    blk_dry = 0;
+  }
+  __syncthreads();
+  if (!sh_run) return;
+  const unsigned long long base = sh_base, in_end = sh_end;
+  const uint32_t s = sh_s, budget = sh_budget, chunk = sh_chunk, stop_at = sh_stop_at;
 
   TState t;
   t.stk = (Pair*)smem_stack + threadIdx.x;
@@ -122,7 +141,17 @@ __global__ void turn_kernel(Dev d, uint32_t cap) {
   }
 
   for (uint32_t left = budget; left > 0 && !t.dead; left--) {
-    if (t.len == 0 && !claim(d, t, in_end, chunk)) break;
+    if (t.len == 0 && !claim(d, t, in_end, chunk)) {
+      // Out of work: count this thread dry (in batches of 8 per block); the
+      // count that crosses `stop_at` ends the turn for everyone.
+      unsigned k = atomicAdd(&blk_dry, 1u) + 1;
+      if ((k & 7) == 0) {
+        unsigned g = atomicAdd(&c->dry, 8u) + 8;
+        if (g >= stop_at) atomicExch(&c->stop, 1u);
+      }
+      break;
+    }
+    if ((left & 15) == 0 && *(volatile unsigned*)&c->stop) break;
     t.len--;
     Pair r = t.stk[(size_t)t.len * t.stride];
     interact(d, t, r);
@@ -173,11 +202,27 @@ __global__ void turn_kernel(Dev d, uint32_t cap) {
       unsigned long long head = ldcg64(&c->head), tail = ldcg64(&c->tail);
       unsigned long long nb = head < in_end ? head : in_end;
       unsigned long long pending = tail - nb;
+      unsigned long long prev_pending = c->pending;
+      if (c->trace && c->turns < c->trace_cap) {
+        unsigned long long now;
+        asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(now));
+        TurnRecord r;
+        r.t_ns = now;
+        r.itrs = c->itrs;
+        r.pending = pending;
+        r.dry = c->dry;
+        r.stopped = c->stop;
+        r.budget = c->budget;
+        r.per_thread = c->static_per_thread;
+        c->trace[c->turns] = r;
+      }
       c->base = nb;
       c->in_end = tail;
       c->pending = pending;
       c->turns += 1;
-      fixed_policy(c, pending, d.nthreads, cap);
+      c->dry = 0;
+      c->stop = 0;
+      fixed_policy(c, pending, prev_pending, d.nthreads, cap);
       unsigned long long take = (unsigned long long)c->static_per_thread * d.nthreads;
       c->head = nb + (take < pending ? take : pending);
       c->blocks_done = 0;
@@ -190,7 +235,7 @@ __global__ void turn_kernel(Dev d, uint32_t cap) {
 // NONE and makes `redex` the only input of the next turn.
 __global__ void boot_kernel(Dev d, Pair redex, uint32_t cap) {
   Ctl* c = d.ctl;
-  d.vars[ROOT_VAR] = NONE;
+  d.vars[ROOT_VAR & d.vars_mask] = NONE;
   unsigned long long at = c->tail;
   d.ring[at & d.ring_mask] = redex;
   c->base = at;
@@ -198,7 +243,10 @@ __global__ void boot_kernel(Dev d, Pair redex, uint32_t cap) {
   c->tail = at + 1;
   c->pending = 1;
   c->blocks_done = 0;
-  fixed_policy(c, 1, d.nthreads, cap);
+  c->dry = 0;
+  c->stop = 0;
+  c->budget = 0;
+  fixed_policy(c, 1, 1, d.nthreads, cap);
   c->head = at + 1;
   __threadfence();
 }
@@ -210,7 +258,7 @@ __global__ void gather_kernel(Dev d, Port root, Port* out, uint32_t* kids, uint3
   __shared__ uint32_t next, lo, hi, overflow;
   auto resolve = [&](Port p) -> Port {
     for (uint32_t g = 0; g < (1u << 20) && get_tag(p) == VAR; g++) {
-      Port v = __ldcg(&d.vars[get_val(p)]);
+      Port v = __ldcg(&d.vars[get_val(p) & d.vars_mask]);
       if (v == NONE || v == 0) break;
       p = v;
     }
@@ -261,7 +309,7 @@ class Runtime {
   Ctl* ctl = nullptr;
   void* mem_node = nullptr; void* mem_vars = nullptr; void* mem_ring = nullptr;
   void* mem_cur = nullptr; void* mem_scratch = nullptr;
-  void* mem_defs = nullptr; void* mem_book = nullptr;
+  void* mem_defs = nullptr; void* mem_book = nullptr; void* mem_trace = nullptr;
   Port* g_out = nullptr; uint32_t* g_kids = nullptr; uint32_t* g_info = nullptr;
   uint32_t gather_cap = 0;
   uint32_t grid = 0, block = 0, cap = 0;
@@ -276,9 +324,9 @@ class Runtime {
   int fail(const std::string& m) { if (err.empty()) err = m; return -1; }
 
   void release() {
-    void* ps[] = {mem_node, mem_vars, mem_ring, mem_cur, mem_scratch, mem_defs, mem_book, g_out, g_kids, g_info, ctl};
+    void* ps[] = {mem_node, mem_vars, mem_ring, mem_cur, mem_scratch, mem_defs, mem_book, g_out, g_kids, g_info, ctl, mem_trace};
     for (void* p : ps) if (p) cudaFree(p);
-    mem_node = mem_vars = mem_ring = mem_cur = mem_scratch = mem_defs = mem_book = nullptr;
+    mem_node = mem_vars = mem_ring = mem_cur = mem_scratch = mem_defs = mem_book = mem_trace = nullptr;
     g_out = nullptr; g_kids = nullptr; g_info = nullptr; ctl = nullptr;
   }
 
@@ -309,11 +357,9 @@ class Runtime {
     if (d.node_slice < 4 || d.vars_slice < 4) return fail("node/var space too small for the thread count");
     d.nthreads = nthreads;
 
-    // The ROOT var is index 0x1FFFFFFF: the var array always spans 2^29 words
-    // of address space, but only the slices and ROOT are ever touched.
     CK(cudaMalloc(&mem_node, n_nodes * sizeof(Pair)));
-    size_t vars_words = (size_t)1 << 29;
-    CK(cudaMalloc(&mem_vars, vars_words * sizeof(Port)));
+    CK(cudaMalloc(&mem_vars, n_vars * sizeof(Port)));
+    d.vars_mask = (uint32_t)(n_vars - 1);
     uint64_t ring_len = 1ull << cfg.ring_log2;
     CK(cudaMalloc(&mem_ring, ring_len * sizeof(Pair)));
     CK(cudaMalloc(&mem_cur, 2ull * nthreads * sizeof(uint32_t)));
@@ -331,11 +377,18 @@ class Runtime {
   // Clears the whole net (node/var words, ring, cursors, counters).
   int reset_net() {
     CK(cudaMemset(mem_node, 0, (1ull << cfg.node_log2) * sizeof(Pair)));
-    // Only the slices and the ROOT word of the var space are used.
-    CK(cudaMemset(mem_vars, 0, ((size_t)d.vars_slice * d.nthreads + 1) * sizeof(Port)));
-    CK(cudaMemset((char*)mem_vars + (size_t)ROOT_VAR * sizeof(Port), 0, sizeof(Port)));
+    CK(cudaMemset(mem_vars, 0, (1ull << cfg.vars_log2) * sizeof(Port)));
     CK(cudaMemset(mem_cur, 0, 2ull * d.nthreads * sizeof(uint32_t)));
     CK(cudaMemset(ctl, 0, sizeof(Ctl)));
+    if (cfg.trace_cap) {
+      if (!mem_trace) CK(cudaMalloc(&mem_trace, (size_t)cfg.trace_cap * sizeof(TurnRecord)));
+      TurnRecord* tp = (TurnRecord*)mem_trace;
+      unsigned cap_ = cfg.trace_cap;
+      CK(cudaMemcpy(&ctl->trace, &tp, sizeof(tp), cudaMemcpyHostToDevice));
+      CK(cudaMemcpy(&ctl->trace_cap, &cap_, sizeof(cap_), cudaMemcpyHostToDevice));
+    }
+    uint32_t frac = cfg.stop_frac_q8 ? cfg.stop_frac_q8 : 128;
+    CK(cudaMemcpy(&ctl->stop_frac_q8, &frac, sizeof(frac), cudaMemcpyHostToDevice));
     std::vector<uint32_t> one(d.nthreads, 1);  // cursors start past word 0 like the reference
     CK(cudaMemcpy(d.ncur, one.data(), d.nthreads * sizeof(uint32_t), cudaMemcpyHostToDevice));
     CK(cudaMemcpy(d.vcur, one.data(), d.nthreads * sizeof(uint32_t), cudaMemcpyHostToDevice));
@@ -474,8 +527,8 @@ class Runtime {
   }
 
   // Single-word device accessors for the host-side readback walk.
-  Port vars_load(uint32_t i) { Port v = 0; cudaMemcpy(&v, d.vars + i, sizeof(Port), cudaMemcpyDeviceToHost); return v; }
-  void vars_store(uint32_t i, Port v) { cudaMemcpy(d.vars + i, &v, sizeof(Port), cudaMemcpyHostToDevice); }
+  Port vars_load(uint32_t i) { Port v = 0; cudaMemcpy(&v, d.vars + (i & d.vars_mask), sizeof(Port), cudaMemcpyDeviceToHost); return v; }
+  void vars_store(uint32_t i, Port v) { cudaMemcpy(d.vars + (i & d.vars_mask), &v, sizeof(Port), cudaMemcpyHostToDevice); }
   Pair node_load(uint32_t i) { Pair v = 0; cudaMemcpy(&v, d.node + i, sizeof(Pair), cudaMemcpyDeviceToHost); return v; }
 
   // Read-only chase (src/hvm.c:781-790).
@@ -657,12 +710,14 @@ extern "C" void hvm_gb300_default_config(hvm_gb300_config* c) {
   memset(c, 0, sizeof(*c));
   c->device = 0;
   c->threads_per_block = 128;
-  c->stack_cap = 64;
   c->blocks_per_sm = 0;
   c->node_log2 = 29;
   c->vars_log2 = 29;
   c->ring_log2 = 26;
   c->max_turns = 0;
+  c->stop_frac_q8 = 128;
+  c->stack_cap = 16;
+  c->trace_cap = 0;
 }
 
 extern "C" int hvm_gb300_create(const hvm_gb300_config* cfg, hvm_gb300_runtime** out) {
@@ -691,6 +746,29 @@ extern "C" int hvm_gb300_run(hvm_gb300_runtime* r, hvm_gb300_stats* stats) {
   r->rt.err.clear();
   if (r->rt.run_main()) return -1;
   if (stats && r->rt.stats(stats)) return -1;
+  return 0;
+}
+
+extern "C" int hvm_gb300_trace(hvm_gb300_runtime* r, hvm_gb300_turn* out, size_t cap, size_t* n) {
+  if (!r) return -1;
+  hvm::Ctl h;
+  if (r->rt.read_ctl(h)) return -1;
+  size_t have = h.turns < r->rt.cfg.trace_cap ? (size_t)h.turns : (size_t)r->rt.cfg.trace_cap;
+  if (n) *n = have;
+  if (!out || !r->rt.mem_trace) return 0;
+  size_t k = have < cap ? have : cap;
+  std::vector<hvm::TurnRecord> tmp(k);
+  if (k && cudaMemcpy(tmp.data(), r->rt.mem_trace, k * sizeof(hvm::TurnRecord), cudaMemcpyDeviceToHost) != cudaSuccess)
+    return r->rt.fail("trace copy failed");
+  for (size_t i = 0; i < k; i++) {
+    out[i].t_ns = tmp[i].t_ns;
+    out[i].itrs = tmp[i].itrs;
+    out[i].pending = tmp[i].pending;
+    out[i].dry = tmp[i].dry;
+    out[i].stopped = tmp[i].stopped;
+    out[i].budget = tmp[i].budget;
+    out[i].per_thread = tmp[i].per_thread;
+  }
   return 0;
 }
 
