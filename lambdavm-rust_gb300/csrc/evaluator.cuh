@@ -93,6 +93,8 @@ struct Dev {
   uint32_t node_slice, vars_slice;   // words per thread slice
   uint32_t* ncur;             // per-thread allocation cursors (persist across turns)
   uint32_t* vcur;
+  uint32_t* nhome;            // per-thread home slice indices (persist across turns)
+  uint32_t* vhome;
   uint32_t* nloc;             // CALL scratch: [max_def_nodes][nthreads]
   uint32_t* vloc;             // CALL scratch: [max_def_vars][nthreads]
   uint32_t nthreads;
@@ -127,6 +129,7 @@ struct TState {
   uint32_t gid;
   uint32_t node_base, vars_base;
   uint32_t ncur, vcur;
+  uint32_t nhome, vhome;      // current home slices of the allocators
   unsigned long long base;    // ring index of this turn's first input (overflow check)
   unsigned long long itrs, leak, retries;
   unsigned long long hist[8];
@@ -151,26 +154,47 @@ __device__ __forceinline__ void push(const Dev& d, TState& t, Pair r) {
 }
 
 // ---- allocation (src/hvm.cu:880-912, src/hvm.c:713-755) ------------------------
+//
+// Like the reference, a thread scans a slice of the node/var space for free
+// (zero) words with a cursor that persists across turns, so freed words are
+// reused as the cursor wraps. Unlike the reference, a word is claimed with a
+// CAS (0 -> MARK for nodes, 0 -> NONE for vars), so slices are home regions
+// rather than exclusive property: a thread whose slice is full hops to the
+// next slice instead of failing, and any number of threads may share one.
+// The last node word is never handed out, so MARK (all ones) never collides
+// with a real node.
 
-// Returns a free node word of this thread's slice, or 0 when `budget` scans
-// found none. `budget` bounds the scans of one allocation batch, so a batch
-// can never wrap around its slice and hand out the same word twice.
-__device__ __forceinline__ uint32_t alloc_node(const Dev& d, TState& t, uint32_t& budget) {
-  while (budget > 0) {
-    budget--;
-    uint32_t at = t.node_base + t.ncur;
-    if (++t.ncur == d.node_slice) t.ncur = 0;
-    if (at != 0 && nload(d, at) == 0) return at;
+constexpr Pair NODE_MARK = ~0ull;
+constexpr uint32_t MAX_HOPS = 64;
+
+__device__ __forceinline__ uint32_t alloc_node(const Dev& d, TState& t) {
+  for (uint32_t hop = 0; hop <= MAX_HOPS; hop++) {
+    for (uint32_t scan = 0; scan < d.node_slice; scan++) {
+      uint32_t at = t.node_base + t.ncur;
+      if (++t.ncur == d.node_slice) t.ncur = 0;
+      if (at != 0 && nload(d, at) == 0 &&
+          atomicCAS((unsigned long long*)&d.node[at], 0ull, (unsigned long long)NODE_MARK) == 0ull) {
+        return at;
+      }
+    }
+    // Home slice full: move to the next one.
+    t.nhome = t.nhome + 1 == d.nthreads ? 0 : t.nhome + 1;
+    t.node_base = t.nhome * d.node_slice;
+    t.ncur = 0;
   }
   return 0;
 }
 
-__device__ __forceinline__ uint32_t alloc_var(const Dev& d, TState& t, uint32_t& budget) {
-  while (budget > 0) {
-    budget--;
-    uint32_t at = t.vars_base + t.vcur;
-    if (++t.vcur == d.vars_slice) t.vcur = 0;
-    if (at != 0 && vload(d, at) == 0) return at;
+__device__ __forceinline__ uint32_t alloc_var(const Dev& d, TState& t) {
+  for (uint32_t hop = 0; hop <= MAX_HOPS; hop++) {
+    for (uint32_t scan = 0; scan < d.vars_slice; scan++) {
+      uint32_t at = t.vars_base + t.vcur;
+      if (++t.vcur == d.vars_slice) t.vcur = 0;
+      if (at != 0 && vload(d, at) == 0 && atomicCAS(&d.vars[at], 0u, NONE) == 0u) return at;
+    }
+    t.vhome = t.vhome + 1 == d.nthreads ? 0 : t.vhome + 1;
+    t.vars_base = t.vhome * d.vars_slice;
+    t.vcur = 0;
   }
   return 0;
 }
@@ -234,19 +258,15 @@ __device__ __forceinline__ int rule_anni(const Dev& d, TState& t, Port a, Port b
 }
 
 __device__ __forceinline__ int rule_comm(const Dev& d, TState& t, Port a, Port b) {
-  uint32_t nb = d.node_slice, vb = d.vars_slice;
-  uint32_t n0 = alloc_node(d, t, nb), n1 = alloc_node(d, t, nb);
-  uint32_t n2 = alloc_node(d, t, nb), n3 = alloc_node(d, t, nb);
-  if (!n3) { set_status(d, ST_OOM_NODES, t.gid); return IR_FATAL; }
-  uint32_t v0 = alloc_var(d, t, vb), v1 = alloc_var(d, t, vb);
-  uint32_t v2 = alloc_var(d, t, vb), v3 = alloc_var(d, t, vb);
-  if (!v3) { set_status(d, ST_OOM_VARS, t.gid); return IR_FATAL; }
   Pair A = nload(d, get_val(a));
   Pair B = nload(d, get_val(b));
   if (A == 0 || B == 0) return IR_RETRY;
+  uint32_t n0 = alloc_node(d, t), n1 = alloc_node(d, t), n2 = alloc_node(d, t), n3 = alloc_node(d, t);
+  if (!n0 || !n1 || !n2 || !n3) { set_status(d, ST_OOM_NODES, t.gid); return IR_FATAL; }
+  uint32_t v0 = alloc_var(d, t), v1 = alloc_var(d, t), v2 = alloc_var(d, t), v3 = alloc_var(d, t);
+  if (!v0 || !v1 || !v2 || !v3) { set_status(d, ST_OOM_VARS, t.gid); return IR_FATAL; }
   nstore(d, get_val(a), 0);
   nstore(d, get_val(b), 0);
-  vstore(d, v0, NONE); vstore(d, v1, NONE); vstore(d, v2, NONE); vstore(d, v3, NONE);
   nstore(d, n0, new_pair(new_port(VAR, v0), new_port(VAR, v1)));
   nstore(d, n1, new_pair(new_port(VAR, v2), new_port(VAR, v3)));
   nstore(d, n2, new_pair(new_port(VAR, v0), new_port(VAR, v2)));
@@ -260,9 +280,6 @@ __device__ __forceinline__ int rule_comm(const Dev& d, TState& t, Port a, Port b
 }
 
 __device__ __forceinline__ int rule_oper(const Dev& d, TState& t, Port a, Port b) {
-  uint32_t nb = d.node_slice;
-  uint32_t n0 = alloc_node(d, t, nb);
-  if (!n0) { set_status(d, ST_OOM_NODES, t.gid); return IR_FATAL; }
   Pair B = nload(d, get_val(b));
   if (B == 0) return IR_RETRY;
   nstore(d, get_val(b), 0);
@@ -271,6 +288,8 @@ __device__ __forceinline__ int rule_oper(const Dev& d, TState& t, Port a, Port b
   if (get_tag(b1) == NUM) {
     link(d, t, new_port(NUM, operate(get_val(a), get_val(b1))), b2);
   } else {
+    uint32_t n0 = alloc_node(d, t);
+    if (!n0) { set_status(d, ST_OOM_NODES, t.gid); return IR_FATAL; }
     nstore(d, n0, new_pair(a, b2));
     publish();
     link(d, t, b1, new_port(OPR, n0));
@@ -279,13 +298,13 @@ __device__ __forceinline__ int rule_oper(const Dev& d, TState& t, Port a, Port b
 }
 
 __device__ __forceinline__ int rule_swit(const Dev& d, TState& t, Port a, Port b) {
-  uint32_t nb = d.node_slice;
-  uint32_t n0 = alloc_node(d, t, nb), n1 = alloc_node(d, t, nb);
-  if (!n1) { set_status(d, ST_OOM_NODES, t.gid); return IR_FATAL; }
   Pair B = nload(d, get_val(b));
   if (B == 0) return IR_RETRY;
-  nstore(d, get_val(b), 0);
   uint32_t n = get_u24(get_val(a));
+  uint32_t n0 = alloc_node(d, t);
+  uint32_t n1 = n == 0 ? 1u : alloc_node(d, t);
+  if (!n0 || !n1) { set_status(d, ST_OOM_NODES, t.gid); return IR_FATAL; }
+  nstore(d, get_val(b), 0);
   if (n == 0) {
     nstore(d, n0, new_pair(get_snd(B), new_port(ERA, 0)));
   } else {
@@ -310,18 +329,16 @@ __device__ int rule_call(const Dev& d, TState& t, Port a, Port b) {
   const DefHdr h = d.defs[fid];
   // Copy optimisation: a safe REF meeting a DUP is duplicated like an eraser.
   if (h.safe && get_tag(b) == DUP) return rule_eras(d, t, a, b);
-  uint32_t nb = d.node_slice, vb = d.vars_slice;
   for (uint32_t i = 0; i < h.node_len; i++) {
-    uint32_t at = alloc_node(d, t, nb);
+    uint32_t at = alloc_node(d, t);
     if (!at) { set_status(d, ST_OOM_NODES, t.gid); return IR_FATAL; }
     d.nloc[(size_t)i * d.nthreads + t.gid] = at;
   }
   for (uint32_t i = 0; i < h.vars_len; i++) {
-    uint32_t at = alloc_var(d, t, vb);
+    uint32_t at = alloc_var(d, t);  // claimed as NONE: created
     if (!at) { set_status(d, ST_OOM_VARS, t.gid); return IR_FATAL; }
     d.vloc[(size_t)i * d.nthreads + t.gid] = at;
   }
-  for (uint32_t i = 0; i < h.vars_len; i++) vstore(d, d.vloc[(size_t)i * d.nthreads + t.gid], NONE);
   const Pair* nodes = d.book + h.off + h.rbag_len;
   for (uint32_t i = 0; i < h.node_len; i++) {
     Pair p = __ldg((const unsigned long long*)&nodes[i]);

@@ -124,8 +124,10 @@ __global__ void turn_kernel(Dev d, uint32_t cap) {
   t.len = 0;
   t.cap = cap;
   t.gid = blockIdx.x * blockDim.x + threadIdx.x;
-  t.node_base = t.gid * d.node_slice;
-  t.vars_base = t.gid * d.vars_slice;
+  t.nhome = d.nhome[t.gid];
+  t.vhome = d.vhome[t.gid];
+  t.node_base = t.nhome * d.node_slice;
+  t.vars_base = t.vhome * d.vars_slice;
   t.ncur = d.ncur[t.gid];
   t.vcur = d.vcur[t.gid];
   t.base = base;
@@ -159,6 +161,8 @@ __global__ void turn_kernel(Dev d, uint32_t cap) {
 
   d.ncur[t.gid] = t.ncur;
   d.vcur[t.gid] = t.vcur;
+  d.nhome[t.gid] = t.nhome;
+  d.vhome[t.gid] = t.vhome;
 
   // Flush the LIFO to the ring tail, one atomic per warp.
   __syncwarp();
@@ -352,7 +356,7 @@ class Runtime {
 
     uint64_t n_nodes = 1ull << cfg.node_log2, n_vars = 1ull << cfg.vars_log2;
     // Slices exclude word 0 and the ROOT var at the top of the var space.
-    d.node_slice = (uint32_t)((n_nodes - 1) / nthreads);
+    d.node_slice = (uint32_t)((n_nodes - 2) / nthreads);
     d.vars_slice = (uint32_t)((n_vars - 2) / nthreads);
     if (d.node_slice < 4 || d.vars_slice < 4) return fail("node/var space too small for the thread count");
     d.nthreads = nthreads;
@@ -362,7 +366,7 @@ class Runtime {
     d.vars_mask = (uint32_t)(n_vars - 1);
     uint64_t ring_len = 1ull << cfg.ring_log2;
     CK(cudaMalloc(&mem_ring, ring_len * sizeof(Pair)));
-    CK(cudaMalloc(&mem_cur, 2ull * nthreads * sizeof(uint32_t)));
+    CK(cudaMalloc(&mem_cur, 4ull * nthreads * sizeof(uint32_t)));
     CK(cudaMalloc((void**)&ctl, sizeof(Ctl)));
     d.node = (Pair*)mem_node;
     d.vars = (Port*)mem_vars;
@@ -370,6 +374,8 @@ class Runtime {
     d.ring_mask = ring_len - 1;
     d.ncur = (uint32_t*)mem_cur;
     d.vcur = d.ncur + nthreads;
+    d.nhome = d.vcur + nthreads;
+    d.vhome = d.nhome + nthreads;
     d.ctl = ctl;
     return reset_net();
   }
@@ -378,7 +384,11 @@ class Runtime {
   int reset_net() {
     CK(cudaMemset(mem_node, 0, (1ull << cfg.node_log2) * sizeof(Pair)));
     CK(cudaMemset(mem_vars, 0, (1ull << cfg.vars_log2) * sizeof(Port)));
-    CK(cudaMemset(mem_cur, 0, 2ull * d.nthreads * sizeof(uint32_t)));
+    CK(cudaMemset(mem_cur, 0, 4ull * d.nthreads * sizeof(uint32_t)));
+    std::vector<uint32_t> home(d.nthreads);
+    for (uint32_t g = 0; g < d.nthreads; g++) home[g] = g;
+    CK(cudaMemcpy(d.nhome, home.data(), d.nthreads * sizeof(uint32_t), cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(d.vhome, home.data(), d.nthreads * sizeof(uint32_t), cudaMemcpyHostToDevice));
     CK(cudaMemset(ctl, 0, sizeof(Ctl)));
     if (cfg.trace_cap) {
       if (!mem_trace) CK(cudaMalloc(&mem_trace, (size_t)cfg.trace_cap * sizeof(TurnRecord)));
