@@ -78,8 +78,21 @@ struct alignas(128) Ctl {
   unsigned int policy;              // 0 = fixed policy
   unsigned int pad_c[1];
   unsigned long long hist[8];       // interactions per rule (diagnostic)
+  unsigned int npool_next;          // next page id of the node pool
+  unsigned int vpool_next;          // next page id of the var pool
   TurnRecord* trace;                // per-turn records (null = off)
   unsigned int trace_cap;
+};
+
+constexpr Pair NODE_MARK = ~0ull;
+
+struct PagedSpace {
+  uint32_t page_log2;        // words per page = 1 << page_log2
+  uint32_t max_pages;        // capacity of each thread's page list
+  uint32_t* lists;           // [nthreads][max_pages] page ids
+  uint32_t* counts;          // [nthreads] pages owned
+  uint32_t* pos;             // [nthreads] index into the list of the page being scanned
+  uint32_t* off;             // [nthreads] word offset of the next chunk in that page
 };
 
 // Everything a turn kernel needs; passed by value.
@@ -88,13 +101,11 @@ struct Dev {
   Port* vars;                 // var words, 2^k entries; var v lives at v & vars_mask,
                               // so ROOT (0x1FFFFFFF) lands on the last word
   uint32_t vars_mask;
+  uint32_t node_mask;         // node space size - 1
   Pair* ring;                 // global redex ring
   unsigned long long ring_mask;
-  uint32_t node_slice, vars_slice;   // words per thread slice
-  uint32_t* ncur;             // per-thread allocation cursors (persist across turns)
-  uint32_t* vcur;
-  uint32_t* nhome;            // per-thread home slice indices (persist across turns)
-  uint32_t* vhome;
+  PagedSpace nspace, vspace;  // per-thread page lists (persist across turns)
+  uint32_t npool_end, vpool_end;  // one past the last page id the pools may hand out
   uint32_t* nloc;             // CALL scratch: [max_def_nodes][nthreads]
   uint32_t* vloc;             // CALL scratch: [max_def_vars][nthreads]
   uint32_t nthreads;
@@ -120,6 +131,15 @@ __device__ __forceinline__ void set_status(const Dev& d, uint32_t code, uint32_t
   if (atomicCAS(&d.ctl->status, 0u, code) == 0u) d.ctl->err_info = info;
 }
 
+// Per-thread allocator registers for one space.
+struct Alloc {
+  uint32_t pos, off, count;  // page-list position, next chunk offset, pages owned
+  uint32_t page;             // id of the page at `pos`
+  uint32_t chunk;            // word index of the chunk `mask` describes
+  uint32_t mask;             // free words of that chunk not yet handed out
+  uint32_t dry_chunks;       // chunks scanned since the last free word
+};
+
 // ---- per-thread state ----------------------------------------------------------
 
 struct TState {
@@ -127,9 +147,7 @@ struct TState {
   uint32_t stride;
   uint32_t len, cap;
   uint32_t gid;
-  uint32_t node_base, vars_base;
-  uint32_t ncur, vcur;
-  uint32_t nhome, vhome;      // current home slices of the allocators
+  Alloc na, va;               // node / var allocators
   unsigned long long base;    // ring index of this turn's first input (overflow check)
   unsigned long long itrs, leak, retries;
   unsigned long long hist[8];
@@ -155,48 +173,118 @@ __device__ __forceinline__ void push(const Dev& d, TState& t, Pair r) {
 
 // ---- allocation (src/hvm.cu:880-912, src/hvm.c:713-755) ------------------------
 //
-// Like the reference, a thread scans a slice of the node/var space for free
-// (zero) words with a cursor that persists across turns, so freed words are
-// reused as the cursor wraps. Unlike the reference, a word is claimed with a
-// CAS (0 -> MARK for nodes, 0 -> NONE for vars), so slices are home regions
-// rather than exclusive property: a thread whose slice is full hops to the
-// next slice instead of failing, and any number of threads may share one.
-// The last node word is never handed out, so MARK (all ones) never collides
-// with a real node.
+// As in the reference, a thread allocates by scanning memory it owns for free
+// (zero) words with a cursor that persists across turns, so words freed by
+// any thread are reused when the cursor comes back round. The GB300 layout:
+//   * the node and var spaces are cut into pages (a power of two of words,
+//     >= one 64-byte chunk); each thread owns a list of pages exclusively, so
+//     a word it sees free stays free until it takes it -- no atomics;
+//   * the scan reads one 64-byte chunk per L2 round trip (8 node words or 16
+//     var words, vector loads) and keeps a bitmask of the free words, so most
+//     allocations cost no memory access at all;
+//   * a thread that scanned two pages' worth of chunks without finding a free
+//     word takes a fresh page from a global pool (one atomic) instead of
+//     failing; only an exhausted pool or page list is out-of-memory.
+// A node word is marked (all ones) as soon as it is taken, so a later scan
+// of the same chunk inside one interaction cannot hand it out twice; the
+// last node word is never used, so the mark is not a real node. A var is
+// created (NONE) as soon as it is taken. Word 0 of each space and the ROOT
+// var (the last var word) are never handed out.
 
-constexpr Pair NODE_MARK = ~0ull;
-constexpr uint32_t MAX_HOPS = 64;
+__device__ __forceinline__ unsigned int* pool_counter(const Dev& d, bool vars) {
+  return vars ? &d.ctl->vpool_next : &d.ctl->npool_next;
+}
 
-__device__ __forceinline__ uint32_t alloc_node(const Dev& d, TState& t) {
-  for (uint32_t hop = 0; hop <= MAX_HOPS; hop++) {
-    for (uint32_t scan = 0; scan < d.node_slice; scan++) {
-      uint32_t at = t.node_base + t.ncur;
-      if (++t.ncur == d.node_slice) t.ncur = 0;
-      if (at != 0 && nload(d, at) == 0 &&
-          atomicCAS((unsigned long long*)&d.node[at], 0ull, (unsigned long long)NODE_MARK) == 0ull) {
-        return at;
+template <bool VARS>
+__device__ __forceinline__ uint32_t chunk_mask(const Dev& d, uint32_t base) {
+  uint32_t m = 0;
+  if (!VARS) {
+    const ulonglong2* p = (const ulonglong2*)&d.node[base];
+    #pragma unroll
+    for (int k = 0; k < 4; k++) {
+      ulonglong2 v = __ldcg(p + k);
+      m |= (v.x == 0 ? 1u : 0u) << (2 * k);
+      m |= (v.y == 0 ? 1u : 0u) << (2 * k + 1);
+    }
+    if (base == 0) m &= ~1u;
+    if (base + 8 > d.node_mask) m &= ~(1u << (d.node_mask - base));  // never the MARK word
+  } else {
+    const uint4* p = (const uint4*)&d.vars[base];
+    #pragma unroll
+    for (int k = 0; k < 4; k++) {
+      uint4 v = __ldcg(p + k);
+      m |= (v.x == 0 ? 1u : 0u) << (4 * k);
+      m |= (v.y == 0 ? 1u : 0u) << (4 * k + 1);
+      m |= (v.z == 0 ? 1u : 0u) << (4 * k + 2);
+      m |= (v.w == 0 ? 1u : 0u) << (4 * k + 3);
+    }
+    if (base == 0) m &= ~1u;
+    if (base + 16 > d.vars_mask) m &= ~(1u << (d.vars_mask - base));  // ROOT
+  }
+  return m;
+}
+
+template <bool VARS>
+__device__ __forceinline__ uint32_t alloc_word(const Dev& d, TState& t, Alloc& a) {
+  const PagedSpace& sp = VARS ? d.vspace : d.nspace;
+  const uint32_t chunk_words = VARS ? 16u : 8u;
+  const uint32_t page_words = 1u << sp.page_log2;
+  const uint32_t chunks_per_page = page_words / chunk_words;
+  for (uint32_t guard = 0; guard < (1u << 22); guard++) {
+    if (a.mask) {
+      uint32_t b = __ffs(a.mask) - 1;
+      a.mask &= a.mask - 1;
+      uint32_t at = a.chunk + b;
+      if (VARS) vstore(d, at, NONE); else nstore(d, at, NODE_MARK);
+      return at;
+    }
+    // Next chunk: within the page, then the next owned page, then a new page.
+    if (a.off >= page_words) {
+      a.off = 0;
+      if (a.dry_chunks >= 2 * chunks_per_page || a.count == 1 && a.dry_chunks >= chunks_per_page) {
+        if (a.count >= sp.max_pages) return 0;
+        uint32_t fresh = atomicAdd(pool_counter(d, VARS), 1u);
+        if (fresh >= (VARS ? d.vpool_end : d.npool_end)) return 0;
+        sp.lists[(size_t)t.gid * sp.max_pages + a.count] = fresh;
+        a.pos = a.count;
+        a.count++;
+        sp.counts[t.gid] = a.count;
+        a.page = fresh;
+        a.dry_chunks = 0;
+      } else {
+        a.pos = a.pos + 1 == a.count ? 0 : a.pos + 1;
+        a.page = __ldcg(&sp.lists[(size_t)t.gid * sp.max_pages + a.pos]);
       }
     }
-    // Home slice full: move to the next one.
-    t.nhome = t.nhome + 1 == d.nthreads ? 0 : t.nhome + 1;
-    t.node_base = t.nhome * d.node_slice;
-    t.ncur = 0;
+    a.chunk = (a.page << sp.page_log2) + a.off;
+    a.off += chunk_words;
+    a.mask = chunk_mask<VARS>(d, a.chunk);
+    a.dry_chunks = a.mask ? 0 : a.dry_chunks + 1;
   }
   return 0;
 }
 
-__device__ __forceinline__ uint32_t alloc_var(const Dev& d, TState& t) {
-  for (uint32_t hop = 0; hop <= MAX_HOPS; hop++) {
-    for (uint32_t scan = 0; scan < d.vars_slice; scan++) {
-      uint32_t at = t.vars_base + t.vcur;
-      if (++t.vcur == d.vars_slice) t.vcur = 0;
-      if (at != 0 && vload(d, at) == 0 && atomicCAS(&d.vars[at], 0u, NONE) == 0u) return at;
-    }
-    t.vhome = t.vhome + 1 == d.nthreads ? 0 : t.vhome + 1;
-    t.vars_base = t.vhome * d.vars_slice;
-    t.vcur = 0;
-  }
-  return 0;
+__device__ __forceinline__ uint32_t alloc_node(const Dev& d, TState& t) { return alloc_word<false>(d, t, t.na); }
+__device__ __forceinline__ uint32_t alloc_var(const Dev& d, TState& t) { return alloc_word<true>(d, t, t.va); }
+
+// Loads a thread's allocator state at turn start; it resumes at the chunk it
+// was scanning when the previous turn ended.
+template <bool VARS>
+__device__ __forceinline__ void alloc_load(const PagedSpace& sp, uint32_t gid, Alloc& a) {
+  const uint32_t chunk_words = VARS ? 16u : 8u;
+  a.pos = sp.pos[gid];
+  a.off = sp.off[gid];
+  a.count = sp.counts[gid];
+  a.page = sp.lists[(size_t)gid * sp.max_pages + a.pos];
+  a.off = a.off >= chunk_words ? a.off - chunk_words : 0;
+  a.chunk = 0;
+  a.mask = 0;
+  a.dry_chunks = 0;
+}
+
+__device__ __forceinline__ void alloc_save(const PagedSpace& sp, uint32_t gid, const Alloc& a) {
+  sp.pos[gid] = a.pos;
+  sp.off[gid] = a.off;
 }
 
 // ---- linking (src/hvm.c:784-840) ----------------------------------------------

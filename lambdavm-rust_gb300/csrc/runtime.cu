@@ -33,6 +33,9 @@
 
 namespace hvm {
 
+// Capacity of each thread's page list (pages of one space a thread may own).
+constexpr uint32_t MAX_PAGES = 64;
+
 static const char* status_text(uint32_t s) {
   switch (s) {
     case ST_OK: return "ok";
@@ -124,12 +127,8 @@ __global__ void turn_kernel(Dev d, uint32_t cap) {
   t.len = 0;
   t.cap = cap;
   t.gid = blockIdx.x * blockDim.x + threadIdx.x;
-  t.nhome = d.nhome[t.gid];
-  t.vhome = d.vhome[t.gid];
-  t.node_base = t.nhome * d.node_slice;
-  t.vars_base = t.vhome * d.vars_slice;
-  t.ncur = d.ncur[t.gid];
-  t.vcur = d.vcur[t.gid];
+  alloc_load<false>(d.nspace, t.gid, t.na);
+  alloc_load<true>(d.vspace, t.gid, t.va);
   t.base = base;
   t.itrs = t.leak = t.retries = 0;
   for (int i = 0; i < 8; i++) t.hist[i] = 0;
@@ -159,10 +158,8 @@ __global__ void turn_kernel(Dev d, uint32_t cap) {
     interact(d, t, r);
   }
 
-  d.ncur[t.gid] = t.ncur;
-  d.vcur[t.gid] = t.vcur;
-  d.nhome[t.gid] = t.nhome;
-  d.vhome[t.gid] = t.vhome;
+  alloc_save(d.nspace, t.gid, t.na);
+  alloc_save(d.vspace, t.gid, t.va);
 
   // Flush the LIFO to the ring tail, one atomic per warp.
   __syncwarp();
@@ -232,6 +229,23 @@ __global__ void turn_kernel(Dev d, uint32_t cap) {
       c->blocks_done = 0;
       __threadfence();
     }
+  }
+}
+
+// Gives thread g page g of each space and points both pools past them.
+__global__ void reset_alloc_kernel(Dev d) {
+  uint32_t g = blockIdx.x * blockDim.x + threadIdx.x;
+  if (g < d.nthreads) {
+    for (const PagedSpace* sp : {&d.nspace, &d.vspace}) {
+      sp->lists[(size_t)g * sp->max_pages] = g;
+      sp->counts[g] = 1;
+      sp->pos[g] = 0;
+      sp->off[g] = 0;
+    }
+  }
+  if (g == 0) {
+    d.ctl->npool_next = d.nthreads;
+    d.ctl->vpool_next = d.nthreads;
   }
 }
 
@@ -355,27 +369,42 @@ class Runtime {
     uint32_t nthreads = grid * block;
 
     uint64_t n_nodes = 1ull << cfg.node_log2, n_vars = 1ull << cfg.vars_log2;
-    // Slices exclude word 0 and the ROOT var at the top of the var space.
-    d.node_slice = (uint32_t)((n_nodes - 2) / nthreads);
-    d.vars_slice = (uint32_t)((n_vars - 2) / nthreads);
-    if (d.node_slice < 4 || d.vars_slice < 4) return fail("node/var space too small for the thread count");
     d.nthreads = nthreads;
-
+    // Pages: a power of two of words, at most 512 node / 1024 var words, and
+    // small enough that every thread starts with one page and at least as
+    // many pages again remain in the pool.
+    auto page_log2_for = [&](uint64_t words, uint32_t max_log2, uint32_t min_log2) -> int {
+      int l = (int)max_log2;
+      while (l >= (int)min_log2 && (words >> l) < 2ull * nthreads) l--;
+      return l < (int)min_log2 ? -1 : l;
+    };
+    int nl = page_log2_for(n_nodes, 9, 3), vl = page_log2_for(n_vars, 10, 4);
+    if (nl < 0 || vl < 0) return fail("node/var space too small for the thread count");
+    d.nspace.page_log2 = (uint32_t)nl;
+    d.vspace.page_log2 = (uint32_t)vl;
+    d.nspace.max_pages = d.vspace.max_pages = MAX_PAGES;
+    d.npool_end = (uint32_t)(n_nodes >> nl);
+    d.vpool_end = (uint32_t)(n_vars >> vl);
+    d.node_mask = (uint32_t)(n_nodes - 1);
     CK(cudaMalloc(&mem_node, n_nodes * sizeof(Pair)));
     CK(cudaMalloc(&mem_vars, n_vars * sizeof(Port)));
     d.vars_mask = (uint32_t)(n_vars - 1);
     uint64_t ring_len = 1ull << cfg.ring_log2;
     CK(cudaMalloc(&mem_ring, ring_len * sizeof(Pair)));
-    CK(cudaMalloc(&mem_cur, 4ull * nthreads * sizeof(uint32_t)));
+    // Page lists + counts + positions + offsets, for both spaces.
+    CK(cudaMalloc(&mem_cur, 2ull * nthreads * (MAX_PAGES + 3) * sizeof(uint32_t)));
     CK(cudaMalloc((void**)&ctl, sizeof(Ctl)));
     d.node = (Pair*)mem_node;
     d.vars = (Port*)mem_vars;
     d.ring = (Pair*)mem_ring;
     d.ring_mask = ring_len - 1;
-    d.ncur = (uint32_t*)mem_cur;
-    d.vcur = d.ncur + nthreads;
-    d.nhome = d.vcur + nthreads;
-    d.vhome = d.nhome + nthreads;
+    uint32_t* w = (uint32_t*)mem_cur;
+    for (PagedSpace* sp : {&d.nspace, &d.vspace}) {
+      sp->lists = w; w += (size_t)nthreads * MAX_PAGES;
+      sp->counts = w; w += nthreads;
+      sp->pos = w; w += nthreads;
+      sp->off = w; w += nthreads;
+    }
     d.ctl = ctl;
     return reset_net();
   }
@@ -384,12 +413,9 @@ class Runtime {
   int reset_net() {
     CK(cudaMemset(mem_node, 0, (1ull << cfg.node_log2) * sizeof(Pair)));
     CK(cudaMemset(mem_vars, 0, (1ull << cfg.vars_log2) * sizeof(Port)));
-    CK(cudaMemset(mem_cur, 0, 4ull * d.nthreads * sizeof(uint32_t)));
-    std::vector<uint32_t> home(d.nthreads);
-    for (uint32_t g = 0; g < d.nthreads; g++) home[g] = g;
-    CK(cudaMemcpy(d.nhome, home.data(), d.nthreads * sizeof(uint32_t), cudaMemcpyHostToDevice));
-    CK(cudaMemcpy(d.vhome, home.data(), d.nthreads * sizeof(uint32_t), cudaMemcpyHostToDevice));
     CK(cudaMemset(ctl, 0, sizeof(Ctl)));
+    uint32_t frac = cfg.stop_frac_q8 ? cfg.stop_frac_q8 : 128;
+    CK(cudaMemcpy(&ctl->stop_frac_q8, &frac, sizeof(frac), cudaMemcpyHostToDevice));
     if (cfg.trace_cap) {
       if (!mem_trace) CK(cudaMalloc(&mem_trace, (size_t)cfg.trace_cap * sizeof(TurnRecord)));
       TurnRecord* tp = (TurnRecord*)mem_trace;
@@ -397,11 +423,9 @@ class Runtime {
       CK(cudaMemcpy(&ctl->trace, &tp, sizeof(tp), cudaMemcpyHostToDevice));
       CK(cudaMemcpy(&ctl->trace_cap, &cap_, sizeof(cap_), cudaMemcpyHostToDevice));
     }
-    uint32_t frac = cfg.stop_frac_q8 ? cfg.stop_frac_q8 : 128;
-    CK(cudaMemcpy(&ctl->stop_frac_q8, &frac, sizeof(frac), cudaMemcpyHostToDevice));
-    std::vector<uint32_t> one(d.nthreads, 1);  // cursors start past word 0 like the reference
-    CK(cudaMemcpy(d.ncur, one.data(), d.nthreads * sizeof(uint32_t), cudaMemcpyHostToDevice));
-    CK(cudaMemcpy(d.vcur, one.data(), d.nthreads * sizeof(uint32_t), cudaMemcpyHostToDevice));
+    // Thread g starts with page g of each space; the pools start after them.
+    reset_alloc_kernel<<<(d.nthreads + 255) / 256, 256>>>(d);
+    CK(cudaGetLastError());
     norm_seconds = 0;
     norm_calls = 0;
     return 0;

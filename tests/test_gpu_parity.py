@@ -102,7 +102,7 @@ def test_hvm_cu_cli(hvm, tmp_path, workloads):
 
 def test_errors_are_reported_not_hung(hvm, workloads):
     # A node space too small for the net ends in an error status, not a hang.
-    with hvm.Runtime(device=0, node_log2=15, threads_per_block=32, blocks_per_sm=1) as r:
+    with hvm.Runtime(device=0, node_log2=17, threads_per_block=32, blocks_per_sm=1) as r:
         r.load(workloads.tree_sum(18))
         with pytest.raises(hvm.HvmError, match="out of node memory|ring"):
             r.run()
