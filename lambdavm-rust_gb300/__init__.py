@@ -41,6 +41,7 @@ class Config(ctypes.Structure):
         ("max_turns", ctypes.c_uint32),
         ("stop_frac_q8", ctypes.c_uint32),
         ("trace_cap", ctypes.c_uint32),
+        ("reg_cap_blocks", ctypes.c_uint32),
     ]
 
 

@@ -143,9 +143,9 @@ struct Alloc {
 // ---- per-thread state ----------------------------------------------------------
 
 struct TState {
-  Pair* stk;                  // this thread's LIFO in shared memory (stride = blockDim.x)
+  Pair* stk;                  // this thread's deque in shared memory (stride = blockDim.x)
   uint32_t stride;
-  uint32_t len, cap;
+  uint32_t lo, len, cap;      // entries lo .. lo+len-1 (mod cap); cap is a power of two
   uint32_t gid;
   Alloc na, va;               // node / var allocators
   unsigned long long base;    // ring index of this turn's first input (overflow check)
@@ -154,21 +154,35 @@ struct TState {
   bool dead;                  // set after a fatal status: stop interacting
 };
 
-// Spills one redex to the global ring (available to every thread next turn).
-__device__ __forceinline__ void ring_push(const Dev& d, TState& t, Pair r) {
-  unsigned long long at = atomicAdd(&d.ctl->tail, 1ull);
-  if (at - t.base > d.ring_mask) { set_status(d, ST_RING_FULL, 0); t.dead = true; return; }
-  d.ring[at & d.ring_mask] = r;
-  t.leak++;
+// Local redex deque: the thread pops and pushes at the top (LIFO, depth
+// first, like the reference's per-thread bags); when it is full, the oldest
+// half moves to the global ring with one atomic (those are the redexes other
+// threads will take first next turn).
+__device__ __forceinline__ Pair& slot(TState& t, uint32_t i) {
+  return t.stk[(size_t)((t.lo + i) & (t.cap - 1)) * t.stride];
+}
+
+__device__ __forceinline__ void spill_oldest(const Dev& d, TState& t, uint32_t k) {
+  unsigned long long at = atomicAdd(&d.ctl->tail, (unsigned long long)k);
+  if (at + k - t.base > d.ring_mask + 1) { set_status(d, ST_RING_FULL, 0); t.dead = true; return; }
+  for (uint32_t i = 0; i < k; i++) d.ring[(at + i) & d.ring_mask] = slot(t, i);
+  t.lo = (t.lo + k) & (t.cap - 1);
+  t.len -= k;
+  t.leak += k;
 }
 
 __device__ __forceinline__ void push(const Dev& d, TState& t, Pair r) {
-  if (t.len < t.cap) {
-    t.stk[(size_t)t.len * t.stride] = r;
-    t.len++;
-  } else {
-    ring_push(d, t, r);
+  if (t.len == t.cap) {
+    spill_oldest(d, t, t.cap / 2);
+    if (t.dead) return;
   }
+  slot(t, t.len) = r;
+  t.len++;
+}
+
+__device__ __forceinline__ Pair pop(TState& t) {
+  t.len--;
+  return slot(t, t.len);
 }
 
 // ---- allocation (src/hvm.cu:880-912, src/hvm.c:713-755) ------------------------

@@ -88,7 +88,7 @@ __device__ void fixed_policy(Ctl* c, unsigned long long pending, unsigned long l
     unsigned long long per = pending / nthreads;
     s = (uint32_t)(per < cap / 2 ? per : cap / 2);
     if (s == 0) s = 1;
-    chunk = 2;
+    chunk = cap / 4 > 1 ? cap / 4 : 1;
     budget = 1u << 16;
   }
   unsigned long long busy = pending < nthreads ? pending : nthreads;
@@ -99,7 +99,10 @@ __device__ void fixed_policy(Ctl* c, unsigned long long pending, unsigned long l
   c->chunk = chunk;
 }
 
-__global__ void turn_kernel(Dev d, uint32_t cap) {
+// MIN_BLOCKS_128 > 0 asks the compiler to fit that many 128-thread blocks per
+// SM (a register cap); the runtime picks the variant from the configuration.
+template <int MIN_BLOCKS_128>
+__global__ void __launch_bounds__(128, MIN_BLOCKS_128 > 0 ? MIN_BLOCKS_128 : 1) turn_kernel(Dev d, uint32_t cap) {
   extern __shared__ unsigned long long smem_stack[];
   Ctl* c = d.ctl;
   // Turn parameters are read once per block so every thread of the block
@@ -124,6 +127,7 @@ __global__ void turn_kernel(Dev d, uint32_t cap) {
   TState t;
   t.stk = (Pair*)smem_stack + threadIdx.x;
   t.stride = blockDim.x;
+  t.lo = 0;
   t.len = 0;
   t.cap = cap;
   t.gid = blockIdx.x * blockDim.x + threadIdx.x;
@@ -141,21 +145,23 @@ __global__ void turn_kernel(Dev d, uint32_t cap) {
     push(d, t, (Pair)__ldcg((const unsigned long long*)&d.ring[at & d.ring_mask]));
   }
 
-  for (uint32_t left = budget; left > 0 && !t.dead; left--) {
+  unsigned stop_seen = 0;
+  for (uint32_t left = budget; left > 0 && !t.dead && !stop_seen; left--) {
     if (t.len == 0 && !claim(d, t, in_end, chunk)) {
-      // Out of work: count this thread dry (in batches of 8 per block); the
+      // Out of work: count this thread dry (in batches of 16 per block); the
       // count that crosses `stop_at` ends the turn for everyone.
       unsigned k = atomicAdd(&blk_dry, 1u) + 1;
-      if ((k & 7) == 0) {
-        unsigned g = atomicAdd(&c->dry, 8u) + 8;
+      if ((k & 15) == 0) {
+        unsigned g = atomicAdd(&c->dry, 16u) + 16;
         if (g >= stop_at) atomicExch(&c->stop, 1u);
       }
       break;
     }
-    if ((left & 15) == 0 && *(volatile unsigned*)&c->stop) break;
-    t.len--;
-    Pair r = t.stk[(size_t)t.len * t.stride];
-    interact(d, t, r);
+    // The stop flag is loaded before the interaction and tested after it, so
+    // its latency hides behind the interaction's own memory traffic.
+    unsigned stop_now = *(volatile unsigned*)&c->stop;
+    interact(d, t, pop(t));
+    stop_seen = stop_now;
   }
 
   alloc_save(d.nspace, t.gid, t.na);
@@ -178,19 +184,29 @@ __global__ void turn_kernel(Dev d, uint32_t cap) {
     if (wbase + total - base > d.ring_mask + 1) {
       if (lane == 0) set_status(d, ST_RING_FULL, 1);
     } else {
-      for (uint32_t i = 0; i < n; i++) d.ring[(my + i) & d.ring_mask] = t.stk[(size_t)i * t.stride];
+      for (uint32_t i = 0; i < n; i++) d.ring[(my + i) & d.ring_mask] = slot(t, i);
       t.leak += n;
     }
   }
 
-  // Counters: one atomic per warp.
+  // Counters: reduced per warp, then per block in shared memory, then one
+  // global atomic per counter per block.
+  __shared__ unsigned long long blk_cnt[11];
+  if (threadIdx.x < 11) blk_cnt[threadIdx.x] = 0;
+  __syncthreads();
   unsigned long long v;
-  v = warp_sum(t.itrs);    if (lane == 0 && v) atomicAdd(&c->itrs, v);
-  v = warp_sum(t.leak);    if (lane == 0 && v) atomicAdd(&c->leak, v);
-  v = warp_sum(t.retries); if (lane == 0 && v) atomicAdd(&c->retries, v);
+  v = warp_sum(t.itrs);    if (lane == 0 && v) atomicAdd(&blk_cnt[0], v);
+  v = warp_sum(t.leak);    if (lane == 0 && v) atomicAdd(&blk_cnt[1], v);
+  v = warp_sum(t.retries); if (lane == 0 && v) atomicAdd(&blk_cnt[2], v);
   for (int i = 0; i < 8; i++) {
     v = warp_sum(t.hist[i]);
-    if (lane == 0 && v) atomicAdd(&c->hist[i], v);
+    if (lane == 0 && v) atomicAdd(&blk_cnt[3 + i], v);
+  }
+  __syncthreads();
+  if (threadIdx.x < 11 && blk_cnt[threadIdx.x]) {
+    unsigned long long* dst = threadIdx.x == 0 ? &c->itrs : threadIdx.x == 1 ? &c->leak
+                            : threadIdx.x == 2 ? &c->retries : &c->hist[threadIdx.x - 3];
+    atomicAdd(dst, blk_cnt[threadIdx.x]);
   }
 
   // The last block to finish closes the turn and picks the next one.
@@ -331,6 +347,7 @@ class Runtime {
   Port* g_out = nullptr; uint32_t* g_kids = nullptr; uint32_t* g_info = nullptr;
   uint32_t gather_cap = 0;
   uint32_t grid = 0, block = 0, cap = 0;
+  void (*turn_fn)(Dev, uint32_t) = nullptr;
   size_t smem = 0;
   uint32_t max_def_nodes = 1, max_def_vars = 1;
   int sms = 0;
@@ -356,13 +373,21 @@ class Runtime {
     block = cfg.threads_per_block;
     cap = cfg.stack_cap;
     if (block == 0 || block % 32 || block > 1024) return fail("threads_per_block must be a multiple of 32 in [32, 1024]");
-    if (cap == 0) return fail("stack_cap must be positive");
+    if (cap < 2 || (cap & (cap - 1))) return fail("stack_cap must be a power of two >= 2");
     if (cfg.node_log2 < 10 || cfg.node_log2 > 29 || cfg.vars_log2 < 10 || cfg.vars_log2 > 29)
       return fail("node_log2/vars_log2 must be in [10, 29]");
     smem = (size_t)block * cap * sizeof(Pair);
-    CK(cudaFuncSetAttribute(turn_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    if (block != 128 && cfg.reg_cap_blocks) return fail("reg_cap_blocks needs threads_per_block = 128");
+    switch (cfg.reg_cap_blocks) {
+      case 0: turn_fn = turn_kernel<0>; break;
+      case 12: turn_fn = turn_kernel<12>; break;
+      case 16: turn_fn = turn_kernel<16>; break;
+      default: return fail("reg_cap_blocks must be 0, 12 or 16");
+    }
+    if (block > 128 && cfg.reg_cap_blocks == 0) turn_fn = turn_kernel<0>;
+    CK(cudaFuncSetAttribute(turn_fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     int per_sm = 0;
-    CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, turn_kernel, (int)block, smem));
+    CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, turn_fn, (int)block, smem));
     if (per_sm <= 0) return fail("turn kernel does not fit on an SM with this block size / stack capacity");
     if (cfg.blocks_per_sm && (int)cfg.blocks_per_sm < per_sm) per_sm = (int)cfg.blocks_per_sm;
     grid = (uint32_t)(per_sm * sms);
@@ -537,7 +562,7 @@ class Runtime {
     unsigned long long last_itrs = ~0ull, last_pending = ~0ull;
     Ctl h;
     for (;;) {
-      for (uint32_t i = 0; i < batch; i++) turn_kernel<<<grid, block, smem>>>(d, cap);
+      for (uint32_t i = 0; i < batch; i++) turn_fn<<<grid, block, smem>>>(d, cap);
       CK(cudaGetLastError());
       turns_run += batch;
       if (read_ctl(h)) return -1;
