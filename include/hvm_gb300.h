@@ -73,7 +73,7 @@ typedef struct {
   uint32_t max_turns;         /* 0 = unbounded; else fail after this many turns */
   uint32_t stop_frac_q8;      /* a turn ends once busy threads < (1 - f/256) x initially busy */
   uint32_t trace_cap;         /* record up to this many turns (0 = off), see hvm_gb300_trace */
-  uint32_t reg_cap_blocks;    /* 0, or 12/16: cap registers so that many 128-thread blocks fit per SM */
+  uint32_t reg_cap_blocks;    /* 0, or 8/12/16: cap registers so that many 128-thread blocks fit per SM */
 } hvm_gb300_config;
 
 typedef struct {

@@ -26,8 +26,8 @@ namespace hvm {
 // Device status codes (0 = running / ok). Written once, first error wins.
 enum : uint32_t {
   ST_OK = 0,
-  ST_OOM_NODES = 1,     // a thread's node slice has no free word
-  ST_OOM_VARS = 2,      // a thread's var slice has no free word
+  ST_OOM_NODES = 1,     // no free node/var word: page list full or page pool empty
+  ST_OOM_VARS = 2,      // (reserved)
   ST_RING_FULL = 3,     // the global redex ring overflowed
   ST_LINK_UNSET = 4,    // a link met a var word that was never created
   ST_LINK_LIMIT = 5,    // a substitution chain exceeded the iteration bound
@@ -301,191 +301,247 @@ __device__ __forceinline__ void alloc_save(const PagedSpace& sp, uint32_t gid, c
   sp.off[gid] = a.off;
 }
 
-// ---- linking (src/hvm.c:784-840) ----------------------------------------------
-
-// Follows a var chain, consuming every resolved var on the way.
-__device__ __forceinline__ Port enter(const Dev& d, Port p) {
-  for (uint32_t guard = 0; guard < (1u << 24) && get_tag(p) == VAR; guard++) {
-    Port v = vexch(d, get_val(p), NONE);
-    if (v == NONE || v == 0) break;
-    vstore(d, get_val(p), 0);
-    p = v;
-  }
-  return p;
-}
-
-// Atomically wires A ~ B: publishes a substitution, or makes a redex when
-// both sides are non-vars.
-__device__ void link(const Dev& d, TState& t, Port A, Port B) {
-  for (uint32_t guard = 0; guard < (1u << 24); guard++) {
-    if (get_tag(A) != VAR && get_tag(B) == VAR) { Port x = A; A = B; B = x; }
-    if (get_tag(A) != VAR) { push(d, t, new_pair(A, B)); return; }
-    B = enter(d, B);
-    Port prev = vexch(d, get_val(A), B);
-    if (prev == NONE) return;
-    if (prev == 0) { set_status(d, ST_LINK_UNSET, get_val(A)); t.dead = true; return; }
-    vstore(d, get_val(A), 0);
-    A = prev;
-  }
-  set_status(d, ST_LINK_LIMIT, 0);
-  t.dead = true;
-}
-
-// ---- interactions (src/hvm.c:852-1122) -----------------------------------------
+// ---- warp-lockstep interactions (src/hvm.c:784-1122) -----------------------------
+//
+// Every lane of a warp runs one interaction per round, and all lanes walk the
+// same phases in the same order, whatever their rule:
+//   1. plan    -- rule, swap, def header (no memory traffic beyond the book);
+//   2. load    -- the principal nodes (one predicated load each, all lanes);
+//   3. alloc   -- fresh node/var words from the lane's chunk masks;
+//   4. write   -- take the principal nodes, create the new nodes;
+//   5. fence   -- one gpu-scope fence for the warp, before anything created
+//                 can be reached by another thread through a link;
+//   6. link    -- the rule's list of port pairs, wired by the reference's
+//                 lock-free linker (src/hvm.c:793-840) one step per round:
+//                 each step is a single atomic exchange issued by every
+//                 active lane together.
+// The reference runs the same rules with a divergent switch per thread,
+// which on a SIMT machine serialises the memory round trips of the
+// different rules; here a warp pays about one round trip per phase.
 
 enum : int { IR_DONE = 0, IR_RETRY = 1, IR_FATAL = 2 };
 
-// Publishes this thread's node/var creations before they become reachable
-// from another thread through a link.
-__device__ __forceinline__ void publish() { __threadfence(); }
+// What one lane does this round.
+struct Plan {
+  Port a, b;            // ports after the swap (src/hvm.c:1090-1097)
+  Pair A, B;            // principal nodes of a and b (when the rule takes them)
+  uint32_t rule;        // LINK..SWIT; IDLE_RULE for a lane without a redex
+  uint32_t nlinks;      // port pairs to wire
+  uint32_t n0, n1, n2, n3, v0, v1, v2, v3;  // fresh words of COMM/OPER/SWIT
+  uint32_t node_len, rbag_len, vars_len, off;  // CALL: the def
+  Port root;            // CALL: the def's root
+  Numb cv;              // OPER: the result when both sides are numbers
+  bool oper_num;        // OPER: B1 is a number
+  bool counted;         // counts as an interaction (every rule but LINK)
+};
+constexpr uint32_t IDLE_RULE = 8;
 
-__device__ __forceinline__ int rule_eras(const Dev& d, TState& t, Port a, Port b) {
-  Pair B = nload(d, get_val(b));
-  if (B == 0) return IR_RETRY;
-  nstore(d, get_val(b), 0);
-  link(d, t, a, get_fst(B));
-  link(d, t, a, get_snd(B));
-  return IR_DONE;
-}
-
-__device__ __forceinline__ int rule_anni(const Dev& d, TState& t, Port a, Port b) {
-  Pair A = nload(d, get_val(a));
-  Pair B = nload(d, get_val(b));
-  if (A == 0 || B == 0) return IR_RETRY;
-  nstore(d, get_val(a), 0);
-  nstore(d, get_val(b), 0);
-  link(d, t, get_fst(A), get_fst(B));
-  link(d, t, get_snd(A), get_snd(B));
-  return IR_DONE;
-}
-
-__device__ __forceinline__ int rule_comm(const Dev& d, TState& t, Port a, Port b) {
-  Pair A = nload(d, get_val(a));
-  Pair B = nload(d, get_val(b));
-  if (A == 0 || B == 0) return IR_RETRY;
-  uint32_t n0 = alloc_node(d, t), n1 = alloc_node(d, t), n2 = alloc_node(d, t), n3 = alloc_node(d, t);
-  if (!n0 || !n1 || !n2 || !n3) { set_status(d, ST_OOM_NODES, t.gid); return IR_FATAL; }
-  uint32_t v0 = alloc_var(d, t), v1 = alloc_var(d, t), v2 = alloc_var(d, t), v3 = alloc_var(d, t);
-  if (!v0 || !v1 || !v2 || !v3) { set_status(d, ST_OOM_VARS, t.gid); return IR_FATAL; }
-  nstore(d, get_val(a), 0);
-  nstore(d, get_val(b), 0);
-  nstore(d, n0, new_pair(new_port(VAR, v0), new_port(VAR, v1)));
-  nstore(d, n1, new_pair(new_port(VAR, v2), new_port(VAR, v3)));
-  nstore(d, n2, new_pair(new_port(VAR, v0), new_port(VAR, v2)));
-  nstore(d, n3, new_pair(new_port(VAR, v1), new_port(VAR, v3)));
-  publish();
-  link(d, t, new_port(get_tag(b), n0), get_fst(A));
-  link(d, t, new_port(get_tag(b), n1), get_snd(A));
-  link(d, t, new_port(get_tag(a), n2), get_fst(B));
-  link(d, t, new_port(get_tag(a), n3), get_snd(B));
-  return IR_DONE;
-}
-
-__device__ __forceinline__ int rule_oper(const Dev& d, TState& t, Port a, Port b) {
-  Pair B = nload(d, get_val(b));
-  if (B == 0) return IR_RETRY;
-  nstore(d, get_val(b), 0);
-  Port b1 = get_fst(B);
-  Port b2 = enter(d, get_snd(B));
-  if (get_tag(b1) == NUM) {
-    link(d, t, new_port(NUM, operate(get_val(a), get_val(b1))), b2);
-  } else {
-    uint32_t n0 = alloc_node(d, t);
-    if (!n0) { set_status(d, ST_OOM_NODES, t.gid); return IR_FATAL; }
-    nstore(d, n0, new_pair(a, b2));
-    publish();
-    link(d, t, b1, new_port(OPR, n0));
-  }
-  return IR_DONE;
-}
-
-__device__ __forceinline__ int rule_swit(const Dev& d, TState& t, Port a, Port b) {
-  Pair B = nload(d, get_val(b));
-  if (B == 0) return IR_RETRY;
-  uint32_t n = get_u24(get_val(a));
-  uint32_t n0 = alloc_node(d, t);
-  uint32_t n1 = n == 0 ? 1u : alloc_node(d, t);
-  if (!n0 || !n1) { set_status(d, ST_OOM_NODES, t.gid); return IR_FATAL; }
-  nstore(d, get_val(b), 0);
-  if (n == 0) {
-    nstore(d, n0, new_pair(get_snd(B), new_port(ERA, 0)));
-  } else {
-    nstore(d, n0, new_pair(new_port(ERA, 0), new_port(CON, n1)));
-    nstore(d, n1, new_pair(new_port(NUM, new_u24(n - 1)), get_snd(B)));
-  }
-  publish();
-  link(d, t, new_port(CON, n0), get_fst(B));
-  return IR_DONE;
-}
-
-__device__ __forceinline__ Port relocate(const Dev& d, const TState& t, Port p) {
+__device__ __forceinline__ Port relocate(const Dev& d, uint32_t gid, Port p) {
   Tag tag = get_tag(p);
-  if (tag >= CON) return new_port(tag, d.nloc[(size_t)get_val(p) * d.nthreads + t.gid]);
-  if (tag == VAR) return new_port(VAR, d.vloc[(size_t)get_val(p) * d.nthreads + t.gid]);
+  if (tag >= CON) return new_port(tag, d.nloc[(size_t)get_val(p) * d.nthreads + gid]);
+  if (tag == VAR) return new_port(VAR, d.vloc[(size_t)get_val(p) * d.nthreads + gid]);
   return p;
 }
 
-__device__ int rule_call(const Dev& d, TState& t, Port a, Port b) {
-  uint32_t fid = get_val(a) & 0xFFFFFFFu;
-  if (fid >= d.ndefs) { set_status(d, ST_BAD_REF, fid); return IR_FATAL; }
-  const DefHdr h = d.defs[fid];
-  // Copy optimisation: a safe REF meeting a DUP is duplicated like an eraser.
-  if (h.safe && get_tag(b) == DUP) return rule_eras(d, t, a, b);
-  for (uint32_t i = 0; i < h.node_len; i++) {
-    uint32_t at = alloc_node(d, t);
-    if (!at) { set_status(d, ST_OOM_NODES, t.gid); return IR_FATAL; }
-    d.nloc[(size_t)i * d.nthreads + t.gid] = at;
+// The i-th port pair of the lane's rule (src/hvm.c:852-1070).
+__device__ __forceinline__ void link_pair(const Dev& d, uint32_t gid, const Plan& p, uint32_t i, Port& x, Port& y) {
+  switch (p.rule) {
+    case LINK: x = p.a; y = p.b; break;
+    case ERAS: x = p.a; y = i == 0 ? get_fst(p.B) : get_snd(p.B); break;
+    case ANNI:
+      x = i == 0 ? get_fst(p.A) : get_snd(p.A);
+      y = i == 0 ? get_fst(p.B) : get_snd(p.B);
+      break;
+    case COMM: {
+      uint32_t n = i == 0 ? p.n0 : i == 1 ? p.n1 : i == 2 ? p.n2 : p.n3;
+      x = new_port(i < 2 ? get_tag(p.b) : get_tag(p.a), n);
+      y = i == 0 ? get_fst(p.A) : i == 1 ? get_snd(p.A) : i == 2 ? get_fst(p.B) : get_snd(p.B);
+      break;
+    }
+    case OPER:
+      if (p.oper_num) { x = new_port(NUM, p.cv); y = get_snd(p.B); }
+      else { x = get_fst(p.B); y = new_port(OPR, p.n0); }
+      break;
+    case SWIT: x = new_port(CON, p.n0); y = get_fst(p.B); break;
+    default: {  // CALL
+      if (i < p.rbag_len) {
+        Pair q = __ldg((const unsigned long long*)&d.book[p.off + i]);
+        x = relocate(d, gid, get_fst(q));
+        y = relocate(d, gid, get_snd(q));
+      } else {
+        x = relocate(d, gid, p.root);
+        y = p.b;
+      }
+      break;
+    }
   }
-  for (uint32_t i = 0; i < h.vars_len; i++) {
-    uint32_t at = alloc_var(d, t);  // claimed as NONE: created
-    if (!at) { set_status(d, ST_OOM_VARS, t.gid); return IR_FATAL; }
-    d.vloc[(size_t)i * d.nthreads + t.gid] = at;
-  }
-  const Pair* nodes = d.book + h.off + h.rbag_len;
-  for (uint32_t i = 0; i < h.node_len; i++) {
-    Pair p = __ldg((const unsigned long long*)&nodes[i]);
-    nstore(d, d.nloc[(size_t)i * d.nthreads + t.gid],
-           new_pair(relocate(d, t, get_fst(p)), relocate(d, t, get_snd(p))));
-  }
-  publish();
-  const Pair* rbag = d.book + h.off;
-  for (uint32_t i = 0; i < h.rbag_len; i++) {
-    Pair p = __ldg((const unsigned long long*)&rbag[i]);
-    link(d, t, relocate(d, t, get_fst(p)), relocate(d, t, get_snd(p)));
-  }
-  link(d, t, relocate(d, t, h.root), b);
-  return IR_DONE;
 }
 
-// One interaction on redex `r` (src/hvm.c:1073-1122). Returns the rule run,
-// or -1 when the redex was pushed back for a re-try.
-__device__ __forceinline__ int interact(const Dev& d, TState& t, Pair r) {
+// Plans lane's interaction on redex r; returns false for an invalid REF.
+__device__ __forceinline__ bool plan_redex(const Dev& d, TState& t, Pair r, Plan& p) {
   Port a = get_fst(r), b = get_snd(r);
   Rule rule = get_rule(a, b);
-  if (get_tag(a) == REF && b == ROOT) {
-    rule = CALL;
-  } else if (should_swap(a, b)) {
-    Port x = a; a = b; b = x;
+  if (get_tag(a) == REF && b == ROOT) rule = CALL;
+  else if (should_swap(a, b)) { Port x = a; a = b; b = x; }
+  p.a = a; p.b = b;
+  p.counted = rule != LINK;
+  p.node_len = p.rbag_len = p.vars_len = 0;
+  if (rule == CALL) {
+    uint32_t fid = get_val(a) & 0xFFFFFFFu;
+    if (fid >= d.ndefs) { set_status(d, ST_BAD_REF, fid); t.dead = true; return false; }
+    const DefHdr h = d.defs[fid];
+    if (h.safe && get_tag(b) == DUP) {
+      rule = ERAS;  // copy optimisation (src/hvm.c:870-873): still one interaction
+    } else {
+      p.node_len = h.node_len; p.rbag_len = h.rbag_len; p.vars_len = h.vars_len;
+      p.off = h.off; p.root = h.root;
+    }
   }
-  int rc;
-  switch (rule) {
-    case LINK: link(d, t, a, b); rc = IR_DONE; break;
-    case CALL: rc = rule_call(d, t, a, b); break;
-    case VOID: rc = IR_DONE; break;
-    case ERAS: rc = rule_eras(d, t, a, b); break;
-    case ANNI: rc = rule_anni(d, t, a, b); break;
-    case COMM: rc = rule_comm(d, t, a, b); break;
-    case OPER: rc = rule_oper(d, t, a, b); break;
-    default:   rc = rule_swit(d, t, a, b); break;
+  p.rule = rule;
+  return true;
+}
+
+// Runs one round for the warp: every lane with `has` interacts on `r`.
+// Returns the lane's outcome (IR_DONE / IR_RETRY / IR_FATAL).
+__device__ __forceinline__ int lockstep_round(const Dev& d, TState& t, bool has, Pair r) {
+  Plan p;
+  p.rule = IDLE_RULE;
+  p.nlinks = 0;
+  p.A = p.B = 0;
+  if (has && !plan_redex(d, t, r, p)) has = false;
+  const uint32_t rule = p.rule;
+
+  // 2. load the principal nodes
+  const bool needA = rule == ANNI || rule == COMM;
+  const bool needB = rule == ERAS || rule == ANNI || rule == COMM || rule == OPER || rule == SWIT;
+  if (needA) p.A = nload(d, get_val(p.a));
+  if (needB) p.B = nload(d, get_val(p.b));
+  int rc = IR_DONE;
+  if ((needA && p.A == 0) || (needB && p.B == 0)) rc = IR_RETRY;  // not yet visible: re-try later
+
+  // 3. allocate; 4. write
+  bool made = false;
+  if (rc == IR_DONE && rule != IDLE_RULE) {
+    if (needA) nstore(d, get_val(p.a), 0);
+    if (needB) nstore(d, get_val(p.b), 0);
+    switch (rule) {
+      case LINK: p.nlinks = 1; break;
+      case VOID: p.nlinks = 0; break;
+      case ERAS: case ANNI: p.nlinks = 2; break;
+      case COMM: {
+        p.n0 = alloc_node(d, t); p.n1 = alloc_node(d, t); p.n2 = alloc_node(d, t); p.n3 = alloc_node(d, t);
+        p.v0 = alloc_var(d, t); p.v1 = alloc_var(d, t); p.v2 = alloc_var(d, t); p.v3 = alloc_var(d, t);
+        if (!(p.n0 && p.n1 && p.n2 && p.n3 && p.v0 && p.v1 && p.v2 && p.v3)) { rc = IR_FATAL; break; }
+        nstore(d, p.n0, new_pair(new_port(VAR, p.v0), new_port(VAR, p.v1)));
+        nstore(d, p.n1, new_pair(new_port(VAR, p.v2), new_port(VAR, p.v3)));
+        nstore(d, p.n2, new_pair(new_port(VAR, p.v0), new_port(VAR, p.v2)));
+        nstore(d, p.n3, new_pair(new_port(VAR, p.v1), new_port(VAR, p.v3)));
+        made = true;
+        p.nlinks = 4;
+        break;
+      }
+      case OPER: {
+        Port b1 = get_fst(p.B);
+        p.oper_num = get_tag(b1) == NUM;
+        if (p.oper_num) {
+          p.cv = operate(get_val(p.a), get_val(b1));
+        } else {
+          p.n0 = alloc_node(d, t);
+          if (!p.n0) { rc = IR_FATAL; break; }
+          nstore(d, p.n0, new_pair(p.a, get_snd(p.B)));
+          made = true;
+        }
+        p.nlinks = 1;
+        break;
+      }
+      case SWIT: {
+        uint32_t n = get_u24(get_val(p.a));
+        p.n0 = alloc_node(d, t);
+        p.n1 = n == 0 ? 1u : alloc_node(d, t);
+        if (!p.n0 || !p.n1) { rc = IR_FATAL; break; }
+        if (n == 0) {
+          nstore(d, p.n0, new_pair(get_snd(p.B), new_port(ERA, 0)));
+        } else {
+          nstore(d, p.n0, new_pair(new_port(ERA, 0), new_port(CON, p.n1)));
+          nstore(d, p.n1, new_pair(new_port(NUM, new_u24(n - 1)), get_snd(p.B)));
+        }
+        made = true;
+        p.nlinks = 1;
+        break;
+      }
+      default: {  // CALL (src/hvm.c:865-898)
+        for (uint32_t i = 0; i < p.node_len && rc == IR_DONE; i++) {
+          uint32_t at = alloc_node(d, t);
+          if (!at) rc = IR_FATAL;
+          d.nloc[(size_t)i * d.nthreads + t.gid] = at;
+        }
+        for (uint32_t i = 0; i < p.vars_len && rc == IR_DONE; i++) {
+          uint32_t at = alloc_var(d, t);  // a taken var word is already NONE
+          if (!at) rc = IR_FATAL;
+          d.vloc[(size_t)i * d.nthreads + t.gid] = at;
+        }
+        if (rc != IR_DONE) break;
+        const Pair* nodes = d.book + p.off + p.rbag_len;
+        for (uint32_t i = 0; i < p.node_len; i++) {
+          Pair q = __ldg((const unsigned long long*)&nodes[i]);
+          nstore(d, d.nloc[(size_t)i * d.nthreads + t.gid],
+                 new_pair(relocate(d, t.gid, get_fst(q)), relocate(d, t.gid, get_snd(q))));
+        }
+        made = p.node_len > 0 || p.vars_len > 0;
+        p.nlinks = p.rbag_len + 1;
+        break;
+      }
+    }
+    if (rc == IR_FATAL) {
+      set_status(d, ST_OOM_NODES, t.gid);  // a node or var page list / pool ran out
+      t.dead = true;
+    }
   }
-  if (rc == IR_RETRY) {
-    push(d, t, r);
-    t.retries++;
-    return -1;
+
+  // 5. one fence for the warp if any lane created words
+  if (__any_sync(0xFFFFFFFFu, made)) __threadfence();
+
+  // 6. link, one exchange per step
+  if (rc != IR_DONE) p.nlinks = 0;
+  uint32_t next = 0;
+  bool busy = false, entered = false;
+  Port X = 0, Y = 0;
+  for (uint32_t guard = 0; guard < (1u << 24); guard++) {
+    // Resolve, without memory traffic, every pair that needs no exchange.
+    while (!busy && next < p.nlinks) {
+      link_pair(d, t.gid, p, next++, X, Y);
+      if (get_tag(X) != VAR && get_tag(Y) == VAR) { Port z = X; X = Y; Y = z; }
+      if (get_tag(X) != VAR) push(d, t, new_pair(X, Y));  // both sides principal: a redex
+      else { busy = true; entered = false; }
+    }
+    if (!__any_sync(0xFFFFFFFFu, busy)) break;
+    if (busy) {
+      // Enter Y while it is a var (src/hvm.c:793-808), then publish X -> Y.
+      const bool enter_step = !entered && get_tag(Y) == VAR;
+      const uint32_t addr = enter_step ? get_val(Y) : get_val(X);
+      const Port put = enter_step ? NONE : Y;
+      const Port got = vexch(d, addr, put);
+      if (enter_step) {
+        if (got == NONE || got == 0) entered = true;
+        else { vstore(d, addr, 0); Y = got; }
+      } else if (got == NONE) {
+        busy = false;
+      } else if (got == 0) {
+        set_status(d, ST_LINK_UNSET, addr); t.dead = true; busy = false;
+      } else {
+        vstore(d, addr, 0);
+        X = got;
+        entered = false;
+        // X now holds what the other side published: re-normalise.
+        if (get_tag(X) != VAR && get_tag(Y) == VAR) { Port z = X; X = Y; Y = z; }
+        if (get_tag(X) != VAR) { push(d, t, new_pair(X, Y)); busy = false; }
+      }
+    }
   }
-  if (rc == IR_FATAL) { t.dead = true; return -1; }
-  if (rule != LINK) { t.itrs++; t.hist[rule]++; }
-  return rule;
+
+  if (has && rc == IR_RETRY) { push(d, t, r); t.retries++; }
+  if (has && rc == IR_DONE && p.counted) { t.itrs++; t.hist[rule]++; }
+  return rc;
 }
 
 }  // namespace hvm

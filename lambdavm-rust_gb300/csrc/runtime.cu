@@ -145,23 +145,55 @@ __global__ void __launch_bounds__(128, MIN_BLOCKS_128 > 0 ? MIN_BLOCKS_128 : 1) 
     push(d, t, (Pair)__ldcg((const unsigned long long*)&d.ring[at & d.ring_mask]));
   }
 
-  unsigned stop_seen = 0;
-  for (uint32_t left = budget; left > 0 && !t.dead && !stop_seen; left--) {
-    if (t.len == 0 && !claim(d, t, in_end, chunk)) {
-      // Out of work: count this thread dry (in batches of 16 per block); the
-      // count that crosses `stop_at` ends the turn for everyone.
-      unsigned k = atomicAdd(&blk_dry, 1u) + 1;
-      if ((k & 15) == 0) {
-        unsigned g = atomicAdd(&c->dry, 16u) + 16;
+  const unsigned lane = threadIdx.x & 31;
+  const unsigned lt_mask = (1u << lane) - 1;
+  Pair* warp_stk = t.stk - lane;  // lane j's deque starts at warp_stk + j
+  for (uint32_t round = 0; round < budget; round++) {
+    // Intra-warp balancing: each empty lane takes the oldest redex of a lane
+    // holding two or more (all in shared memory, no global traffic).
+    unsigned want = __ballot_sync(0xFFFFFFFFu, t.len == 0);
+    unsigned give = __ballot_sync(0xFFFFFFFFu, t.len >= 2);
+    if (want && give) {
+      unsigned m = min(__popc(want), __popc(give));
+      unsigned rw = __popc(want & lt_mask), rg = __popc(give & lt_mask);
+      bool recv = ((want >> lane) & 1) && rw < m;
+      int donor = recv ? (int)__fns(give, 0, rw + 1) : (int)lane;
+      unsigned dlo = __shfl_sync(0xFFFFFFFFu, t.lo, donor);
+      Pair got = recv ? warp_stk[(size_t)dlo * t.stride + donor] : 0;
+      __syncwarp();
+      if (((give >> lane) & 1) && rg < m) { t.lo = (t.lo + 1) & (t.cap - 1); t.len--; }
+      if (recv) push(d, t, got);
+    }
+    // Lanes still empty claim ring input, one atomic for the warp.
+    unsigned empty = __ballot_sync(0xFFFFFFFFu, t.len == 0);
+    if (empty) {
+      unsigned long long h = 0;
+      if (lane == 0) {
+        h = ldcg64(&c->head);
+        if (h < in_end) h = atomicAdd(&c->head, (unsigned long long)__popc(empty));
+      }
+      h = __shfl_sync(0xFFFFFFFFu, h, 0);
+      unsigned k = __popc(empty & lt_mask);
+      if (((empty >> lane) & 1) && h + k < in_end) {
+        push(d, t, (Pair)__ldcg((const unsigned long long*)&d.ring[(h + k) & d.ring_mask]));
+      }
+    }
+    if (!__any_sync(0xFFFFFFFFu, t.len > 0)) {
+      // The whole warp ran dry: count it; enough dry threads end the turn.
+      if (lane == 0) {
+        unsigned g = atomicAdd(&c->dry, 32u) + 32;
         if (g >= stop_at) atomicExch(&c->stop, 1u);
       }
       break;
     }
-    // The stop flag is loaded before the interaction and tested after it, so
-    // its latency hides behind the interaction's own memory traffic.
-    unsigned stop_now = *(volatile unsigned*)&c->stop;
-    interact(d, t, pop(t));
-    stop_seen = stop_now;
+    // The stop flag is loaded before the round and tested after it, so its
+    // latency hides behind the round's own memory traffic.
+    unsigned stop_now = lane == 0 ? *(volatile unsigned*)&c->stop : 0;
+    const bool has = t.len > 0;
+    const Pair r = has ? pop(t) : 0;
+    lockstep_round(d, t, has, r);
+    if (__any_sync(0xFFFFFFFFu, t.dead)) break;
+    if (__shfl_sync(0xFFFFFFFFu, stop_now, 0)) break;
   }
 
   alloc_save(d.nspace, t.gid, t.na);
@@ -169,7 +201,6 @@ __global__ void __launch_bounds__(128, MIN_BLOCKS_128 > 0 ? MIN_BLOCKS_128 : 1) 
 
   // Flush the LIFO to the ring tail, one atomic per warp.
   __syncwarp();
-  const unsigned lane = threadIdx.x & 31;
   uint32_t n = t.len, incl = n;
   for (int o = 1; o < 32; o <<= 1) {
     uint32_t y = __shfl_up_sync(0xFFFFFFFFu, incl, o);
@@ -380,9 +411,10 @@ class Runtime {
     if (block != 128 && cfg.reg_cap_blocks) return fail("reg_cap_blocks needs threads_per_block = 128");
     switch (cfg.reg_cap_blocks) {
       case 0: turn_fn = turn_kernel<0>; break;
+      case 8: turn_fn = turn_kernel<8>; break;
       case 12: turn_fn = turn_kernel<12>; break;
       case 16: turn_fn = turn_kernel<16>; break;
-      default: return fail("reg_cap_blocks must be 0, 12 or 16");
+      default: return fail("reg_cap_blocks must be 0, 8, 12 or 16");
     }
     if (block > 128 && cfg.reg_cap_blocks == 0) turn_fn = turn_kernel<0>;
     CK(cudaFuncSetAttribute(turn_fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
