@@ -74,6 +74,7 @@ typedef struct {
   uint32_t stop_frac_q8;      /* a turn ends once busy threads < (1 - f/256) x initially busy */
   uint32_t trace_cap;         /* record up to this many turns (0 = off), see hvm_gb300_trace */
   uint32_t reg_cap_blocks;    /* 0, or 8/12/16: cap registers so that many 128-thread blocks fit per SM */
+  uint32_t profile;           /* 1 = collect per-warp round counters into hvm_gb300_stats.prof */
 } hvm_gb300_config;
 
 typedef struct {
@@ -82,6 +83,8 @@ typedef struct {
   uint64_t turns;         /* evaluator turns run */
   uint64_t retries;       /* availability re-tries */
   uint64_t rule_hist[8];  /* interactions per rule: LINK CALL VOID ERAS ANNI COMM OPER SWIT */
+  uint64_t prof[8];       /* with profile=1: rounds, busy lanes, link steps, warp cycles in
+                             the turn loop, and in the load / write / fence / link phases */
   double seconds;         /* wall time inside normalisation */
   uint32_t threads, grid, block;
 } hvm_gb300_stats;

@@ -42,6 +42,7 @@ class Config(ctypes.Structure):
         ("stop_frac_q8", ctypes.c_uint32),
         ("trace_cap", ctypes.c_uint32),
         ("reg_cap_blocks", ctypes.c_uint32),
+        ("profile", ctypes.c_uint32),
     ]
 
 
@@ -64,6 +65,7 @@ class _Stats(ctypes.Structure):
         ("turns", ctypes.c_uint64),
         ("retries", ctypes.c_uint64),
         ("rule_hist", ctypes.c_uint64 * 8),
+        ("prof", ctypes.c_uint64 * 8),
         ("seconds", ctypes.c_double),
         ("threads", ctypes.c_uint32),
         ("grid", ctypes.c_uint32),
@@ -167,6 +169,7 @@ class RunStats:
     grid: int
     block: int
     rule_hist: dict = field(default_factory=dict)
+    prof: tuple = ()
 
     @property
     def mips(self) -> float:
@@ -211,7 +214,8 @@ class Runtime:
         self._check(lib().hvm_gb300_run(self._h, ctypes.byref(st)))
         return RunStats(itrs=st.itrs, leak=st.leak, turns=st.turns, retries=st.retries, seconds=st.seconds,
                         threads=st.threads, grid=st.grid, block=st.block,
-                        rule_hist={RULE_NAMES[i]: int(st.rule_hist[i]) for i in range(8)})
+                        rule_hist={RULE_NAMES[i]: int(st.rule_hist[i]) for i in range(8)},
+                        prof=tuple(int(x) for x in st.prof))
 
     def result(self) -> str:
         n = ctypes.c_size_t()

@@ -78,6 +78,8 @@ struct alignas(128) Ctl {
   unsigned int policy;              // 0 = fixed policy
   unsigned int pad_c[1];
   unsigned long long hist[8];       // interactions per rule (diagnostic)
+  unsigned long long prof[8];       // profile counters (when prof_on): see PROF_*
+  unsigned int prof_on;
   unsigned int npool_next;          // next page id of the node pool
   unsigned int vpool_next;          // next page id of the var pool
   TurnRecord* trace;                // per-turn records (null = off)
@@ -321,6 +323,10 @@ __device__ __forceinline__ void alloc_save(const PagedSpace& sp, uint32_t gid, c
 
 enum : int { IR_DONE = 0, IR_RETRY = 1, IR_FATAL = 2 };
 
+// Profile counters (per warp, lane 0, summed into Ctl::prof when enabled).
+enum { PROF_ROUNDS, PROF_LANES, PROF_STEPS, PROF_CYC_ROUND, PROF_CYC_LOAD, PROF_CYC_WRITE, PROF_CYC_FENCE, PROF_CYC_LINK };
+struct WarpProf { unsigned long long v[8]; };
+
 // What one lane does this round.
 struct Plan {
   Port a, b;            // ports after the swap (src/hvm.c:1090-1097)
@@ -403,7 +409,8 @@ __device__ __forceinline__ bool plan_redex(const Dev& d, TState& t, Pair r, Plan
 
 // Runs one round for the warp: every lane with `has` interacts on `r`.
 // Returns the lane's outcome (IR_DONE / IR_RETRY / IR_FATAL).
-__device__ __forceinline__ int lockstep_round(const Dev& d, TState& t, bool has, Pair r) {
+__device__ __forceinline__ int lockstep_round(const Dev& d, TState& t, bool has, Pair r, WarpProf* wp) {
+  long long c0 = wp ? clock64() : 0;
   Plan p;
   p.rule = IDLE_RULE;
   p.nlinks = 0;
@@ -418,6 +425,8 @@ __device__ __forceinline__ int lockstep_round(const Dev& d, TState& t, bool has,
   if (needB) p.B = nload(d, get_val(p.b));
   int rc = IR_DONE;
   if ((needA && p.A == 0) || (needB && p.B == 0)) rc = IR_RETRY;  // not yet visible: re-try later
+  long long c1 = 0;
+  if (wp) { __syncwarp(); c1 = clock64(); }
 
   // 3. allocate; 4. write
   bool made = false;
@@ -498,8 +507,12 @@ __device__ __forceinline__ int lockstep_round(const Dev& d, TState& t, bool has,
     }
   }
 
+  long long c2 = 0, c3 = 0;
+  if (wp) { __syncwarp(); c2 = clock64(); }
   // 5. one fence for the warp if any lane created words
   if (__any_sync(0xFFFFFFFFu, made)) __threadfence();
+  if (wp) c3 = clock64();
+  uint32_t steps = 0;
 
   // 6. link, one exchange per step
   if (rc != IR_DONE) p.nlinks = 0;
@@ -515,6 +528,7 @@ __device__ __forceinline__ int lockstep_round(const Dev& d, TState& t, bool has,
       else { busy = true; entered = false; }
     }
     if (!__any_sync(0xFFFFFFFFu, busy)) break;
+    steps++;
     if (busy) {
       // Enter Y while it is a var (src/hvm.c:793-808), then publish X -> Y.
       const bool enter_step = !entered && get_tag(Y) == VAR;
@@ -539,6 +553,17 @@ __device__ __forceinline__ int lockstep_round(const Dev& d, TState& t, bool has,
     }
   }
 
+  if (wp) {
+    long long c4 = clock64();
+    wp->v[PROF_ROUNDS] += 1;
+    wp->v[PROF_LANES] += __popc(__ballot_sync(0xFFFFFFFFu, has));
+    wp->v[PROF_STEPS] += steps;
+    wp->v[PROF_CYC_ROUND] += c4 - c0;
+    wp->v[PROF_CYC_LOAD] += c1 - c0;
+    wp->v[PROF_CYC_WRITE] += c2 - c1;
+    wp->v[PROF_CYC_FENCE] += c3 - c2;
+    wp->v[PROF_CYC_LINK] += c4 - c3;
+  }
   if (has && rc == IR_RETRY) { push(d, t, r); t.retries++; }
   if (has && rc == IR_DONE && p.counted) { t.itrs++; t.hist[rule]++; }
   return rc;

@@ -148,6 +148,10 @@ __global__ void __launch_bounds__(128, MIN_BLOCKS_128 > 0 ? MIN_BLOCKS_128 : 1) 
   const unsigned lane = threadIdx.x & 31;
   const unsigned lt_mask = (1u << lane) - 1;
   Pair* warp_stk = t.stk - lane;  // lane j's deque starts at warp_stk + j
+  WarpProf prof;
+  const bool prof_on = __ldcg(&c->prof_on) != 0;
+  for (int i = 0; i < 8; i++) prof.v[i] = 0;
+  long long t_loop = clock64();
   for (uint32_t round = 0; round < budget; round++) {
     // Intra-warp balancing: each empty lane takes the oldest redex of a lane
     // holding two or more (all in shared memory, no global traffic).
@@ -191,11 +195,15 @@ __global__ void __launch_bounds__(128, MIN_BLOCKS_128 > 0 ? MIN_BLOCKS_128 : 1) 
     unsigned stop_now = lane == 0 ? *(volatile unsigned*)&c->stop : 0;
     const bool has = t.len > 0;
     const Pair r = has ? pop(t) : 0;
-    lockstep_round(d, t, has, r);
+    lockstep_round(d, t, has, r, prof_on ? &prof : nullptr);
     if (__any_sync(0xFFFFFFFFu, t.dead)) break;
     if (__shfl_sync(0xFFFFFFFFu, stop_now, 0)) break;
   }
 
+  if (prof_on && lane == 0) {
+    prof.v[PROF_CYC_ROUND] = clock64() - t_loop;  // whole loop, including balancing and claims
+    for (int i = 0; i < 8; i++) if (prof.v[i]) atomicAdd(&c->prof[i], prof.v[i]);
+  }
   alloc_save(d.nspace, t.gid, t.na);
   alloc_save(d.vspace, t.gid, t.va);
 
@@ -471,6 +479,7 @@ class Runtime {
     CK(cudaMemset(mem_node, 0, (1ull << cfg.node_log2) * sizeof(Pair)));
     CK(cudaMemset(mem_vars, 0, (1ull << cfg.vars_log2) * sizeof(Port)));
     CK(cudaMemset(ctl, 0, sizeof(Ctl)));
+    if (cfg.profile) { uint32_t one = 1; CK(cudaMemcpy(&ctl->prof_on, &one, sizeof(one), cudaMemcpyHostToDevice)); }
     uint32_t frac = cfg.stop_frac_q8 ? cfg.stop_frac_q8 : 128;
     CK(cudaMemcpy(&ctl->stop_frac_q8, &frac, sizeof(frac), cudaMemcpyHostToDevice));
     if (cfg.trace_cap) {
@@ -781,6 +790,7 @@ class Runtime {
     st->turns = h.turns;
     st->retries = h.retries;
     for (int i = 0; i < 8; i++) st->rule_hist[i] = h.hist[i];
+    for (int i = 0; i < 8; i++) st->prof[i] = h.prof[i];
     st->seconds = norm_seconds;
     st->threads = d.nthreads;
     st->grid = grid;
