@@ -211,53 +211,76 @@ __device__ __forceinline__ unsigned int* pool_counter(const Dev& d, bool vars) {
   return vars ? &d.ctl->vpool_next : &d.ctl->npool_next;
 }
 
+// 256-bit load that bypasses L1 (sm_100+).
+__device__ __forceinline__ void ld_cg_v4(const void* p, unsigned long long& a, unsigned long long& b,
+                                         unsigned long long& c, unsigned long long& e) {
+  asm volatile("ld.global.cg.v4.u64 {%0,%1,%2,%3}, [%4];" : "=l"(a), "=l"(b), "=l"(c), "=l"(e) : "l"(p));
+}
+
+constexpr uint32_t CHUNK = 32;  // words per scanned chunk (256 B of nodes, 128 B of vars)
+
+// Bit i of the result is set when word base+i is free and may be handed out.
 template <bool VARS>
 __device__ __forceinline__ uint32_t chunk_mask(const Dev& d, uint32_t base) {
   uint32_t m = 0;
   if (!VARS) {
-    const ulonglong2* p = (const ulonglong2*)&d.node[base];
     #pragma unroll
-    for (int k = 0; k < 4; k++) {
-      ulonglong2 v = __ldcg(p + k);
-      m |= (v.x == 0 ? 1u : 0u) << (2 * k);
-      m |= (v.y == 0 ? 1u : 0u) << (2 * k + 1);
+    for (int k = 0; k < 8; k++) {
+      unsigned long long w0, w1, w2, w3;
+      ld_cg_v4(&d.node[base + 4 * k], w0, w1, w2, w3);
+      m |= ((w0 == 0) | (w1 == 0) << 1 | (w2 == 0) << 2 | (w3 == 0) << 3) << (4 * k);
     }
-    if (base == 0) m &= ~1u;
-    if (base + 8 > d.node_mask) m &= ~(1u << (d.node_mask - base));  // never the MARK word
+    if (base + CHUNK > d.node_mask) m &= ~(1u << (d.node_mask - base));  // never the MARK word
   } else {
-    const uint4* p = (const uint4*)&d.vars[base];
     #pragma unroll
     for (int k = 0; k < 4; k++) {
-      uint4 v = __ldcg(p + k);
-      m |= (v.x == 0 ? 1u : 0u) << (4 * k);
-      m |= (v.y == 0 ? 1u : 0u) << (4 * k + 1);
-      m |= (v.z == 0 ? 1u : 0u) << (4 * k + 2);
-      m |= (v.w == 0 ? 1u : 0u) << (4 * k + 3);
+      unsigned long long w0, w1, w2, w3;
+      ld_cg_v4(&d.vars[base + 8 * k], w0, w1, w2, w3);
+      uint32_t b8 = 0;
+      b8 |= ((uint32_t)w0 == 0) | ((uint32_t)(w0 >> 32) == 0) << 1;
+      b8 |= ((uint32_t)w1 == 0) << 2 | ((uint32_t)(w1 >> 32) == 0) << 3;
+      b8 |= ((uint32_t)w2 == 0) << 4 | ((uint32_t)(w2 >> 32) == 0) << 5;
+      b8 |= ((uint32_t)w3 == 0) << 6 | ((uint32_t)(w3 >> 32) == 0) << 7;
+      m |= b8 << (8 * k);
     }
-    if (base == 0) m &= ~1u;
-    if (base + 16 > d.vars_mask) m &= ~(1u << (d.vars_mask - base));  // ROOT
+    if (base + CHUNK > d.vars_mask) m &= ~(1u << (d.vars_mask - base));  // ROOT
   }
+  if (base == 0) m &= ~1u;
   return m;
 }
 
+// Bit i set iff bits i .. i+n-1 of m are all set (1 <= n <= 32).
+__device__ __forceinline__ uint32_t runs_of(uint32_t m, uint32_t n) {
+  uint32_t len = 1;
+  while (len * 2 <= n) { m &= m >> len; len <<= 1; }
+  if (len < n) m &= m >> (n - len);
+  return m;
+}
+
+// Takes n (1..32) consecutive free words of one chunk; returns the first, or
+// 0 when the page list is full and the pool is empty. Taken words are
+// written at once (vars as NONE, nodes as MARK) so no later scan can see them
+// free before their owner fills them.
 template <bool VARS>
-__device__ __forceinline__ uint32_t alloc_word(const Dev& d, TState& t, Alloc& a) {
+__device__ __forceinline__ uint32_t alloc_run(const Dev& d, TState& t, Alloc& a, uint32_t n) {
   const PagedSpace& sp = VARS ? d.vspace : d.nspace;
-  const uint32_t chunk_words = VARS ? 16u : 8u;
   const uint32_t page_words = 1u << sp.page_log2;
-  const uint32_t chunks_per_page = page_words / chunk_words;
+  const uint32_t chunks_per_page = page_words / CHUNK;
   for (uint32_t guard = 0; guard < (1u << 22); guard++) {
-    if (a.mask) {
-      uint32_t b = __ffs(a.mask) - 1;
-      a.mask &= a.mask - 1;
+    uint32_t r = runs_of(a.mask, n);
+    if (r) {
+      uint32_t b = __ffs(r) - 1;
+      a.mask &= ~((n == 32 ? ~0u : (1u << n) - 1) << b);
       uint32_t at = a.chunk + b;
-      if (VARS) vstore(d, at, NONE); else nstore(d, at, NODE_MARK);
+      for (uint32_t i = 0; i < n; i++) {
+        if (VARS) vstore(d, at + i, NONE); else nstore(d, at + i, NODE_MARK);
+      }
       return at;
     }
     // Next chunk: within the page, then the next owned page, then a new page.
     if (a.off >= page_words) {
       a.off = 0;
-      if (a.dry_chunks >= 2 * chunks_per_page || a.count == 1 && a.dry_chunks >= chunks_per_page) {
+      if (a.dry_chunks >= 2 * chunks_per_page || (a.count == 1 && a.dry_chunks >= chunks_per_page)) {
         if (a.count >= sp.max_pages) return 0;
         uint32_t fresh = atomicAdd(pool_counter(d, VARS), 1u);
         if (fresh >= (VARS ? d.vpool_end : d.npool_end)) return 0;
@@ -273,21 +296,21 @@ __device__ __forceinline__ uint32_t alloc_word(const Dev& d, TState& t, Alloc& a
       }
     }
     a.chunk = (a.page << sp.page_log2) + a.off;
-    a.off += chunk_words;
+    a.off += CHUNK;
     a.mask = chunk_mask<VARS>(d, a.chunk);
-    a.dry_chunks = a.mask ? 0 : a.dry_chunks + 1;
+    a.dry_chunks = runs_of(a.mask, n) ? 0 : a.dry_chunks + 1;
   }
   return 0;
 }
 
-__device__ __forceinline__ uint32_t alloc_node(const Dev& d, TState& t) { return alloc_word<false>(d, t, t.na); }
-__device__ __forceinline__ uint32_t alloc_var(const Dev& d, TState& t) { return alloc_word<true>(d, t, t.va); }
+__device__ __forceinline__ uint32_t alloc_node(const Dev& d, TState& t) { return alloc_run<false>(d, t, t.na, 1); }
+__device__ __forceinline__ uint32_t alloc_var(const Dev& d, TState& t) { return alloc_run<true>(d, t, t.va, 1); }
 
 // Loads a thread's allocator state at turn start; it resumes at the chunk it
 // was scanning when the previous turn ended.
 template <bool VARS>
 __device__ __forceinline__ void alloc_load(const PagedSpace& sp, uint32_t gid, Alloc& a) {
-  const uint32_t chunk_words = VARS ? 16u : 8u;
+  const uint32_t chunk_words = CHUNK;
   a.pos = sp.pos[gid];
   a.off = sp.off[gid];
   a.count = sp.counts[gid];
@@ -335,6 +358,8 @@ struct Plan {
   uint32_t nlinks;      // port pairs to wire
   uint32_t n0, n1, n2, n3, v0, v1, v2, v3;  // fresh words of COMM/OPER/SWIT
   uint32_t node_len, rbag_len, vars_len, off;  // CALL: the def
+  uint32_t nbase, vbase;  // CALL: first fresh node / var (contiguous runs), or
+  bool contig;            //       per-word scratch tables when the def is large
   Port root;            // CALL: the def's root
   Numb cv;              // OPER: the result when both sides are numbers
   bool oper_num;        // OPER: B1 is a number
@@ -342,8 +367,15 @@ struct Plan {
 };
 constexpr uint32_t IDLE_RULE = 8;
 
-__device__ __forceinline__ Port relocate(const Dev& d, uint32_t gid, Port p) {
+// Maps a def-local port to the fresh words of this CALL (adjust_port,
+// src/hvm.c:346-362): base + index for contiguous runs, else the scratch tables.
+__device__ __forceinline__ Port relocate(const Dev& d, uint32_t gid, const Plan& pl, Port p) {
   Tag tag = get_tag(p);
+  if (pl.contig) {
+    if (tag >= CON) return new_port(tag, pl.nbase + get_val(p));
+    if (tag == VAR) return new_port(VAR, pl.vbase + get_val(p));
+    return p;
+  }
   if (tag >= CON) return new_port(tag, d.nloc[(size_t)get_val(p) * d.nthreads + gid]);
   if (tag == VAR) return new_port(VAR, d.vloc[(size_t)get_val(p) * d.nthreads + gid]);
   return p;
@@ -372,10 +404,10 @@ __device__ __forceinline__ void link_pair(const Dev& d, uint32_t gid, const Plan
     default: {  // CALL
       if (i < p.rbag_len) {
         Pair q = __ldg((const unsigned long long*)&d.book[p.off + i]);
-        x = relocate(d, gid, get_fst(q));
-        y = relocate(d, gid, get_snd(q));
+        x = relocate(d, gid, p, get_fst(q));
+        y = relocate(d, gid, p, get_snd(q));
       } else {
-        x = relocate(d, gid, p.root);
+        x = relocate(d, gid, p, p.root);
         y = p.b;
       }
       break;
@@ -405,6 +437,52 @@ __device__ __forceinline__ bool plan_redex(const Dev& d, TState& t, Pair r, Plan
   }
   p.rule = rule;
   return true;
+}
+
+// One in-flight link A ~ B of the reference's linker (src/hvm.c:811-840),
+// advanced one exchange at a time.
+struct Slot {
+  Port X, Y;
+  bool busy, entered;
+};
+
+// Takes the lane's next port pairs into an idle slot, wiring on the spot every
+// pair that needs no exchange (both sides principal: a new redex).
+__device__ __forceinline__ void slot_fill(const Dev& d, TState& t, const Plan& p, uint32_t& next, Slot& s) {
+  while (!s.busy && next < p.nlinks) {
+    link_pair(d, t.gid, p, next++, s.X, s.Y);
+    if (get_tag(s.X) != VAR && get_tag(s.Y) == VAR) { Port z = s.X; s.X = s.Y; s.Y = z; }
+    if (get_tag(s.X) != VAR) push(d, t, new_pair(s.X, s.Y));
+    else { s.busy = true; s.entered = false; }
+  }
+}
+
+// The exchange this slot needs next: enter Y while it is a var
+// (src/hvm.c:793-808), then publish X -> Y.
+__device__ __forceinline__ void slot_request(const Slot& s, uint32_t& addr, Port& put) {
+  const bool enter_step = !s.entered && get_tag(s.Y) == VAR;
+  addr = enter_step ? get_val(s.Y) : get_val(s.X);
+  put = enter_step ? NONE : s.Y;
+}
+
+__device__ __forceinline__ void slot_result(const Dev& d, TState& t, Slot& s, uint32_t addr, Port got) {
+  if (!s.busy) return;
+  const bool enter_step = !s.entered && get_tag(s.Y) == VAR;
+  if (enter_step) {
+    if (got == NONE || got == 0) s.entered = true;
+    else { vstore(d, addr, 0); s.Y = got; }
+  } else if (got == NONE) {
+    s.busy = false;  // the other side will find Y here
+  } else if (got == 0) {
+    set_status(d, ST_LINK_UNSET, addr); t.dead = true; s.busy = false;
+  } else {
+    // The other side had published `got` for X: take X and wire got ~ Y.
+    vstore(d, addr, 0);
+    s.X = got;
+    s.entered = false;
+    if (get_tag(s.X) != VAR && get_tag(s.Y) == VAR) { Port z = s.X; s.X = s.Y; s.Y = z; }
+    if (get_tag(s.X) != VAR) { push(d, t, new_pair(s.X, s.Y)); s.busy = false; }
+  }
 }
 
 // Runs one round for the warp: every lane with `has` interacts on `r`.
@@ -479,22 +557,30 @@ __device__ __forceinline__ int lockstep_round(const Dev& d, TState& t, bool has,
         break;
       }
       default: {  // CALL (src/hvm.c:865-898)
-        for (uint32_t i = 0; i < p.node_len && rc == IR_DONE; i++) {
-          uint32_t at = alloc_node(d, t);
-          if (!at) rc = IR_FATAL;
-          d.nloc[(size_t)i * d.nthreads + t.gid] = at;
+        p.contig = p.node_len <= CHUNK && p.vars_len <= CHUNK;
+        if (p.contig) {
+          // Vars first (taken as NONE), then the nodes, written in place.
+          p.vbase = p.vars_len ? alloc_run<true>(d, t, t.va, p.vars_len) : 0;
+          p.nbase = p.node_len ? alloc_run<false>(d, t, t.na, p.node_len) : 0;
+          if ((p.vars_len && !p.vbase) || (p.node_len && !p.nbase)) { rc = IR_FATAL; break; }
+        } else {
+          for (uint32_t i = 0; i < p.node_len && rc == IR_DONE; i++) {
+            uint32_t at = alloc_node(d, t);
+            if (!at) rc = IR_FATAL;
+            d.nloc[(size_t)i * d.nthreads + t.gid] = at;
+          }
+          for (uint32_t i = 0; i < p.vars_len && rc == IR_DONE; i++) {
+            uint32_t at = alloc_var(d, t);
+            if (!at) rc = IR_FATAL;
+            d.vloc[(size_t)i * d.nthreads + t.gid] = at;
+          }
+          if (rc != IR_DONE) break;
         }
-        for (uint32_t i = 0; i < p.vars_len && rc == IR_DONE; i++) {
-          uint32_t at = alloc_var(d, t);  // a taken var word is already NONE
-          if (!at) rc = IR_FATAL;
-          d.vloc[(size_t)i * d.nthreads + t.gid] = at;
-        }
-        if (rc != IR_DONE) break;
         const Pair* nodes = d.book + p.off + p.rbag_len;
         for (uint32_t i = 0; i < p.node_len; i++) {
           Pair q = __ldg((const unsigned long long*)&nodes[i]);
-          nstore(d, d.nloc[(size_t)i * d.nthreads + t.gid],
-                 new_pair(relocate(d, t.gid, get_fst(q)), relocate(d, t.gid, get_snd(q))));
+          uint32_t at = p.contig ? p.nbase + i : d.nloc[(size_t)i * d.nthreads + t.gid];
+          nstore(d, at, new_pair(relocate(d, t.gid, p, get_fst(q)), relocate(d, t.gid, p, get_snd(q))));
         }
         made = p.node_len > 0 || p.vars_len > 0;
         p.nlinks = p.rbag_len + 1;
@@ -514,43 +600,25 @@ __device__ __forceinline__ int lockstep_round(const Dev& d, TState& t, bool has,
   if (wp) c3 = clock64();
   uint32_t steps = 0;
 
-  // 6. link, one exchange per step
+  // 6. link: two independent link chains per lane, one exchange each per
+  //    step, so a rule's pairs are wired two at a time.
   if (rc != IR_DONE) p.nlinks = 0;
   uint32_t next = 0;
-  bool busy = false, entered = false;
-  Port X = 0, Y = 0;
+  Slot s0, s1;
+  s0.busy = s1.busy = false;
   for (uint32_t guard = 0; guard < (1u << 24); guard++) {
-    // Resolve, without memory traffic, every pair that needs no exchange.
-    while (!busy && next < p.nlinks) {
-      link_pair(d, t.gid, p, next++, X, Y);
-      if (get_tag(X) != VAR && get_tag(Y) == VAR) { Port z = X; X = Y; Y = z; }
-      if (get_tag(X) != VAR) push(d, t, new_pair(X, Y));  // both sides principal: a redex
-      else { busy = true; entered = false; }
-    }
-    if (!__any_sync(0xFFFFFFFFu, busy)) break;
+    slot_fill(d, t, p, next, s0);
+    slot_fill(d, t, p, next, s1);
+    if (!__any_sync(0xFFFFFFFFu, s0.busy || s1.busy)) break;
     steps++;
-    if (busy) {
-      // Enter Y while it is a var (src/hvm.c:793-808), then publish X -> Y.
-      const bool enter_step = !entered && get_tag(Y) == VAR;
-      const uint32_t addr = enter_step ? get_val(Y) : get_val(X);
-      const Port put = enter_step ? NONE : Y;
-      const Port got = vexch(d, addr, put);
-      if (enter_step) {
-        if (got == NONE || got == 0) entered = true;
-        else { vstore(d, addr, 0); Y = got; }
-      } else if (got == NONE) {
-        busy = false;
-      } else if (got == 0) {
-        set_status(d, ST_LINK_UNSET, addr); t.dead = true; busy = false;
-      } else {
-        vstore(d, addr, 0);
-        X = got;
-        entered = false;
-        // X now holds what the other side published: re-normalise.
-        if (get_tag(X) != VAR && get_tag(Y) == VAR) { Port z = X; X = Y; Y = z; }
-        if (get_tag(X) != VAR) { push(d, t, new_pair(X, Y)); busy = false; }
-      }
-    }
+    uint32_t a0, a1;
+    Port q0, q1;
+    slot_request(s0, a0, q0);
+    slot_request(s1, a1, q1);
+    Port g0 = s0.busy ? vexch(d, a0, q0) : 0;
+    Port g1 = s1.busy ? vexch(d, a1, q1) : 0;
+    slot_result(d, t, s0, a0, g0);
+    slot_result(d, t, s1, a1, g1);
   }
 
   if (wp) {

@@ -443,7 +443,7 @@ class Runtime {
       while (l >= (int)min_log2 && (words >> l) < 2ull * nthreads) l--;
       return l < (int)min_log2 ? -1 : l;
     };
-    int nl = page_log2_for(n_nodes, 9, 3), vl = page_log2_for(n_vars, 10, 4);
+    int nl = page_log2_for(n_nodes, 9, 5), vl = page_log2_for(n_vars, 10, 5);
     if (nl < 0 || vl < 0) return fail("node/var space too small for the thread count");
     d.nspace.page_log2 = (uint32_t)nl;
     d.vspace.page_log2 = (uint32_t)vl;
