@@ -100,10 +100,12 @@ def test_hvm_cu_cli(hvm, tmp_path, workloads):
     assert lines[4].startswith("- MIPS: ")
 
 
-def test_errors_are_reported_not_hung(hvm, workloads):
-    # A node space too small for the net ends in an error status, not a hang.
-    with hvm.Runtime(device=0, node_log2=17, threads_per_block=32, blocks_per_sm=1) as r:
-        r.load(workloads.tree_sum(18))
+def test_errors_are_reported_not_hung(hvm, workloads, ref_programs):
+    # A node space too small for the net ends in an error status, not a hang:
+    # examples/sum_tree builds a 2^20-leaf tree (2^21 live nodes) first.
+    code = next(p["code"] for p in ref_programs if p["name"] == "examples/sum_tree/main.hvm")
+    with hvm.Runtime(device=0, node_log2=19, threads_per_block=32, blocks_per_sm=1) as r:
+        r.load(code)
         with pytest.raises(hvm.HvmError, match="out of node memory|ring"):
             r.run()
     # A turn budget that ends before the normal form is reported.
