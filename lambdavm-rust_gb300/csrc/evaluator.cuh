@@ -139,7 +139,8 @@ struct Alloc {
   uint32_t page;             // id of the page at `pos`
   uint32_t chunk;            // word index of the chunk `mask` describes
   uint32_t mask;             // free words of that chunk not yet handed out
-  uint32_t dry_chunks;       // chunks scanned since the last free word
+  uint32_t dry_chunks;       // chunks scanned since the last chunk with room
+  bool pool_dry;             // the page pool ran out during this turn
 };
 
 // ---- per-thread state ----------------------------------------------------------
@@ -218,6 +219,10 @@ __device__ __forceinline__ void ld_cg_v4(const void* p, unsigned long long& a, u
 }
 
 constexpr uint32_t CHUNK = 32;  // words per scanned chunk (256 B of nodes, 128 B of vars)
+// A lane that met this many chunks in a row without room takes a fresh page
+// (while its page list has space); after MAX_DRY_CHUNKS it gives up.
+constexpr uint32_t DRY_CHUNKS_FOR_NEW_PAGE = 4;
+constexpr uint32_t MAX_DRY_CHUNKS = 4096;
 
 // Bit i of the result is set when word base+i is free and may be handed out.
 template <bool VARS>
@@ -249,62 +254,68 @@ __device__ __forceinline__ uint32_t chunk_mask(const Dev& d, uint32_t base) {
   return m;
 }
 
-// Bit i set iff bits i .. i+n-1 of m are all set (1 <= n <= 32).
-__device__ __forceinline__ uint32_t runs_of(uint32_t m, uint32_t n) {
-  uint32_t len = 1;
-  while (len * 2 <= n) { m &= m >> len; len <<= 1; }
-  if (len < n) m &= m >> (n - len);
-  return m;
-}
-
-// Takes n (1..32) consecutive free words of one chunk; returns the first, or
-// 0 when the page list is full and the pool is empty. Taken words are
-// written at once (vars as NONE, nodes as MARK) so no later scan can see them
+// Takes n (1..32) free words of one chunk -- the n lowest free positions, not
+// necessarily adjacent -- and returns the chunk's first word with `used` =
+// the bit set of the words taken (word j of the run is the j-th set bit).
+// Returns 0 when the page list is full and the pool is empty. Taken words are
+// written at once (vars as NONE, nodes as MARK) so no later scan sees them
 // free before their owner fills them.
 template <bool VARS>
-__device__ __forceinline__ uint32_t alloc_run(const Dev& d, TState& t, Alloc& a, uint32_t n) {
+__device__ __forceinline__ uint32_t alloc_set(const Dev& d, TState& t, Alloc& a, uint32_t n, uint32_t& used) {
   const PagedSpace& sp = VARS ? d.vspace : d.nspace;
   const uint32_t page_words = 1u << sp.page_log2;
-  const uint32_t chunks_per_page = page_words / CHUNK;
   for (uint32_t guard = 0; guard < (1u << 22); guard++) {
-    uint32_t r = runs_of(a.mask, n);
-    if (r) {
-      uint32_t b = __ffs(r) - 1;
-      a.mask &= ~((n == 32 ? ~0u : (1u << n) - 1) << b);
-      uint32_t at = a.chunk + b;
-      for (uint32_t i = 0; i < n; i++) {
-        if (VARS) vstore(d, at + i, NONE); else nstore(d, at + i, NODE_MARK);
+    if ((uint32_t)__popc(a.mask) >= n) {
+      uint32_t m = a.mask, u = 0;
+      for (uint32_t i = 0; i < n; i++) { uint32_t lo = m & (0u - m); u |= lo; m ^= lo; }
+      a.mask = m;
+      used = u;
+      for (uint32_t w = u; w; w &= w - 1) {
+        uint32_t at = a.chunk + (__ffs(w) - 1);
+        if (VARS) vstore(d, at, NONE); else nstore(d, at, NODE_MARK);
       }
-      return at;
+      return a.chunk;
     }
-    // Next chunk: within the page, then the next owned page, then a new page.
-    if (a.off >= page_words) {
-      a.off = 0;
-      if (a.dry_chunks >= 2 * chunks_per_page || (a.count == 1 && a.dry_chunks >= chunks_per_page)) {
-        if (a.count >= sp.max_pages) return 0;
-        uint32_t fresh = atomicAdd(pool_counter(d, VARS), 1u);
-        if (fresh >= (VARS ? d.vpool_end : d.npool_end)) return 0;
+    // Next chunk: within the page, then the next owned page; after a few
+    // chunks with too few free words, a fresh page from the pool.
+    bool grabbed = false;
+    if (a.dry_chunks >= DRY_CHUNKS_FOR_NEW_PAGE && a.count < sp.max_pages && !a.pool_dry) {
+      uint32_t fresh = atomicAdd(pool_counter(d, VARS), 1u);
+      if (fresh < (VARS ? d.vpool_end : d.npool_end)) {
         sp.lists[(size_t)t.gid * sp.max_pages + a.count] = fresh;
         a.pos = a.count;
         a.count++;
         sp.counts[t.gid] = a.count;
         a.page = fresh;
+        a.off = 0;
         a.dry_chunks = 0;
+        grabbed = true;
       } else {
-        a.pos = a.pos + 1 == a.count ? 0 : a.pos + 1;
-        a.page = __ldcg(&sp.lists[(size_t)t.gid * sp.max_pages + a.pos]);
+        a.pool_dry = true;  // pool exhausted: keep cycling through owned pages
       }
+    }
+    if (!grabbed && a.off >= page_words) {
+      if (a.dry_chunks >= MAX_DRY_CHUNKS) return 0;  // every owned page is full
+      a.pos = a.pos + 1 == a.count ? 0 : a.pos + 1;
+      a.page = __ldcg(&sp.lists[(size_t)t.gid * sp.max_pages + a.pos]);
+      a.off = 0;
     }
     a.chunk = (a.page << sp.page_log2) + a.off;
     a.off += CHUNK;
     a.mask = chunk_mask<VARS>(d, a.chunk);
-    a.dry_chunks = runs_of(a.mask, n) ? 0 : a.dry_chunks + 1;
+    a.dry_chunks = (uint32_t)__popc(a.mask) >= n ? 0 : a.dry_chunks + 1;
   }
   return 0;
 }
 
-__device__ __forceinline__ uint32_t alloc_node(const Dev& d, TState& t) { return alloc_run<false>(d, t, t.na, 1); }
-__device__ __forceinline__ uint32_t alloc_var(const Dev& d, TState& t) { return alloc_run<true>(d, t, t.va, 1); }
+__device__ __forceinline__ uint32_t alloc_one(const Dev& d, TState& t, Alloc& a, bool vars) {
+  uint32_t used = 0;
+  uint32_t base = vars ? alloc_set<true>(d, t, a, 1, used) : alloc_set<false>(d, t, a, 1, used);
+  return base ? base + (__ffs(used) - 1) : (used ? (__ffs(used) - 1) : 0);
+}
+
+__device__ __forceinline__ uint32_t alloc_node(const Dev& d, TState& t) { return alloc_one(d, t, t.na, false); }
+__device__ __forceinline__ uint32_t alloc_var(const Dev& d, TState& t) { return alloc_one(d, t, t.va, true); }
 
 // Loads a thread's allocator state at turn start; it resumes at the chunk it
 // was scanning when the previous turn ended.
@@ -319,6 +330,7 @@ __device__ __forceinline__ void alloc_load(const PagedSpace& sp, uint32_t gid, A
   a.chunk = 0;
   a.mask = 0;
   a.dry_chunks = 0;
+  a.pool_dry = false;
 }
 
 __device__ __forceinline__ void alloc_save(const PagedSpace& sp, uint32_t gid, const Alloc& a) {
@@ -358,8 +370,9 @@ struct Plan {
   uint32_t nlinks;      // port pairs to wire
   uint32_t n0, n1, n2, n3, v0, v1, v2, v3;  // fresh words of COMM/OPER/SWIT
   uint32_t node_len, rbag_len, vars_len, off;  // CALL: the def
-  uint32_t nbase, vbase;  // CALL: first fresh node / var (contiguous runs), or
-  bool contig;            //       per-word scratch tables when the def is large
+  uint32_t nbase, vbase;  // CALL: chunk holding the fresh nodes / vars ...
+  uint32_t nused, vused;  //       ... at these bit positions (j-th word = j-th set bit),
+  bool contig;            //       or per-word scratch tables when the def is large
   Port root;            // CALL: the def's root
   Numb cv;              // OPER: the result when both sides are numbers
   bool oper_num;        // OPER: B1 is a number
@@ -372,8 +385,8 @@ constexpr uint32_t IDLE_RULE = 8;
 __device__ __forceinline__ Port relocate(const Dev& d, uint32_t gid, const Plan& pl, Port p) {
   Tag tag = get_tag(p);
   if (pl.contig) {
-    if (tag >= CON) return new_port(tag, pl.nbase + get_val(p));
-    if (tag == VAR) return new_port(VAR, pl.vbase + get_val(p));
+    if (tag >= CON) return new_port(tag, pl.nbase + __fns(pl.nused, 0, get_val(p) + 1));
+    if (tag == VAR) return new_port(VAR, pl.vbase + __fns(pl.vused, 0, get_val(p) + 1));
     return p;
   }
   if (tag >= CON) return new_port(tag, d.nloc[(size_t)get_val(p) * d.nthreads + gid]);
@@ -560,9 +573,10 @@ __device__ __forceinline__ int lockstep_round(const Dev& d, TState& t, bool has,
         p.contig = p.node_len <= CHUNK && p.vars_len <= CHUNK;
         if (p.contig) {
           // Vars first (taken as NONE), then the nodes, written in place.
-          p.vbase = p.vars_len ? alloc_run<true>(d, t, t.va, p.vars_len) : 0;
-          p.nbase = p.node_len ? alloc_run<false>(d, t, t.na, p.node_len) : 0;
-          if ((p.vars_len && !p.vbase) || (p.node_len && !p.nbase)) { rc = IR_FATAL; break; }
+          p.vused = p.nused = 0;
+          p.vbase = p.vars_len ? alloc_set<true>(d, t, t.va, p.vars_len, p.vused) : 0;
+          p.nbase = p.node_len ? alloc_set<false>(d, t, t.na, p.node_len, p.nused) : 0;
+          if ((p.vars_len && !p.vused) || (p.node_len && !p.nused)) { rc = IR_FATAL; break; }
         } else {
           for (uint32_t i = 0; i < p.node_len && rc == IR_DONE; i++) {
             uint32_t at = alloc_node(d, t);
@@ -579,7 +593,7 @@ __device__ __forceinline__ int lockstep_round(const Dev& d, TState& t, bool has,
         const Pair* nodes = d.book + p.off + p.rbag_len;
         for (uint32_t i = 0; i < p.node_len; i++) {
           Pair q = __ldg((const unsigned long long*)&nodes[i]);
-          uint32_t at = p.contig ? p.nbase + i : d.nloc[(size_t)i * d.nthreads + t.gid];
+          uint32_t at = p.contig ? p.nbase + __fns(p.nused, 0, i + 1) : d.nloc[(size_t)i * d.nthreads + t.gid];
           nstore(d, at, new_pair(relocate(d, t.gid, p, get_fst(q)), relocate(d, t.gid, p, get_snd(q))));
         }
         made = p.node_len > 0 || p.vars_len > 0;
