@@ -75,6 +75,7 @@ typedef struct {
   uint32_t trace_cap;         /* record up to this many turns (0 = off), see hvm_gb300_trace */
   uint32_t reg_cap_blocks;    /* 0, or 8/12/16: cap registers so that many 128-thread blocks fit per SM */
   uint32_t profile;           /* 1 = collect per-warp round counters into hvm_gb300_stats.prof */
+  uint32_t cache_cap;         /* recycled node / var words kept per thread (0 = no recycling) */
 } hvm_gb300_config;
 
 typedef struct {

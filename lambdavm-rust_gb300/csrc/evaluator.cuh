@@ -151,6 +151,9 @@ struct TState {
   uint32_t lo, len, cap;      // entries lo .. lo+len-1 (mod cap); cap is a power of two
   uint32_t gid;
   Alloc na, va;               // node / var allocators
+  uint32_t* ncache;           // recycled node words (shared memory, stride = blockDim.x)
+  uint32_t* vcache;           // recycled var words
+  uint32_t nfree, vfree, ccap;  // cached counts; capacity of each cache
   unsigned long long base;    // ring index of this turn's first input (overflow check)
   unsigned long long itrs, leak, retries;
   unsigned long long hist[8];
@@ -257,9 +260,9 @@ __device__ __forceinline__ uint32_t chunk_mask(const Dev& d, uint32_t base) {
 // Takes n (1..32) free words of one chunk -- the n lowest free positions, not
 // necessarily adjacent -- and returns the chunk's first word with `used` =
 // the bit set of the words taken (word j of the run is the j-th set bit).
-// Returns 0 when the page list is full and the pool is empty. Taken words are
-// written at once (vars as NONE, nodes as MARK) so no later scan sees them
-// free before their owner fills them.
+// Returns 0 when the page list is full and the pool is empty. Taken var words
+// are created (NONE) at once; callers write taken node words before their
+// next allocation, so no later scan can see them free while they are taken.
 template <bool VARS>
 __device__ __forceinline__ uint32_t alloc_set(const Dev& d, TState& t, Alloc& a, uint32_t n, uint32_t& used) {
   const PagedSpace& sp = VARS ? d.vspace : d.nspace;
@@ -270,9 +273,8 @@ __device__ __forceinline__ uint32_t alloc_set(const Dev& d, TState& t, Alloc& a,
       for (uint32_t i = 0; i < n; i++) { uint32_t lo = m & (0u - m); u |= lo; m ^= lo; }
       a.mask = m;
       used = u;
-      for (uint32_t w = u; w; w &= w - 1) {
-        uint32_t at = a.chunk + (__ffs(w) - 1);
-        if (VARS) vstore(d, at, NONE); else nstore(d, at, NODE_MARK);
+      if (VARS) {
+        for (uint32_t w = u; w; w &= w - 1) vstore(d, a.chunk + (__ffs(w) - 1), NONE);
       }
       return a.chunk;
     }
@@ -316,6 +318,49 @@ __device__ __forceinline__ uint32_t alloc_one(const Dev& d, TState& t, Alloc& a,
 
 __device__ __forceinline__ uint32_t alloc_node(const Dev& d, TState& t) { return alloc_one(d, t, t.na, false); }
 __device__ __forceinline__ uint32_t alloc_var(const Dev& d, TState& t) { return alloc_one(d, t, t.va, true); }
+
+// ---- recycling -----------------------------------------------------------------
+//
+// A node a lane takes (the principal nodes of its redex) and a var it
+// consumes (both ends linked) are unreachable from then on, so the lane may
+// reuse the word directly instead of zeroing it for the page owner's scan and
+// allocating another one. Each lane keeps up to `ccap` such words per space
+// in shared memory; when its cache is full, or at the end of the turn, it
+// releases words the reference's way, by writing 0 (src/hvm.c:688-694).
+
+__device__ __forceinline__ void free_node(const Dev& d, TState& t, uint32_t at) {
+  if (t.nfree < t.ccap) { t.ncache[(size_t)t.nfree * t.stride] = at; t.nfree++; }
+  else nstore(d, at, 0);
+}
+
+__device__ __forceinline__ void free_var(const Dev& d, TState& t, uint32_t at) {
+  if (t.vfree < t.ccap) { t.vcache[(size_t)t.vfree * t.stride] = at; t.vfree++; }
+  else vstore(d, at, 0);
+}
+
+// A node word for this lane: recycled if it has one, else from its pages.
+// The caller writes it before its next allocation.
+__device__ __forceinline__ uint32_t take_node(const Dev& d, TState& t) {
+  if (t.nfree) { t.nfree--; return t.ncache[(size_t)t.nfree * t.stride]; }
+  return alloc_node(d, t);
+}
+
+// A var word, created (NONE).
+__device__ __forceinline__ uint32_t take_var(const Dev& d, TState& t) {
+  if (t.vfree) {
+    t.vfree--;
+    uint32_t at = t.vcache[(size_t)t.vfree * t.stride];
+    vstore(d, at, NONE);
+    return at;
+  }
+  return alloc_var(d, t);
+}
+
+__device__ __forceinline__ void release_caches(const Dev& d, TState& t) {
+  for (uint32_t i = 0; i < t.nfree; i++) nstore(d, t.ncache[(size_t)i * t.stride], 0);
+  for (uint32_t i = 0; i < t.vfree; i++) vstore(d, t.vcache[(size_t)i * t.stride], 0);
+  t.nfree = t.vfree = 0;
+}
 
 // Loads a thread's allocator state at turn start; it resumes at the chunk it
 // was scanning when the previous turn ended.
@@ -370,32 +415,41 @@ struct Plan {
   uint32_t nlinks;      // port pairs to wire
   uint32_t n0, n1, n2, n3, v0, v1, v2, v3;  // fresh words of COMM/OPER/SWIT
   uint32_t node_len, rbag_len, vars_len, off;  // CALL: the def
-  uint32_t nbase, vbase;  // CALL: chunk holding the fresh nodes / vars ...
-  uint32_t nused, vused;  //       ... at these bit positions (j-th word = j-th set bit),
-  bool contig;            //       or per-word scratch tables when the def is large
+  // CALL: where the def's fresh words are. Mode CACHE: recycled words at
+  // cache slots base .. base+len-1; mode CHUNK: the words of chunk `base` at
+  // the set bits of `used` (j-th word = j-th set bit); mode TABLE: per-word
+  // scratch tables (defs larger than a chunk).
+  uint32_t nbase, vbase, nused, vused;
+  uint8_t nmode, vmode;
   Port root;            // CALL: the def's root
   Numb cv;              // OPER: the result when both sides are numbers
   bool oper_num;        // OPER: B1 is a number
   bool counted;         // counts as an interaction (every rule but LINK)
 };
 constexpr uint32_t IDLE_RULE = 8;
+enum : uint8_t { FROM_CACHE = 0, FROM_CHUNK = 1, FROM_TABLE = 2 };
 
 // Maps a def-local port to the fresh words of this CALL (adjust_port,
-// src/hvm.c:346-362): base + index for contiguous runs, else the scratch tables.
-__device__ __forceinline__ Port relocate(const Dev& d, uint32_t gid, const Plan& pl, Port p) {
+// src/hvm.c:346-362).
+__device__ __forceinline__ uint32_t fresh_node(const Dev& d, const TState& t, const Plan& pl, uint32_t j) {
+  if (pl.nmode == FROM_CACHE) return t.ncache[(size_t)(pl.nbase + j) * t.stride];
+  if (pl.nmode == FROM_CHUNK) return pl.nbase + __fns(pl.nused, 0, j + 1);
+  return d.nloc[(size_t)j * d.nthreads + t.gid];
+}
+__device__ __forceinline__ uint32_t fresh_var(const Dev& d, const TState& t, const Plan& pl, uint32_t j) {
+  if (pl.vmode == FROM_CACHE) return t.vcache[(size_t)(pl.vbase + j) * t.stride];
+  if (pl.vmode == FROM_CHUNK) return pl.vbase + __fns(pl.vused, 0, j + 1);
+  return d.vloc[(size_t)j * d.nthreads + t.gid];
+}
+__device__ __forceinline__ Port relocate(const Dev& d, const TState& t, const Plan& pl, Port p) {
   Tag tag = get_tag(p);
-  if (pl.contig) {
-    if (tag >= CON) return new_port(tag, pl.nbase + __fns(pl.nused, 0, get_val(p) + 1));
-    if (tag == VAR) return new_port(VAR, pl.vbase + __fns(pl.vused, 0, get_val(p) + 1));
-    return p;
-  }
-  if (tag >= CON) return new_port(tag, d.nloc[(size_t)get_val(p) * d.nthreads + gid]);
-  if (tag == VAR) return new_port(VAR, d.vloc[(size_t)get_val(p) * d.nthreads + gid]);
+  if (tag >= CON) return new_port(tag, fresh_node(d, t, pl, get_val(p)));
+  if (tag == VAR) return new_port(VAR, fresh_var(d, t, pl, get_val(p)));
   return p;
 }
 
 // The i-th port pair of the lane's rule (src/hvm.c:852-1070).
-__device__ __forceinline__ void link_pair(const Dev& d, uint32_t gid, const Plan& p, uint32_t i, Port& x, Port& y) {
+__device__ __forceinline__ void link_pair(const Dev& d, const TState& t, const Plan& p, uint32_t i, Port& x, Port& y) {
   switch (p.rule) {
     case LINK: x = p.a; y = p.b; break;
     case ERAS: x = p.a; y = i == 0 ? get_fst(p.B) : get_snd(p.B); break;
@@ -417,10 +471,10 @@ __device__ __forceinline__ void link_pair(const Dev& d, uint32_t gid, const Plan
     default: {  // CALL
       if (i < p.rbag_len) {
         Pair q = __ldg((const unsigned long long*)&d.book[p.off + i]);
-        x = relocate(d, gid, p, get_fst(q));
-        y = relocate(d, gid, p, get_snd(q));
+        x = relocate(d, t, p, get_fst(q));
+        y = relocate(d, t, p, get_snd(q));
       } else {
-        x = relocate(d, gid, p, p.root);
+        x = relocate(d, t, p, p.root);
         y = p.b;
       }
       break;
@@ -463,7 +517,7 @@ struct Slot {
 // pair that needs no exchange (both sides principal: a new redex).
 __device__ __forceinline__ void slot_fill(const Dev& d, TState& t, const Plan& p, uint32_t& next, Slot& s) {
   while (!s.busy && next < p.nlinks) {
-    link_pair(d, t.gid, p, next++, s.X, s.Y);
+    link_pair(d, t, p, next++, s.X, s.Y);
     if (get_tag(s.X) != VAR && get_tag(s.Y) == VAR) { Port z = s.X; s.X = s.Y; s.Y = z; }
     if (get_tag(s.X) != VAR) push(d, t, new_pair(s.X, s.Y));
     else { s.busy = true; s.entered = false; }
@@ -483,14 +537,14 @@ __device__ __forceinline__ void slot_result(const Dev& d, TState& t, Slot& s, ui
   const bool enter_step = !s.entered && get_tag(s.Y) == VAR;
   if (enter_step) {
     if (got == NONE || got == 0) s.entered = true;
-    else { vstore(d, addr, 0); s.Y = got; }
+    else { free_var(d, t, addr); s.Y = got; }
   } else if (got == NONE) {
     s.busy = false;  // the other side will find Y here
   } else if (got == 0) {
     set_status(d, ST_LINK_UNSET, addr); t.dead = true; s.busy = false;
   } else {
     // The other side had published `got` for X: take X and wire got ~ Y.
-    vstore(d, addr, 0);
+    free_var(d, t, addr);
     s.X = got;
     s.entered = false;
     if (get_tag(s.X) != VAR && get_tag(s.Y) == VAR) { Port z = s.X; s.X = s.Y; s.Y = z; }
@@ -519,23 +573,27 @@ __device__ __forceinline__ int lockstep_round(const Dev& d, TState& t, bool has,
   long long c1 = 0;
   if (wp) { __syncwarp(); c1 = clock64(); }
 
-  // 3. allocate; 4. write
+  // 3. take the principal nodes (recycled), allocate, 4. write
   bool made = false;
   if (rc == IR_DONE && rule != IDLE_RULE) {
-    if (needA) nstore(d, get_val(p.a), 0);
-    if (needB) nstore(d, get_val(p.b), 0);
+    if (needA) free_node(d, t, get_val(p.a));
+    if (needB) free_node(d, t, get_val(p.b));
     switch (rule) {
       case LINK: p.nlinks = 1; break;
       case VOID: p.nlinks = 0; break;
       case ERAS: case ANNI: p.nlinks = 2; break;
       case COMM: {
-        p.n0 = alloc_node(d, t); p.n1 = alloc_node(d, t); p.n2 = alloc_node(d, t); p.n3 = alloc_node(d, t);
-        p.v0 = alloc_var(d, t); p.v1 = alloc_var(d, t); p.v2 = alloc_var(d, t); p.v3 = alloc_var(d, t);
-        if (!(p.n0 && p.n1 && p.n2 && p.n3 && p.v0 && p.v1 && p.v2 && p.v3)) { rc = IR_FATAL; break; }
-        nstore(d, p.n0, new_pair(new_port(VAR, p.v0), new_port(VAR, p.v1)));
-        nstore(d, p.n1, new_pair(new_port(VAR, p.v2), new_port(VAR, p.v3)));
-        nstore(d, p.n2, new_pair(new_port(VAR, p.v0), new_port(VAR, p.v2)));
-        nstore(d, p.n3, new_pair(new_port(VAR, p.v1), new_port(VAR, p.v3)));
+        p.v0 = take_var(d, t); p.v1 = take_var(d, t); p.v2 = take_var(d, t); p.v3 = take_var(d, t);
+        if (!(p.v0 && p.v1 && p.v2 && p.v3)) { rc = IR_FATAL; break; }
+        p.n0 = take_node(d, t);
+        if (p.n0) nstore(d, p.n0, new_pair(new_port(VAR, p.v0), new_port(VAR, p.v1)));
+        p.n1 = take_node(d, t);
+        if (p.n1) nstore(d, p.n1, new_pair(new_port(VAR, p.v2), new_port(VAR, p.v3)));
+        p.n2 = take_node(d, t);
+        if (p.n2) nstore(d, p.n2, new_pair(new_port(VAR, p.v0), new_port(VAR, p.v2)));
+        p.n3 = take_node(d, t);
+        if (p.n3) nstore(d, p.n3, new_pair(new_port(VAR, p.v1), new_port(VAR, p.v3)));
+        if (!(p.n0 && p.n1 && p.n2 && p.n3)) { rc = IR_FATAL; break; }
         made = true;
         p.nlinks = 4;
         break;
@@ -546,7 +604,7 @@ __device__ __forceinline__ int lockstep_round(const Dev& d, TState& t, bool has,
         if (p.oper_num) {
           p.cv = operate(get_val(p.a), get_val(b1));
         } else {
-          p.n0 = alloc_node(d, t);
+          p.n0 = take_node(d, t);
           if (!p.n0) { rc = IR_FATAL; break; }
           nstore(d, p.n0, new_pair(p.a, get_snd(p.B)));
           made = true;
@@ -556,33 +614,39 @@ __device__ __forceinline__ int lockstep_round(const Dev& d, TState& t, bool has,
       }
       case SWIT: {
         uint32_t n = get_u24(get_val(p.a));
-        p.n0 = alloc_node(d, t);
-        p.n1 = n == 0 ? 1u : alloc_node(d, t);
-        if (!p.n0 || !p.n1) { rc = IR_FATAL; break; }
         if (n == 0) {
+          p.n0 = take_node(d, t);
+          if (!p.n0) { rc = IR_FATAL; break; }
           nstore(d, p.n0, new_pair(get_snd(p.B), new_port(ERA, 0)));
         } else {
-          nstore(d, p.n0, new_pair(new_port(ERA, 0), new_port(CON, p.n1)));
+          p.n1 = take_node(d, t);
+          if (!p.n1) { rc = IR_FATAL; break; }
           nstore(d, p.n1, new_pair(new_port(NUM, new_u24(n - 1)), get_snd(p.B)));
+          p.n0 = take_node(d, t);
+          if (!p.n0) { rc = IR_FATAL; break; }
+          nstore(d, p.n0, new_pair(new_port(ERA, 0), new_port(CON, p.n1)));
         }
         made = true;
         p.nlinks = 1;
         break;
       }
       default: {  // CALL (src/hvm.c:865-898)
-        p.contig = p.node_len <= CHUNK && p.vars_len <= CHUNK;
-        if (p.contig) {
-          // Vars first (taken as NONE), then the nodes, written in place.
-          p.vused = p.nused = 0;
-          p.vbase = p.vars_len ? alloc_set<true>(d, t, t.va, p.vars_len, p.vused) : 0;
-          p.nbase = p.node_len ? alloc_set<false>(d, t, t.na, p.node_len, p.nused) : 0;
-          if ((p.vars_len && !p.vused) || (p.node_len && !p.nused)) { rc = IR_FATAL; break; }
+        // Vars: recycled when the cache holds enough, else one chunk's free
+        // words, else (large defs) per-word scratch tables.
+        if (p.vars_len <= t.vfree) {
+          // The slots stay counted in `vfree` until the end of the round: the
+          // link phase relocates through them while it recycles more vars on
+          // top (see the compaction after the link phase).
+          p.vmode = FROM_CACHE;
+          p.vbase = t.vfree - p.vars_len;
+          for (uint32_t i = 0; i < p.vars_len; i++) vstore(d, t.vcache[(size_t)(p.vbase + i) * t.stride], NONE);
+        } else if (p.vars_len <= CHUNK) {
+          p.vmode = FROM_CHUNK;
+          p.vused = 0;
+          p.vbase = alloc_set<true>(d, t, t.va, p.vars_len, p.vused);
+          if (!p.vused) { rc = IR_FATAL; break; }
         } else {
-          for (uint32_t i = 0; i < p.node_len && rc == IR_DONE; i++) {
-            uint32_t at = alloc_node(d, t);
-            if (!at) rc = IR_FATAL;
-            d.nloc[(size_t)i * d.nthreads + t.gid] = at;
-          }
+          p.vmode = FROM_TABLE;
           for (uint32_t i = 0; i < p.vars_len && rc == IR_DONE; i++) {
             uint32_t at = alloc_var(d, t);
             if (!at) rc = IR_FATAL;
@@ -590,11 +654,29 @@ __device__ __forceinline__ int lockstep_round(const Dev& d, TState& t, bool has,
           }
           if (rc != IR_DONE) break;
         }
+        if (p.node_len <= t.nfree) {
+          p.nmode = FROM_CACHE;
+          t.nfree -= p.node_len;
+          p.nbase = t.nfree;
+        } else if (p.node_len <= CHUNK) {
+          p.nmode = FROM_CHUNK;
+          p.nused = 0;
+          p.nbase = alloc_set<false>(d, t, t.na, p.node_len, p.nused);
+          if (!p.nused) { rc = IR_FATAL; break; }
+        } else {
+          p.nmode = FROM_TABLE;
+          for (uint32_t i = 0; i < p.node_len && rc == IR_DONE; i++) {
+            uint32_t at = alloc_node(d, t);
+            if (!at) { rc = IR_FATAL; break; }
+            nstore(d, at, NODE_MARK);  // held until written below
+            d.nloc[(size_t)i * d.nthreads + t.gid] = at;
+          }
+          if (rc != IR_DONE) break;
+        }
         const Pair* nodes = d.book + p.off + p.rbag_len;
         for (uint32_t i = 0; i < p.node_len; i++) {
           Pair q = __ldg((const unsigned long long*)&nodes[i]);
-          uint32_t at = p.contig ? p.nbase + __fns(p.nused, 0, i + 1) : d.nloc[(size_t)i * d.nthreads + t.gid];
-          nstore(d, at, new_pair(relocate(d, t.gid, p, get_fst(q)), relocate(d, t.gid, p, get_snd(q))));
+          nstore(d, fresh_node(d, t, p, i), new_pair(relocate(d, t, p, get_fst(q)), relocate(d, t, p, get_snd(q))));
         }
         made = p.node_len > 0 || p.vars_len > 0;
         p.nlinks = p.rbag_len + 1;
@@ -635,6 +717,15 @@ __device__ __forceinline__ int lockstep_round(const Dev& d, TState& t, bool has,
     slot_result(d, t, s1, a1, g1);
   }
 
+  // Drop the var slots a CALL took from the cache; vars recycled during the
+  // link phase sit above them and move down.
+  if (rc == IR_DONE && rule == CALL && p.vmode == FROM_CACHE && p.vars_len) {
+    uint32_t top = p.vbase + p.vars_len;
+    for (uint32_t i = top; i < t.vfree; i++) {
+      t.vcache[(size_t)(i - p.vars_len) * t.stride] = t.vcache[(size_t)i * t.stride];
+    }
+    t.vfree -= p.vars_len;
+  }
   if (wp) {
     long long c4 = clock64();
     wp->v[PROF_ROUNDS] += 1;

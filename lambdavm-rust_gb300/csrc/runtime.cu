@@ -102,7 +102,7 @@ __device__ void fixed_policy(Ctl* c, unsigned long long pending, unsigned long l
 // MIN_BLOCKS_128 > 0 asks the compiler to fit that many 128-thread blocks per
 // SM (a register cap); the runtime picks the variant from the configuration.
 template <int MIN_BLOCKS_128>
-__global__ void __launch_bounds__(128, MIN_BLOCKS_128 > 0 ? MIN_BLOCKS_128 : 1) turn_kernel(Dev d, uint32_t cap) {
+__global__ void __launch_bounds__(128, MIN_BLOCKS_128 > 0 ? MIN_BLOCKS_128 : 1) turn_kernel(Dev d, uint32_t cap, uint32_t ccap) {
   extern __shared__ unsigned long long smem_stack[];
   Ctl* c = d.ctl;
   // Turn parameters are read once per block so every thread of the block
@@ -127,6 +127,10 @@ __global__ void __launch_bounds__(128, MIN_BLOCKS_128 > 0 ? MIN_BLOCKS_128 : 1) 
   TState t;
   t.stk = (Pair*)smem_stack + threadIdx.x;
   t.stride = blockDim.x;
+  t.ccap = ccap;
+  t.ncache = (uint32_t*)((Pair*)smem_stack + (size_t)cap * blockDim.x) + threadIdx.x;
+  t.vcache = t.ncache + (size_t)ccap * blockDim.x;
+  t.nfree = t.vfree = 0;
   t.lo = 0;
   t.len = 0;
   t.cap = cap;
@@ -204,6 +208,7 @@ __global__ void __launch_bounds__(128, MIN_BLOCKS_128 > 0 ? MIN_BLOCKS_128 : 1) 
     prof.v[PROF_CYC_ROUND] = clock64() - t_loop;  // whole loop, including balancing and claims
     for (int i = 0; i < 8; i++) if (prof.v[i]) atomicAdd(&c->prof[i], prof.v[i]);
   }
+  release_caches(d, t);
   alloc_save(d.nspace, t.gid, t.na);
   alloc_save(d.vspace, t.gid, t.va);
 
@@ -386,7 +391,8 @@ class Runtime {
   Port* g_out = nullptr; uint32_t* g_kids = nullptr; uint32_t* g_info = nullptr;
   uint32_t gather_cap = 0;
   uint32_t grid = 0, block = 0, cap = 0;
-  void (*turn_fn)(Dev, uint32_t) = nullptr;
+  void (*turn_fn)(Dev, uint32_t, uint32_t) = nullptr;
+  uint32_t ccap = 0;
   size_t smem = 0;
   uint32_t max_def_nodes = 1, max_def_vars = 1;
   int sms = 0;
@@ -415,7 +421,9 @@ class Runtime {
     if (cap < 2 || (cap & (cap - 1))) return fail("stack_cap must be a power of two >= 2");
     if (cfg.node_log2 < 10 || cfg.node_log2 > 29 || cfg.vars_log2 < 10 || cfg.vars_log2 > 29)
       return fail("node_log2/vars_log2 must be in [10, 29]");
-    smem = (size_t)block * cap * sizeof(Pair);
+    ccap = cfg.cache_cap;
+    if (ccap > 256) return fail("cache_cap must be <= 256");
+    smem = (size_t)block * cap * sizeof(Pair) + 2ull * block * ccap * sizeof(uint32_t);
     if (block != 128 && cfg.reg_cap_blocks) return fail("reg_cap_blocks needs threads_per_block = 128");
     switch (cfg.reg_cap_blocks) {
       case 0: turn_fn = turn_kernel<0>; break;
@@ -603,7 +611,7 @@ class Runtime {
     unsigned long long last_itrs = ~0ull, last_pending = ~0ull;
     Ctl h;
     for (;;) {
-      for (uint32_t i = 0; i < batch; i++) turn_fn<<<grid, block, smem>>>(d, cap);
+      for (uint32_t i = 0; i < batch; i++) turn_fn<<<grid, block, smem>>>(d, cap, ccap);
       CK(cudaGetLastError());
       turns_run += batch;
       if (read_ctl(h)) return -1;
@@ -817,7 +825,9 @@ extern "C" void hvm_gb300_default_config(hvm_gb300_config* c) {
   c->ring_log2 = 26;
   c->max_turns = 0;
   c->stop_frac_q8 = 128;
-  c->stack_cap = 16;
+  c->stack_cap = 8;
+  c->cache_cap = 16;
+  c->reg_cap_blocks = 8;
   c->trace_cap = 0;
 }
 
