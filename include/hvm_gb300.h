@@ -64,7 +64,7 @@ typedef struct hvm_gb300_runtime hvm_gb300_runtime;
 
 typedef struct {
   int32_t device;             /* CUDA device ordinal */
-  uint32_t threads_per_block; /* multiple of 32 */
+  uint32_t threads_per_block; /* multiple of 32, at most 128 */
   uint32_t stack_cap;         /* redexes per thread in the shared-memory LIFO */
   uint32_t blocks_per_sm;     /* 0 = as many as fit */
   uint32_t node_log2;         /* node space 2^k words (k <= 29, the port width) */

@@ -417,14 +417,14 @@ class Runtime {
     CK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, cfg.device));
     block = cfg.threads_per_block;
     cap = cfg.stack_cap;
-    if (block == 0 || block % 32 || block > 1024) return fail("threads_per_block must be a multiple of 32 in [32, 1024]");
+    if (block == 0 || block % 32 || block > 128) return fail("threads_per_block must be a multiple of 32 in [32, 128]");
     if (cap < 2 || (cap & (cap - 1))) return fail("stack_cap must be a power of two >= 2");
     if (cfg.node_log2 < 10 || cfg.node_log2 > 29 || cfg.vars_log2 < 10 || cfg.vars_log2 > 29)
       return fail("node_log2/vars_log2 must be in [10, 29]");
     ccap = cfg.cache_cap;
     if (ccap > 256) return fail("cache_cap must be <= 256");
     smem = (size_t)block * cap * sizeof(Pair) + 2ull * block * ccap * sizeof(uint32_t);
-    if (block != 128 && cfg.reg_cap_blocks) return fail("reg_cap_blocks needs threads_per_block = 128");
+    if (block > 128) return fail("threads_per_block must be <= 128");
     switch (cfg.reg_cap_blocks) {
       case 0: turn_fn = turn_kernel<0>; break;
       case 8: turn_fn = turn_kernel<8>; break;
@@ -432,7 +432,6 @@ class Runtime {
       case 16: turn_fn = turn_kernel<16>; break;
       default: return fail("reg_cap_blocks must be 0, 8, 12 or 16");
     }
-    if (block > 128 && cfg.reg_cap_blocks == 0) turn_fn = turn_kernel<0>;
     CK(cudaFuncSetAttribute(turn_fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     int per_sm = 0;
     CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, turn_fn, (int)block, smem));
