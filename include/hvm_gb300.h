@@ -84,8 +84,10 @@ typedef struct {
   uint64_t turns;         /* evaluator turns run */
   uint64_t retries;       /* availability re-tries */
   uint64_t rule_hist[8];  /* interactions per rule: LINK CALL VOID ERAS ANNI COMM OPER SWIT */
-  uint64_t prof[8];       /* with profile=1: rounds, busy lanes, link steps, warp cycles in
-                             the turn loop, and in the load / write / fence / link phases */
+  uint64_t prof[16];      /* with profile=1: rounds, busy lanes, link steps, warp cycles in
+                             the turn loop, and in the load / write / fence / link phases;
+                             CALL lanes and their lane cycles in var alloc / node alloc / node
+                             writes; COMM/OPER/SWIT lanes and lane cycles; lane cycles freeing */
   double seconds;         /* wall time inside normalisation */
   uint32_t threads, grid, block;
 } hvm_gb300_stats;

@@ -66,7 +66,7 @@ class _Stats(ctypes.Structure):
         ("turns", ctypes.c_uint64),
         ("retries", ctypes.c_uint64),
         ("rule_hist", ctypes.c_uint64 * 8),
-        ("prof", ctypes.c_uint64 * 8),
+        ("prof", ctypes.c_uint64 * 16),
         ("seconds", ctypes.c_double),
         ("threads", ctypes.c_uint32),
         ("grid", ctypes.c_uint32),

@@ -78,7 +78,7 @@ struct alignas(128) Ctl {
   unsigned int policy;              // 0 = fixed policy
   unsigned int pad_c[1];
   unsigned long long hist[8];       // interactions per rule (diagnostic)
-  unsigned long long prof[8];       // profile counters (when prof_on): see PROF_*
+  unsigned long long prof[16];      // profile counters (when prof_on): see PROF_*
   unsigned int prof_on;
   unsigned int npool_next;          // next page id of the node pool
   unsigned int vpool_next;          // next page id of the var pool
@@ -404,8 +404,10 @@ __device__ __forceinline__ void alloc_save(const PagedSpace& sp, uint32_t gid, c
 enum : int { IR_DONE = 0, IR_RETRY = 1, IR_FATAL = 2 };
 
 // Profile counters (per warp, lane 0, summed into Ctl::prof when enabled).
-enum { PROF_ROUNDS, PROF_LANES, PROF_STEPS, PROF_CYC_ROUND, PROF_CYC_LOAD, PROF_CYC_WRITE, PROF_CYC_FENCE, PROF_CYC_LINK };
-struct WarpProf { unsigned long long v[8]; };
+enum { PROF_ROUNDS, PROF_LANES, PROF_STEPS, PROF_CYC_ROUND, PROF_CYC_LOAD, PROF_CYC_WRITE, PROF_CYC_FENCE, PROF_CYC_LINK,
+       PROF_CALLS, PROF_CYC_CALL_VARS, PROF_CYC_CALL_NODES, PROF_CYC_CALL_WRITE, PROF_SMALL, PROF_CYC_SMALL,
+       PROF_CYC_FREE, PROF_SPARE };
+struct WarpProf { unsigned long long v[16]; };
 
 // What one lane does this round.
 struct Plan {
@@ -575,9 +577,12 @@ __device__ __forceinline__ int lockstep_round(const Dev& d, TState& t, bool has,
 
   // 3. take the principal nodes (recycled), allocate, 4. write
   bool made = false;
+  long long l0 = 0, l1 = 0, l2 = 0, l3 = 0, l4 = 0, lf = 0;
   if (rc == IR_DONE && rule != IDLE_RULE) {
+    if (wp) l0 = clock64();
     if (needA) free_node(d, t, get_val(p.a));
     if (needB) free_node(d, t, get_val(p.b));
+    if (wp) lf = clock64();
     switch (rule) {
       case LINK: p.nlinks = 1; break;
       case VOID: p.nlinks = 0; break;
@@ -654,6 +659,7 @@ __device__ __forceinline__ int lockstep_round(const Dev& d, TState& t, bool has,
           }
           if (rc != IR_DONE) break;
         }
+        if (wp) l1 = clock64();
         if (p.node_len <= t.nfree) {
           p.nmode = FROM_CACHE;
           t.nfree -= p.node_len;
@@ -673,11 +679,13 @@ __device__ __forceinline__ int lockstep_round(const Dev& d, TState& t, bool has,
           }
           if (rc != IR_DONE) break;
         }
+        if (wp) l2 = clock64();
         const Pair* nodes = d.book + p.off + p.rbag_len;
         for (uint32_t i = 0; i < p.node_len; i++) {
           Pair q = __ldg((const unsigned long long*)&nodes[i]);
           nstore(d, fresh_node(d, t, p, i), new_pair(relocate(d, t, p, get_fst(q)), relocate(d, t, p, get_snd(q))));
         }
+        if (wp) l3 = clock64();
         made = p.node_len > 0 || p.vars_len > 0;
         p.nlinks = p.rbag_len + 1;
         break;
@@ -687,6 +695,25 @@ __device__ __forceinline__ int lockstep_round(const Dev& d, TState& t, bool has,
       set_status(d, ST_OOM_NODES, t.gid);  // a node or var page list / pool ran out
       t.dead = true;
     }
+    if (wp) l4 = clock64();
+  }
+  if (wp) {
+    const bool is_call = rc == IR_DONE && rule == CALL;
+    const bool is_small = rc == IR_DONE && (rule == COMM || rule == OPER || rule == SWIT);
+    unsigned long long cv = is_call ? (unsigned long long)(l1 - lf) : 0;
+    unsigned long long cn = is_call ? (unsigned long long)(l2 - l1) : 0;
+    unsigned long long cw = is_call ? (unsigned long long)(l3 - l2) : 0;
+    unsigned long long cs = is_small ? (unsigned long long)(l4 - lf) : 0;
+    unsigned long long cf = (rc == IR_DONE && rule != IDLE_RULE) ? (unsigned long long)(lf - l0) : 0;
+    for (int o = 16; o > 0; o >>= 1) {
+      cv += __shfl_down_sync(0xFFFFFFFFu, cv, o); cn += __shfl_down_sync(0xFFFFFFFFu, cn, o);
+      cw += __shfl_down_sync(0xFFFFFFFFu, cw, o); cs += __shfl_down_sync(0xFFFFFFFFu, cs, o);
+      cf += __shfl_down_sync(0xFFFFFFFFu, cf, o);
+    }
+    wp->v[PROF_CALLS] += __popc(__ballot_sync(0xFFFFFFFFu, is_call));
+    wp->v[PROF_SMALL] += __popc(__ballot_sync(0xFFFFFFFFu, is_small));
+    wp->v[PROF_CYC_CALL_VARS] += cv; wp->v[PROF_CYC_CALL_NODES] += cn; wp->v[PROF_CYC_CALL_WRITE] += cw;
+    wp->v[PROF_CYC_SMALL] += cs; wp->v[PROF_CYC_FREE] += cf;
   }
 
   long long c2 = 0, c3 = 0;

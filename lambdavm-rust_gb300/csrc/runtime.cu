@@ -154,7 +154,7 @@ __global__ void __launch_bounds__(128, MIN_BLOCKS_128 > 0 ? MIN_BLOCKS_128 : 1) 
   Pair* warp_stk = t.stk - lane;  // lane j's deque starts at warp_stk + j
   WarpProf prof;
   const bool prof_on = __ldcg(&c->prof_on) != 0;
-  for (int i = 0; i < 8; i++) prof.v[i] = 0;
+  for (int i = 0; i < 16; i++) prof.v[i] = 0;
   long long t_loop = clock64();
   for (uint32_t round = 0; round < budget; round++) {
     // Intra-warp balancing: each empty lane takes the oldest redex of a lane
@@ -206,7 +206,7 @@ __global__ void __launch_bounds__(128, MIN_BLOCKS_128 > 0 ? MIN_BLOCKS_128 : 1) 
 
   if (prof_on && lane == 0) {
     prof.v[PROF_CYC_ROUND] = clock64() - t_loop;  // whole loop, including balancing and claims
-    for (int i = 0; i < 8; i++) if (prof.v[i]) atomicAdd(&c->prof[i], prof.v[i]);
+    for (int i = 0; i < 16; i++) if (prof.v[i]) atomicAdd(&c->prof[i], prof.v[i]);
   }
   release_caches(d, t);
   alloc_save(d.nspace, t.gid, t.na);
@@ -797,7 +797,7 @@ class Runtime {
     st->turns = h.turns;
     st->retries = h.retries;
     for (int i = 0; i < 8; i++) st->rule_hist[i] = h.hist[i];
-    for (int i = 0; i < 8; i++) st->prof[i] = h.prof[i];
+    for (int i = 0; i < 16; i++) st->prof[i] = h.prof[i];
     st->seconds = norm_seconds;
     st->threads = d.nthreads;
     st->grid = grid;
