@@ -75,7 +75,6 @@ typedef struct {
   uint32_t trace_cap;         /* record up to this many turns (0 = off), see hvm_gb300_trace */
   uint32_t reg_cap_blocks;    /* 0, or 8/12/16: cap registers so that many 128-thread blocks fit per SM */
   uint32_t profile;           /* 1 = collect per-warp round counters into hvm_gb300_stats.prof */
-  uint32_t cache_cap;         /* recycled node / var words kept per thread (0 = no recycling) */
 } hvm_gb300_config;
 
 typedef struct {
@@ -84,11 +83,14 @@ typedef struct {
   uint64_t turns;         /* evaluator turns run */
   uint64_t retries;       /* availability re-tries */
   uint64_t rule_hist[8];  /* interactions per rule: LINK CALL VOID ERAS ANNI COMM OPER SWIT */
-  uint64_t prof[16];      /* with profile=1: rounds, busy lanes, link steps, warp cycles in
-                             the turn loop, and in the load / write / fence / link phases;
-                             CALL lanes and their lane cycles in var alloc / node alloc / node
-                             writes; COMM/OPER/SWIT lanes and lane cycles; lane cycles freeing */
+  uint64_t prof[8];       /* with profile=1: rounds, busy lanes, link steps, warp cycles in
+                             the turn loop, and in the load / write / fence / link phases */
   double seconds;         /* wall time inside normalisation */
+  double kernel_ms;       /* device time of the turn kernels (CUDA events around each launch) */
+  uint64_t turn_launches; /* turn-kernel launches (including trailing no-op turns) */
+  uint64_t launches;      /* all kernel launches of this library */
+  uint64_t h2d_bytes;     /* bytes copied host -> device */
+  uint64_t d2h_bytes;     /* bytes copied device -> host */
   uint32_t threads, grid, block;
 } hvm_gb300_stats;
 
@@ -127,6 +129,10 @@ typedef struct {
 /* Copies up to `cap` turn records of the last run (needs trace_cap > 0);
  * `*n` receives how many exist. */
 int hvm_gb300_trace(hvm_gb300_runtime* rt, hvm_gb300_turn* out, size_t cap, size_t* n);
+
+/* Zeroes the measurement counters of hvm_gb300_stats (kernel_ms, launches,
+ * h2d/d2h bytes); they otherwise accumulate over the runtime's life. */
+void hvm_gb300_reset_counters(hvm_gb300_runtime* rt);
 
 /* Last error message of `rt` ("" if none). */
 const char* hvm_gb300_error(const hvm_gb300_runtime* rt);

@@ -43,7 +43,6 @@ class Config(ctypes.Structure):
         ("trace_cap", ctypes.c_uint32),
         ("reg_cap_blocks", ctypes.c_uint32),
         ("profile", ctypes.c_uint32),
-        ("cache_cap", ctypes.c_uint32),
     ]
 
 
@@ -66,8 +65,13 @@ class _Stats(ctypes.Structure):
         ("turns", ctypes.c_uint64),
         ("retries", ctypes.c_uint64),
         ("rule_hist", ctypes.c_uint64 * 8),
-        ("prof", ctypes.c_uint64 * 16),
+        ("prof", ctypes.c_uint64 * 8),
         ("seconds", ctypes.c_double),
+        ("kernel_ms", ctypes.c_double),
+        ("turn_launches", ctypes.c_uint64),
+        ("launches", ctypes.c_uint64),
+        ("h2d_bytes", ctypes.c_uint64),
+        ("d2h_bytes", ctypes.c_uint64),
         ("threads", ctypes.c_uint32),
         ("grid", ctypes.c_uint32),
         ("block", ctypes.c_uint32),
@@ -87,6 +91,7 @@ EXPORTED_SYMBOLS = (
     "hvm_gb300_run",
     "hvm_gb300_result",
     "hvm_gb300_trace",
+    "hvm_gb300_reset_counters",
     "hvm_gb300_error",
     "hvm_gb300_destroy",
 )
@@ -117,6 +122,8 @@ def lib() -> ctypes.CDLL:
                                    ctypes.POINTER(ctypes.c_size_t)]
     L.hvm_gb300_trace.argtypes = [ctypes.c_void_p, ctypes.POINTER(Turn), ctypes.c_size_t,
                                   ctypes.POINTER(ctypes.c_size_t)]
+    L.hvm_gb300_reset_counters.argtypes = [ctypes.c_void_p]
+    L.hvm_gb300_reset_counters.restype = None
     L.hvm_gb300_error.argtypes = [ctypes.c_void_p]
     L.hvm_gb300_error.restype = ctypes.c_char_p
     L.hvm_gb300_destroy.argtypes = [ctypes.c_void_p]
@@ -171,6 +178,11 @@ class RunStats:
     block: int
     rule_hist: dict = field(default_factory=dict)
     prof: tuple = ()
+    kernel_ms: float = 0.0
+    turn_launches: int = 0
+    launches: int = 0
+    h2d_bytes: int = 0
+    d2h_bytes: int = 0
 
     @property
     def mips(self) -> float:
@@ -216,7 +228,9 @@ class Runtime:
         return RunStats(itrs=st.itrs, leak=st.leak, turns=st.turns, retries=st.retries, seconds=st.seconds,
                         threads=st.threads, grid=st.grid, block=st.block,
                         rule_hist={RULE_NAMES[i]: int(st.rule_hist[i]) for i in range(8)},
-                        prof=tuple(int(x) for x in st.prof))
+                        prof=tuple(int(x) for x in st.prof), kernel_ms=st.kernel_ms,
+                        turn_launches=st.turn_launches, launches=st.launches,
+                        h2d_bytes=st.h2d_bytes, d2h_bytes=st.d2h_bytes)
 
     def result(self) -> str:
         n = ctypes.c_size_t()
@@ -224,6 +238,9 @@ class Runtime:
         out = ctypes.create_string_buffer(n.value + 1)
         self._check(lib().hvm_gb300_result(self._h, out, n.value + 1, ctypes.byref(n)))
         return out.value.decode()
+
+    def reset_counters(self) -> None:
+        lib().hvm_gb300_reset_counters(self._h)
 
     def trace(self) -> list[dict]:
         """Per-turn records of the last run (needs trace_cap > 0)."""

@@ -78,7 +78,7 @@ struct alignas(128) Ctl {
   unsigned int policy;              // 0 = fixed policy
   unsigned int pad_c[1];
   unsigned long long hist[8];       // interactions per rule (diagnostic)
-  unsigned long long prof[16];      // profile counters (when prof_on): see PROF_*
+  unsigned long long prof[8];       // profile counters (when prof_on): see PROF_*
   unsigned int prof_on;
   unsigned int npool_next;          // next page id of the node pool
   unsigned int vpool_next;          // next page id of the var pool
@@ -139,7 +139,7 @@ struct Alloc {
   uint32_t page;             // id of the page at `pos`
   uint32_t chunk;            // word index of the chunk `mask` describes
   uint32_t mask;             // free words of that chunk not yet handed out
-  uint32_t dry_chunks;       // chunks scanned since the last chunk with room
+  uint32_t dry_chunks;       // chunks scanned since the last free word
   bool pool_dry;             // the page pool ran out during this turn
 };
 
@@ -151,9 +151,6 @@ struct TState {
   uint32_t lo, len, cap;      // entries lo .. lo+len-1 (mod cap); cap is a power of two
   uint32_t gid;
   Alloc na, va;               // node / var allocators
-  uint32_t* ncache;           // recycled node words (shared memory, stride = blockDim.x)
-  uint32_t* vcache;           // recycled var words
-  uint32_t nfree, vfree, ccap;  // cached counts; capacity of each cache
   unsigned long long base;    // ring index of this turn's first input (overflow check)
   unsigned long long itrs, leak, retries;
   unsigned long long hist[8];
@@ -222,10 +219,7 @@ __device__ __forceinline__ void ld_cg_v4(const void* p, unsigned long long& a, u
 }
 
 constexpr uint32_t CHUNK = 32;  // words per scanned chunk (256 B of nodes, 128 B of vars)
-// A lane that met this many chunks in a row without room takes a fresh page
-// (while its page list has space); after MAX_DRY_CHUNKS it gives up.
-constexpr uint32_t DRY_CHUNKS_FOR_NEW_PAGE = 4;
-constexpr uint32_t MAX_DRY_CHUNKS = 4096;
+constexpr uint32_t MAX_DRY_PAGES = 4;  // full cycles over a lane's pages before out-of-memory
 
 // Bit i of the result is set when word base+i is free and may be handed out.
 template <bool VARS>
@@ -257,110 +251,70 @@ __device__ __forceinline__ uint32_t chunk_mask(const Dev& d, uint32_t base) {
   return m;
 }
 
-// Takes n (1..32) free words of one chunk -- the n lowest free positions, not
-// necessarily adjacent -- and returns the chunk's first word with `used` =
-// the bit set of the words taken (word j of the run is the j-th set bit).
-// Returns 0 when the page list is full and the pool is empty. Taken var words
-// are created (NONE) at once; callers write taken node words before their
-// next allocation, so no later scan can see them free while they are taken.
+// Bit i set iff bits i .. i+n-1 of m are all set (1 <= n <= 32).
+__device__ __forceinline__ uint32_t runs_of(uint32_t m, uint32_t n) {
+  uint32_t len = 1;
+  while (len * 2 <= n) { m &= m >> len; len <<= 1; }
+  if (len < n) m &= m >> (n - len);
+  return m;
+}
+
+// Takes n (1..32) consecutive free words of one chunk; returns the first, or
+// 0 when the page list is full and the pool is empty. Taken words are
+// written at once (vars as NONE, nodes as MARK) so no later scan can see them
+// free before their owner fills them.
 template <bool VARS>
-__device__ __forceinline__ uint32_t alloc_set(const Dev& d, TState& t, Alloc& a, uint32_t n, uint32_t& used) {
+__device__ __forceinline__ uint32_t alloc_run(const Dev& d, TState& t, Alloc& a, uint32_t n) {
   const PagedSpace& sp = VARS ? d.vspace : d.nspace;
   const uint32_t page_words = 1u << sp.page_log2;
+  const uint32_t chunks_per_page = page_words / CHUNK;
   for (uint32_t guard = 0; guard < (1u << 22); guard++) {
-    if ((uint32_t)__popc(a.mask) >= n) {
-      uint32_t m = a.mask, u = 0;
-      for (uint32_t i = 0; i < n; i++) { uint32_t lo = m & (0u - m); u |= lo; m ^= lo; }
-      a.mask = m;
-      used = u;
-      if (VARS) {
-        for (uint32_t w = u; w; w &= w - 1) vstore(d, a.chunk + (__ffs(w) - 1), NONE);
+    uint32_t r = runs_of(a.mask, n);
+    if (r) {
+      uint32_t b = __ffs(r) - 1;
+      a.mask &= ~((n == 32 ? ~0u : (1u << n) - 1) << b);
+      uint32_t at = a.chunk + b;
+      for (uint32_t i = 0; i < n; i++) {
+        if (VARS) vstore(d, at + i, NONE); else nstore(d, at + i, NODE_MARK);
       }
-      return a.chunk;
+      return at;
     }
-    // Next chunk: within the page, then the next owned page; after a few
-    // chunks with too few free words, a fresh page from the pool.
-    bool grabbed = false;
-    if (a.dry_chunks >= DRY_CHUNKS_FOR_NEW_PAGE && a.count < sp.max_pages && !a.pool_dry) {
-      uint32_t fresh = atomicAdd(pool_counter(d, VARS), 1u);
-      if (fresh < (VARS ? d.vpool_end : d.npool_end)) {
-        sp.lists[(size_t)t.gid * sp.max_pages + a.count] = fresh;
-        a.pos = a.count;
-        a.count++;
-        sp.counts[t.gid] = a.count;
-        a.page = fresh;
-        a.off = 0;
-        a.dry_chunks = 0;
-        grabbed = true;
-      } else {
-        a.pool_dry = true;  // pool exhausted: keep cycling through owned pages
-      }
-    }
-    if (!grabbed && a.off >= page_words) {
-      if (a.dry_chunks >= MAX_DRY_CHUNKS) return 0;  // every owned page is full
-      a.pos = a.pos + 1 == a.count ? 0 : a.pos + 1;
-      a.page = __ldcg(&sp.lists[(size_t)t.gid * sp.max_pages + a.pos]);
+    // Next chunk: within the page, then the next owned page, then a new page.
+    if (a.off >= page_words) {
       a.off = 0;
+      bool grabbed = false;
+      if ((a.dry_chunks >= 2 * chunks_per_page || (a.count == 1 && a.dry_chunks >= chunks_per_page)) &&
+          a.count < sp.max_pages && !a.pool_dry) {
+        uint32_t fresh = atomicAdd(pool_counter(d, VARS), 1u);
+        if (fresh < (VARS ? d.vpool_end : d.npool_end)) {
+          sp.lists[(size_t)t.gid * sp.max_pages + a.count] = fresh;
+          a.pos = a.count;
+          a.count++;
+          sp.counts[t.gid] = a.count;
+          a.page = fresh;
+          a.dry_chunks = 0;
+          grabbed = true;
+        } else {
+          a.pool_dry = true;  // pool exhausted: keep cycling through owned pages
+        }
+      }
+      if (!grabbed) {
+        // Every owned page scanned several times over without room: full.
+        if (a.dry_chunks >= MAX_DRY_PAGES * chunks_per_page * a.count) return 0;
+        a.pos = a.pos + 1 == a.count ? 0 : a.pos + 1;
+        a.page = __ldcg(&sp.lists[(size_t)t.gid * sp.max_pages + a.pos]);
+      }
     }
     a.chunk = (a.page << sp.page_log2) + a.off;
     a.off += CHUNK;
     a.mask = chunk_mask<VARS>(d, a.chunk);
-    a.dry_chunks = (uint32_t)__popc(a.mask) >= n ? 0 : a.dry_chunks + 1;
+    a.dry_chunks = runs_of(a.mask, n) ? 0 : a.dry_chunks + 1;
   }
   return 0;
 }
 
-__device__ __forceinline__ uint32_t alloc_one(const Dev& d, TState& t, Alloc& a, bool vars) {
-  uint32_t used = 0;
-  uint32_t base = vars ? alloc_set<true>(d, t, a, 1, used) : alloc_set<false>(d, t, a, 1, used);
-  return base ? base + (__ffs(used) - 1) : (used ? (__ffs(used) - 1) : 0);
-}
-
-__device__ __forceinline__ uint32_t alloc_node(const Dev& d, TState& t) { return alloc_one(d, t, t.na, false); }
-__device__ __forceinline__ uint32_t alloc_var(const Dev& d, TState& t) { return alloc_one(d, t, t.va, true); }
-
-// ---- recycling -----------------------------------------------------------------
-//
-// A node a lane takes (the principal nodes of its redex) and a var it
-// consumes (both ends linked) are unreachable from then on, so the lane may
-// reuse the word directly instead of zeroing it for the page owner's scan and
-// allocating another one. Each lane keeps up to `ccap` such words per space
-// in shared memory; when its cache is full, or at the end of the turn, it
-// releases words the reference's way, by writing 0 (src/hvm.c:688-694).
-
-__device__ __forceinline__ void free_node(const Dev& d, TState& t, uint32_t at) {
-  if (t.nfree < t.ccap) { t.ncache[(size_t)t.nfree * t.stride] = at; t.nfree++; }
-  else nstore(d, at, 0);
-}
-
-__device__ __forceinline__ void free_var(const Dev& d, TState& t, uint32_t at) {
-  if (t.vfree < t.ccap) { t.vcache[(size_t)t.vfree * t.stride] = at; t.vfree++; }
-  else vstore(d, at, 0);
-}
-
-// A node word for this lane: recycled if it has one, else from its pages.
-// The caller writes it before its next allocation.
-__device__ __forceinline__ uint32_t take_node(const Dev& d, TState& t) {
-  if (t.nfree) { t.nfree--; return t.ncache[(size_t)t.nfree * t.stride]; }
-  return alloc_node(d, t);
-}
-
-// A var word, created (NONE).
-__device__ __forceinline__ uint32_t take_var(const Dev& d, TState& t) {
-  if (t.vfree) {
-    t.vfree--;
-    uint32_t at = t.vcache[(size_t)t.vfree * t.stride];
-    vstore(d, at, NONE);
-    return at;
-  }
-  return alloc_var(d, t);
-}
-
-__device__ __forceinline__ void release_caches(const Dev& d, TState& t) {
-  for (uint32_t i = 0; i < t.nfree; i++) nstore(d, t.ncache[(size_t)i * t.stride], 0);
-  for (uint32_t i = 0; i < t.vfree; i++) vstore(d, t.vcache[(size_t)i * t.stride], 0);
-  t.nfree = t.vfree = 0;
-}
+__device__ __forceinline__ uint32_t alloc_node(const Dev& d, TState& t) { return alloc_run<false>(d, t, t.na, 1); }
+__device__ __forceinline__ uint32_t alloc_var(const Dev& d, TState& t) { return alloc_run<true>(d, t, t.va, 1); }
 
 // Loads a thread's allocator state at turn start; it resumes at the chunk it
 // was scanning when the previous turn ended.
@@ -404,10 +358,8 @@ __device__ __forceinline__ void alloc_save(const PagedSpace& sp, uint32_t gid, c
 enum : int { IR_DONE = 0, IR_RETRY = 1, IR_FATAL = 2 };
 
 // Profile counters (per warp, lane 0, summed into Ctl::prof when enabled).
-enum { PROF_ROUNDS, PROF_LANES, PROF_STEPS, PROF_CYC_ROUND, PROF_CYC_LOAD, PROF_CYC_WRITE, PROF_CYC_FENCE, PROF_CYC_LINK,
-       PROF_CALLS, PROF_CYC_CALL_VARS, PROF_CYC_CALL_NODES, PROF_CYC_CALL_WRITE, PROF_SMALL, PROF_CYC_SMALL,
-       PROF_CYC_FREE, PROF_SPARE };
-struct WarpProf { unsigned long long v[16]; };
+enum { PROF_ROUNDS, PROF_LANES, PROF_STEPS, PROF_CYC_ROUND, PROF_CYC_LOAD, PROF_CYC_WRITE, PROF_CYC_FENCE, PROF_CYC_LINK };
+struct WarpProf { unsigned long long v[8]; };
 
 // What one lane does this round.
 struct Plan {
@@ -417,41 +369,31 @@ struct Plan {
   uint32_t nlinks;      // port pairs to wire
   uint32_t n0, n1, n2, n3, v0, v1, v2, v3;  // fresh words of COMM/OPER/SWIT
   uint32_t node_len, rbag_len, vars_len, off;  // CALL: the def
-  // CALL: where the def's fresh words are. Mode CACHE: recycled words at
-  // cache slots base .. base+len-1; mode CHUNK: the words of chunk `base` at
-  // the set bits of `used` (j-th word = j-th set bit); mode TABLE: per-word
-  // scratch tables (defs larger than a chunk).
-  uint32_t nbase, vbase, nused, vused;
-  uint8_t nmode, vmode;
+  uint32_t nbase, vbase;  // CALL: first fresh node / var (contiguous runs), or
+  bool contig;            //       per-word scratch tables when the def is large
   Port root;            // CALL: the def's root
   Numb cv;              // OPER: the result when both sides are numbers
   bool oper_num;        // OPER: B1 is a number
   bool counted;         // counts as an interaction (every rule but LINK)
 };
 constexpr uint32_t IDLE_RULE = 8;
-enum : uint8_t { FROM_CACHE = 0, FROM_CHUNK = 1, FROM_TABLE = 2 };
 
 // Maps a def-local port to the fresh words of this CALL (adjust_port,
-// src/hvm.c:346-362).
-__device__ __forceinline__ uint32_t fresh_node(const Dev& d, const TState& t, const Plan& pl, uint32_t j) {
-  if (pl.nmode == FROM_CACHE) return t.ncache[(size_t)(pl.nbase + j) * t.stride];
-  if (pl.nmode == FROM_CHUNK) return pl.nbase + __fns(pl.nused, 0, j + 1);
-  return d.nloc[(size_t)j * d.nthreads + t.gid];
-}
-__device__ __forceinline__ uint32_t fresh_var(const Dev& d, const TState& t, const Plan& pl, uint32_t j) {
-  if (pl.vmode == FROM_CACHE) return t.vcache[(size_t)(pl.vbase + j) * t.stride];
-  if (pl.vmode == FROM_CHUNK) return pl.vbase + __fns(pl.vused, 0, j + 1);
-  return d.vloc[(size_t)j * d.nthreads + t.gid];
-}
-__device__ __forceinline__ Port relocate(const Dev& d, const TState& t, const Plan& pl, Port p) {
+// src/hvm.c:346-362): base + index for contiguous runs, else the scratch tables.
+__device__ __forceinline__ Port relocate(const Dev& d, uint32_t gid, const Plan& pl, Port p) {
   Tag tag = get_tag(p);
-  if (tag >= CON) return new_port(tag, fresh_node(d, t, pl, get_val(p)));
-  if (tag == VAR) return new_port(VAR, fresh_var(d, t, pl, get_val(p)));
+  if (pl.contig) {
+    if (tag >= CON) return new_port(tag, pl.nbase + get_val(p));
+    if (tag == VAR) return new_port(VAR, pl.vbase + get_val(p));
+    return p;
+  }
+  if (tag >= CON) return new_port(tag, d.nloc[(size_t)get_val(p) * d.nthreads + gid]);
+  if (tag == VAR) return new_port(VAR, d.vloc[(size_t)get_val(p) * d.nthreads + gid]);
   return p;
 }
 
 // The i-th port pair of the lane's rule (src/hvm.c:852-1070).
-__device__ __forceinline__ void link_pair(const Dev& d, const TState& t, const Plan& p, uint32_t i, Port& x, Port& y) {
+__device__ __forceinline__ void link_pair(const Dev& d, uint32_t gid, const Plan& p, uint32_t i, Port& x, Port& y) {
   switch (p.rule) {
     case LINK: x = p.a; y = p.b; break;
     case ERAS: x = p.a; y = i == 0 ? get_fst(p.B) : get_snd(p.B); break;
@@ -473,10 +415,10 @@ __device__ __forceinline__ void link_pair(const Dev& d, const TState& t, const P
     default: {  // CALL
       if (i < p.rbag_len) {
         Pair q = __ldg((const unsigned long long*)&d.book[p.off + i]);
-        x = relocate(d, t, p, get_fst(q));
-        y = relocate(d, t, p, get_snd(q));
+        x = relocate(d, gid, p, get_fst(q));
+        y = relocate(d, gid, p, get_snd(q));
       } else {
-        x = relocate(d, t, p, p.root);
+        x = relocate(d, gid, p, p.root);
         y = p.b;
       }
       break;
@@ -519,7 +461,7 @@ struct Slot {
 // pair that needs no exchange (both sides principal: a new redex).
 __device__ __forceinline__ void slot_fill(const Dev& d, TState& t, const Plan& p, uint32_t& next, Slot& s) {
   while (!s.busy && next < p.nlinks) {
-    link_pair(d, t, p, next++, s.X, s.Y);
+    link_pair(d, t.gid, p, next++, s.X, s.Y);
     if (get_tag(s.X) != VAR && get_tag(s.Y) == VAR) { Port z = s.X; s.X = s.Y; s.Y = z; }
     if (get_tag(s.X) != VAR) push(d, t, new_pair(s.X, s.Y));
     else { s.busy = true; s.entered = false; }
@@ -539,14 +481,14 @@ __device__ __forceinline__ void slot_result(const Dev& d, TState& t, Slot& s, ui
   const bool enter_step = !s.entered && get_tag(s.Y) == VAR;
   if (enter_step) {
     if (got == NONE || got == 0) s.entered = true;
-    else { free_var(d, t, addr); s.Y = got; }
+    else { vstore(d, addr, 0); s.Y = got; }
   } else if (got == NONE) {
     s.busy = false;  // the other side will find Y here
   } else if (got == 0) {
     set_status(d, ST_LINK_UNSET, addr); t.dead = true; s.busy = false;
   } else {
     // The other side had published `got` for X: take X and wire got ~ Y.
-    free_var(d, t, addr);
+    vstore(d, addr, 0);
     s.X = got;
     s.entered = false;
     if (get_tag(s.X) != VAR && get_tag(s.Y) == VAR) { Port z = s.X; s.X = s.Y; s.Y = z; }
@@ -575,30 +517,23 @@ __device__ __forceinline__ int lockstep_round(const Dev& d, TState& t, bool has,
   long long c1 = 0;
   if (wp) { __syncwarp(); c1 = clock64(); }
 
-  // 3. take the principal nodes (recycled), allocate, 4. write
+  // 3. allocate; 4. write
   bool made = false;
-  long long l0 = 0, l1 = 0, l2 = 0, l3 = 0, l4 = 0, lf = 0;
   if (rc == IR_DONE && rule != IDLE_RULE) {
-    if (wp) l0 = clock64();
-    if (needA) free_node(d, t, get_val(p.a));
-    if (needB) free_node(d, t, get_val(p.b));
-    if (wp) lf = clock64();
+    if (needA) nstore(d, get_val(p.a), 0);
+    if (needB) nstore(d, get_val(p.b), 0);
     switch (rule) {
       case LINK: p.nlinks = 1; break;
       case VOID: p.nlinks = 0; break;
       case ERAS: case ANNI: p.nlinks = 2; break;
       case COMM: {
-        p.v0 = take_var(d, t); p.v1 = take_var(d, t); p.v2 = take_var(d, t); p.v3 = take_var(d, t);
-        if (!(p.v0 && p.v1 && p.v2 && p.v3)) { rc = IR_FATAL; break; }
-        p.n0 = take_node(d, t);
-        if (p.n0) nstore(d, p.n0, new_pair(new_port(VAR, p.v0), new_port(VAR, p.v1)));
-        p.n1 = take_node(d, t);
-        if (p.n1) nstore(d, p.n1, new_pair(new_port(VAR, p.v2), new_port(VAR, p.v3)));
-        p.n2 = take_node(d, t);
-        if (p.n2) nstore(d, p.n2, new_pair(new_port(VAR, p.v0), new_port(VAR, p.v2)));
-        p.n3 = take_node(d, t);
-        if (p.n3) nstore(d, p.n3, new_pair(new_port(VAR, p.v1), new_port(VAR, p.v3)));
-        if (!(p.n0 && p.n1 && p.n2 && p.n3)) { rc = IR_FATAL; break; }
+        p.n0 = alloc_node(d, t); p.n1 = alloc_node(d, t); p.n2 = alloc_node(d, t); p.n3 = alloc_node(d, t);
+        p.v0 = alloc_var(d, t); p.v1 = alloc_var(d, t); p.v2 = alloc_var(d, t); p.v3 = alloc_var(d, t);
+        if (!(p.n0 && p.n1 && p.n2 && p.n3 && p.v0 && p.v1 && p.v2 && p.v3)) { rc = IR_FATAL; break; }
+        nstore(d, p.n0, new_pair(new_port(VAR, p.v0), new_port(VAR, p.v1)));
+        nstore(d, p.n1, new_pair(new_port(VAR, p.v2), new_port(VAR, p.v3)));
+        nstore(d, p.n2, new_pair(new_port(VAR, p.v0), new_port(VAR, p.v2)));
+        nstore(d, p.n3, new_pair(new_port(VAR, p.v1), new_port(VAR, p.v3)));
         made = true;
         p.nlinks = 4;
         break;
@@ -609,7 +544,7 @@ __device__ __forceinline__ int lockstep_round(const Dev& d, TState& t, bool has,
         if (p.oper_num) {
           p.cv = operate(get_val(p.a), get_val(b1));
         } else {
-          p.n0 = take_node(d, t);
+          p.n0 = alloc_node(d, t);
           if (!p.n0) { rc = IR_FATAL; break; }
           nstore(d, p.n0, new_pair(p.a, get_snd(p.B)));
           made = true;
@@ -619,39 +554,32 @@ __device__ __forceinline__ int lockstep_round(const Dev& d, TState& t, bool has,
       }
       case SWIT: {
         uint32_t n = get_u24(get_val(p.a));
+        p.n0 = alloc_node(d, t);
+        p.n1 = n == 0 ? 1u : alloc_node(d, t);
+        if (!p.n0 || !p.n1) { rc = IR_FATAL; break; }
         if (n == 0) {
-          p.n0 = take_node(d, t);
-          if (!p.n0) { rc = IR_FATAL; break; }
           nstore(d, p.n0, new_pair(get_snd(p.B), new_port(ERA, 0)));
         } else {
-          p.n1 = take_node(d, t);
-          if (!p.n1) { rc = IR_FATAL; break; }
-          nstore(d, p.n1, new_pair(new_port(NUM, new_u24(n - 1)), get_snd(p.B)));
-          p.n0 = take_node(d, t);
-          if (!p.n0) { rc = IR_FATAL; break; }
           nstore(d, p.n0, new_pair(new_port(ERA, 0), new_port(CON, p.n1)));
+          nstore(d, p.n1, new_pair(new_port(NUM, new_u24(n - 1)), get_snd(p.B)));
         }
         made = true;
         p.nlinks = 1;
         break;
       }
       default: {  // CALL (src/hvm.c:865-898)
-        // Vars: recycled when the cache holds enough, else one chunk's free
-        // words, else (large defs) per-word scratch tables.
-        if (p.vars_len <= t.vfree) {
-          // The slots stay counted in `vfree` until the end of the round: the
-          // link phase relocates through them while it recycles more vars on
-          // top (see the compaction after the link phase).
-          p.vmode = FROM_CACHE;
-          p.vbase = t.vfree - p.vars_len;
-          for (uint32_t i = 0; i < p.vars_len; i++) vstore(d, t.vcache[(size_t)(p.vbase + i) * t.stride], NONE);
-        } else if (p.vars_len <= CHUNK) {
-          p.vmode = FROM_CHUNK;
-          p.vused = 0;
-          p.vbase = alloc_set<true>(d, t, t.va, p.vars_len, p.vused);
-          if (!p.vused) { rc = IR_FATAL; break; }
+        p.contig = p.node_len <= CHUNK && p.vars_len <= CHUNK;
+        if (p.contig) {
+          // Vars first (taken as NONE), then the nodes, written in place.
+          p.vbase = p.vars_len ? alloc_run<true>(d, t, t.va, p.vars_len) : 0;
+          p.nbase = p.node_len ? alloc_run<false>(d, t, t.na, p.node_len) : 0;
+          if ((p.vars_len && !p.vbase) || (p.node_len && !p.nbase)) { rc = IR_FATAL; break; }
         } else {
-          p.vmode = FROM_TABLE;
+          for (uint32_t i = 0; i < p.node_len && rc == IR_DONE; i++) {
+            uint32_t at = alloc_node(d, t);
+            if (!at) rc = IR_FATAL;
+            d.nloc[(size_t)i * d.nthreads + t.gid] = at;
+          }
           for (uint32_t i = 0; i < p.vars_len && rc == IR_DONE; i++) {
             uint32_t at = alloc_var(d, t);
             if (!at) rc = IR_FATAL;
@@ -659,33 +587,12 @@ __device__ __forceinline__ int lockstep_round(const Dev& d, TState& t, bool has,
           }
           if (rc != IR_DONE) break;
         }
-        if (wp) l1 = clock64();
-        if (p.node_len <= t.nfree) {
-          p.nmode = FROM_CACHE;
-          t.nfree -= p.node_len;
-          p.nbase = t.nfree;
-        } else if (p.node_len <= CHUNK) {
-          p.nmode = FROM_CHUNK;
-          p.nused = 0;
-          p.nbase = alloc_set<false>(d, t, t.na, p.node_len, p.nused);
-          if (!p.nused) { rc = IR_FATAL; break; }
-        } else {
-          p.nmode = FROM_TABLE;
-          for (uint32_t i = 0; i < p.node_len && rc == IR_DONE; i++) {
-            uint32_t at = alloc_node(d, t);
-            if (!at) { rc = IR_FATAL; break; }
-            nstore(d, at, NODE_MARK);  // held until written below
-            d.nloc[(size_t)i * d.nthreads + t.gid] = at;
-          }
-          if (rc != IR_DONE) break;
-        }
-        if (wp) l2 = clock64();
         const Pair* nodes = d.book + p.off + p.rbag_len;
         for (uint32_t i = 0; i < p.node_len; i++) {
           Pair q = __ldg((const unsigned long long*)&nodes[i]);
-          nstore(d, fresh_node(d, t, p, i), new_pair(relocate(d, t, p, get_fst(q)), relocate(d, t, p, get_snd(q))));
+          uint32_t at = p.contig ? p.nbase + i : d.nloc[(size_t)i * d.nthreads + t.gid];
+          nstore(d, at, new_pair(relocate(d, t.gid, p, get_fst(q)), relocate(d, t.gid, p, get_snd(q))));
         }
-        if (wp) l3 = clock64();
         made = p.node_len > 0 || p.vars_len > 0;
         p.nlinks = p.rbag_len + 1;
         break;
@@ -695,25 +602,6 @@ __device__ __forceinline__ int lockstep_round(const Dev& d, TState& t, bool has,
       set_status(d, ST_OOM_NODES, t.gid);  // a node or var page list / pool ran out
       t.dead = true;
     }
-    if (wp) l4 = clock64();
-  }
-  if (wp) {
-    const bool is_call = rc == IR_DONE && rule == CALL;
-    const bool is_small = rc == IR_DONE && (rule == COMM || rule == OPER || rule == SWIT);
-    unsigned long long cv = is_call ? (unsigned long long)(l1 - lf) : 0;
-    unsigned long long cn = is_call ? (unsigned long long)(l2 - l1) : 0;
-    unsigned long long cw = is_call ? (unsigned long long)(l3 - l2) : 0;
-    unsigned long long cs = is_small ? (unsigned long long)(l4 - lf) : 0;
-    unsigned long long cf = (rc == IR_DONE && rule != IDLE_RULE) ? (unsigned long long)(lf - l0) : 0;
-    for (int o = 16; o > 0; o >>= 1) {
-      cv += __shfl_down_sync(0xFFFFFFFFu, cv, o); cn += __shfl_down_sync(0xFFFFFFFFu, cn, o);
-      cw += __shfl_down_sync(0xFFFFFFFFu, cw, o); cs += __shfl_down_sync(0xFFFFFFFFu, cs, o);
-      cf += __shfl_down_sync(0xFFFFFFFFu, cf, o);
-    }
-    wp->v[PROF_CALLS] += __popc(__ballot_sync(0xFFFFFFFFu, is_call));
-    wp->v[PROF_SMALL] += __popc(__ballot_sync(0xFFFFFFFFu, is_small));
-    wp->v[PROF_CYC_CALL_VARS] += cv; wp->v[PROF_CYC_CALL_NODES] += cn; wp->v[PROF_CYC_CALL_WRITE] += cw;
-    wp->v[PROF_CYC_SMALL] += cs; wp->v[PROF_CYC_FREE] += cf;
   }
 
   long long c2 = 0, c3 = 0;
@@ -744,15 +632,6 @@ __device__ __forceinline__ int lockstep_round(const Dev& d, TState& t, bool has,
     slot_result(d, t, s1, a1, g1);
   }
 
-  // Drop the var slots a CALL took from the cache; vars recycled during the
-  // link phase sit above them and move down.
-  if (rc == IR_DONE && rule == CALL && p.vmode == FROM_CACHE && p.vars_len) {
-    uint32_t top = p.vbase + p.vars_len;
-    for (uint32_t i = top; i < t.vfree; i++) {
-      t.vcache[(size_t)(i - p.vars_len) * t.stride] = t.vcache[(size_t)i * t.stride];
-    }
-    t.vfree -= p.vars_len;
-  }
   if (wp) {
     long long c4 = clock64();
     wp->v[PROF_ROUNDS] += 1;

@@ -102,7 +102,7 @@ __device__ void fixed_policy(Ctl* c, unsigned long long pending, unsigned long l
 // MIN_BLOCKS_128 > 0 asks the compiler to fit that many 128-thread blocks per
 // SM (a register cap); the runtime picks the variant from the configuration.
 template <int MIN_BLOCKS_128>
-__global__ void __launch_bounds__(128, MIN_BLOCKS_128 > 0 ? MIN_BLOCKS_128 : 1) turn_kernel(Dev d, uint32_t cap, uint32_t ccap) {
+__global__ void __launch_bounds__(128, MIN_BLOCKS_128 > 0 ? MIN_BLOCKS_128 : 1) turn_kernel(Dev d, uint32_t cap) {
   extern __shared__ unsigned long long smem_stack[];
   Ctl* c = d.ctl;
   // Turn parameters are read once per block so every thread of the block
@@ -127,10 +127,6 @@ __global__ void __launch_bounds__(128, MIN_BLOCKS_128 > 0 ? MIN_BLOCKS_128 : 1) 
   TState t;
   t.stk = (Pair*)smem_stack + threadIdx.x;
   t.stride = blockDim.x;
-  t.ccap = ccap;
-  t.ncache = (uint32_t*)((Pair*)smem_stack + (size_t)cap * blockDim.x) + threadIdx.x;
-  t.vcache = t.ncache + (size_t)ccap * blockDim.x;
-  t.nfree = t.vfree = 0;
   t.lo = 0;
   t.len = 0;
   t.cap = cap;
@@ -154,7 +150,7 @@ __global__ void __launch_bounds__(128, MIN_BLOCKS_128 > 0 ? MIN_BLOCKS_128 : 1) 
   Pair* warp_stk = t.stk - lane;  // lane j's deque starts at warp_stk + j
   WarpProf prof;
   const bool prof_on = __ldcg(&c->prof_on) != 0;
-  for (int i = 0; i < 16; i++) prof.v[i] = 0;
+  for (int i = 0; i < 8; i++) prof.v[i] = 0;
   long long t_loop = clock64();
   for (uint32_t round = 0; round < budget; round++) {
     // Intra-warp balancing: each empty lane takes the oldest redex of a lane
@@ -206,9 +202,8 @@ __global__ void __launch_bounds__(128, MIN_BLOCKS_128 > 0 ? MIN_BLOCKS_128 : 1) 
 
   if (prof_on && lane == 0) {
     prof.v[PROF_CYC_ROUND] = clock64() - t_loop;  // whole loop, including balancing and claims
-    for (int i = 0; i < 16; i++) if (prof.v[i]) atomicAdd(&c->prof[i], prof.v[i]);
+    for (int i = 0; i < 8; i++) if (prof.v[i]) atomicAdd(&c->prof[i], prof.v[i]);
   }
-  release_caches(d, t);
   alloc_save(d.nspace, t.gid, t.na);
   alloc_save(d.vspace, t.gid, t.va);
 
@@ -391,15 +386,24 @@ class Runtime {
   Port* g_out = nullptr; uint32_t* g_kids = nullptr; uint32_t* g_info = nullptr;
   uint32_t gather_cap = 0;
   uint32_t grid = 0, block = 0, cap = 0;
-  void (*turn_fn)(Dev, uint32_t, uint32_t) = nullptr;
-  uint32_t ccap = 0;
+  void (*turn_fn)(Dev, uint32_t) = nullptr;
   size_t smem = 0;
   uint32_t max_def_nodes = 1, max_def_vars = 1;
   int sms = 0;
   double norm_seconds = 0;
   uint64_t norm_calls = 0;
+  // Measurement: device time of turn kernels (events around each launch),
+  // launches of this library's kernels, and bytes copied each way.
+  std::vector<cudaEvent_t> events;
+  double kernel_ms = 0;
+  uint64_t turn_launches = 0, launches = 0, h2d_bytes = 0, d2h_bytes = 0;
 
-  ~Runtime() { release(); }
+  ~Runtime() {
+    for (cudaEvent_t e : events) cudaEventDestroy(e);
+    release();
+  }
+
+  void count_reset() { kernel_ms = 0; turn_launches = launches = h2d_bytes = d2h_bytes = 0; }
 
   int fail(const std::string& m) { if (err.empty()) err = m; return -1; }
 
@@ -421,9 +425,7 @@ class Runtime {
     if (cap < 2 || (cap & (cap - 1))) return fail("stack_cap must be a power of two >= 2");
     if (cfg.node_log2 < 10 || cfg.node_log2 > 29 || cfg.vars_log2 < 10 || cfg.vars_log2 > 29)
       return fail("node_log2/vars_log2 must be in [10, 29]");
-    ccap = cfg.cache_cap;
-    if (ccap > 256) return fail("cache_cap must be <= 256");
-    smem = (size_t)block * cap * sizeof(Pair) + 2ull * block * ccap * sizeof(uint32_t);
+    smem = (size_t)block * cap * sizeof(Pair);
     if (block > 128) return fail("threads_per_block must be <= 128");
     switch (cfg.reg_cap_blocks) {
       case 0: turn_fn = turn_kernel<0>; break;
@@ -499,6 +501,7 @@ class Runtime {
     // Thread g starts with page g of each space; the pools start after them.
     reset_alloc_kernel<<<(d.nthreads + 255) / 256, 256>>>(d);
     CK(cudaGetLastError());
+    launches++;
     norm_seconds = 0;
     norm_calls = 0;
     return 0;
@@ -582,6 +585,7 @@ class Runtime {
     CK(cudaMalloc(&mem_book, flat.size() * sizeof(Pair)));
     CK(cudaMemcpy(mem_defs, hdr.data(), hdr.size() * sizeof(DefHdr), cudaMemcpyHostToDevice));
     CK(cudaMemcpy(mem_book, flat.data(), flat.size() * sizeof(Pair), cudaMemcpyHostToDevice));
+    h2d_bytes += hdr.size() * sizeof(DefHdr) + flat.size() * sizeof(Pair);
     CK(cudaMalloc(&mem_scratch, (size_t)(max_def_nodes + max_def_vars) * d.nthreads * sizeof(uint32_t)));
     d.defs = (const DefHdr*)mem_defs;
     d.book = (const Pair*)mem_book;
@@ -593,12 +597,14 @@ class Runtime {
 
   int read_ctl(Ctl& h) {
     CK(cudaMemcpy(&h, ctl, sizeof(Ctl), cudaMemcpyDeviceToHost));
+    d2h_bytes += sizeof(Ctl);
     return 0;
   }
 
   int boot(Pair redex) {
     boot_kernel<<<1, 1>>>(d, redex, cap);
     CK(cudaGetLastError());
+    launches++;
     return 0;
   }
 
@@ -610,10 +616,26 @@ class Runtime {
     unsigned long long last_itrs = ~0ull, last_pending = ~0ull;
     Ctl h;
     for (;;) {
-      for (uint32_t i = 0; i < batch; i++) turn_fn<<<grid, block, smem>>>(d, cap, ccap);
+      while (events.size() < 2 * batch) {
+        cudaEvent_t e;
+        CK(cudaEventCreate(&e));
+        events.push_back(e);
+      }
+      for (uint32_t i = 0; i < batch; i++) {
+        CK(cudaEventRecord(events[2 * i]));
+        turn_fn<<<grid, block, smem>>>(d, cap);
+        CK(cudaEventRecord(events[2 * i + 1]));
+      }
       CK(cudaGetLastError());
       turns_run += batch;
+      turn_launches += batch;
+      launches += batch;
       if (read_ctl(h)) return -1;
+      for (uint32_t i = 0; i < batch; i++) {
+        float ms = 0;
+        CK(cudaEventElapsedTime(&ms, events[2 * i], events[2 * i + 1]));
+        kernel_ms += ms;
+      }
       if (h.status) return fail(std::string("device error: ") + status_text(h.status) + " (info " + std::to_string(h.err_info) + ")");
       if (h.base == h.in_end) break;
       if (cfg.max_turns && turns_run >= cfg.max_turns) return fail("turn budget exhausted before normal form");
@@ -634,9 +656,22 @@ class Runtime {
   }
 
   // Single-word device accessors for the host-side readback walk.
-  Port vars_load(uint32_t i) { Port v = 0; cudaMemcpy(&v, d.vars + (i & d.vars_mask), sizeof(Port), cudaMemcpyDeviceToHost); return v; }
-  void vars_store(uint32_t i, Port v) { cudaMemcpy(d.vars + (i & d.vars_mask), &v, sizeof(Port), cudaMemcpyHostToDevice); }
-  Pair node_load(uint32_t i) { Pair v = 0; cudaMemcpy(&v, d.node + i, sizeof(Pair), cudaMemcpyDeviceToHost); return v; }
+  Port vars_load(uint32_t i) {
+    Port v = 0;
+    cudaMemcpy(&v, d.vars + (i & d.vars_mask), sizeof(Port), cudaMemcpyDeviceToHost);
+    d2h_bytes += sizeof(Port);
+    return v;
+  }
+  void vars_store(uint32_t i, Port v) {
+    cudaMemcpy(d.vars + (i & d.vars_mask), &v, sizeof(Port), cudaMemcpyHostToDevice);
+    h2d_bytes += sizeof(Port);
+  }
+  Pair node_load(uint32_t i) {
+    Pair v = 0;
+    cudaMemcpy(&v, d.node + i, sizeof(Pair), cudaMemcpyDeviceToHost);
+    d2h_bytes += sizeof(Pair);
+    return v;
+  }
 
   // Read-only chase (src/hvm.c:781-790).
   Port peek(Port p) {
@@ -717,8 +752,10 @@ class Runtime {
     }
     gather_kernel<<<1, 1024>>>(d, ROOT, g_out, g_kids, gather_cap, g_info);
     CK(cudaGetLastError());
+    launches++;
     uint32_t info[2];
     CK(cudaMemcpy(info, g_info, sizeof(info), cudaMemcpyDeviceToHost));
+    d2h_bytes += sizeof(info) + 2ull * info[0] * sizeof(uint32_t);
     if (info[1]) return fail("result tree larger than the readback buffer");
     std::vector<Port> out(info[0]);
     std::vector<uint32_t> kids(info[0]);
@@ -797,8 +834,13 @@ class Runtime {
     st->turns = h.turns;
     st->retries = h.retries;
     for (int i = 0; i < 8; i++) st->rule_hist[i] = h.hist[i];
-    for (int i = 0; i < 16; i++) st->prof[i] = h.prof[i];
+    for (int i = 0; i < 8; i++) st->prof[i] = h.prof[i];
     st->seconds = norm_seconds;
+    st->kernel_ms = kernel_ms;
+    st->turn_launches = turn_launches;
+    st->launches = launches;
+    st->h2d_bytes = h2d_bytes;
+    st->d2h_bytes = d2h_bytes;
     st->threads = d.nthreads;
     st->grid = grid;
     st->block = block;
@@ -825,7 +867,6 @@ extern "C" void hvm_gb300_default_config(hvm_gb300_config* c) {
   c->max_turns = 0;
   c->stop_frac_q8 = 128;
   c->stack_cap = 8;
-  c->cache_cap = 16;
   c->reg_cap_blocks = 8;
   c->trace_cap = 0;
 }
@@ -843,6 +884,10 @@ extern "C" void hvm_gb300_destroy(hvm_gb300_runtime* r) { delete r; }
 
 extern "C" const char* hvm_gb300_error(const hvm_gb300_runtime* r) {
   return r ? r->rt.err.c_str() : "null runtime";
+}
+
+extern "C" void hvm_gb300_reset_counters(hvm_gb300_runtime* r) {
+  if (r) r->rt.count_reset();
 }
 
 extern "C" int hvm_gb300_load_book(hvm_gb300_runtime* r, const uint32_t* book, size_t words) {

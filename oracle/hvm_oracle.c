@@ -22,7 +22,8 @@
  * Parity is pinned by tests against the reference's own C runtime compiled
  * from its sources (oracle/_ref) and against the reference's snapshots.
  *
- * Usage: hvm_oracle [-t threads] <book.bin>
+ * Usage: hvm_oracle [-t threads] [-w] [-n] <book.bin>
+ *   -w  count algorithmic bytes (one worker)   -n  print the normalisation time in ns
  */
 #include <inttypes.h>
 #include <math.h>
@@ -243,10 +244,21 @@ typedef struct {
 
 static Net* g_net;
 static Worker** g_workers;
+
+/* Algorithmic bytes (-w, one worker): the fixed word-touch model of the
+ * reference's evaluator used as the roofline numerator -- node take 16 B
+ * (8 read + 8 write), node create 8 B, var create 4 B, var exchange 8 B
+ * (4 + 4), and 16 B per redex (push 8 + pop 8). Allocation scans,
+ * availability checks and the readback are not counted. */
+static int g_count_bytes;
+static int g_precise;  /* -n: also print the normalisation time in ns */
+static u64 g_bytes;
+#define COUNT(n) do { if (g_count_bytes) g_bytes += (n); } while (0)
 static u32 g_nthreads;
 static u64 g_node_slice, g_vars_slice;
 
 static inline void bag_push(Worker* w, Pair r) {
+  COUNT(16);
   if (shrinking(rule_of(fst_of(r), snd_of(r)))) {
     w->hstack[w->hlen++] = r;
   } else {
@@ -288,11 +300,11 @@ static u32 grab_vars(Worker* w, u32 want) {
 }
 
 static inline Pair node_get(u32 i) { return atomic_load_explicit(&g_net->node[i], memory_order_relaxed); }
-static inline void node_put(u32 i, Pair p) { atomic_store_explicit(&g_net->node[i], p, memory_order_relaxed); }
-static inline Pair node_swap(u32 i, Pair p) { return atomic_exchange_explicit(&g_net->node[i], p, memory_order_relaxed); }
+static inline void node_put(u32 i, Pair p) { COUNT(8); atomic_store_explicit(&g_net->node[i], p, memory_order_relaxed); }
+static inline Pair node_swap(u32 i, Pair p) { COUNT(16); return atomic_exchange_explicit(&g_net->node[i], p, memory_order_relaxed); }
 static inline Port var_get(u32 i) { return atomic_load_explicit(&g_net->vars[i], memory_order_relaxed); }
-static inline void var_put(u32 i, Port p) { atomic_store_explicit(&g_net->vars[i], p, memory_order_relaxed); }
-static inline Port var_swap(u32 i, Port p) { return atomic_exchange_explicit(&g_net->vars[i], p, memory_order_relaxed); }
+static inline void var_put(u32 i, Port p) { COUNT(4); atomic_store_explicit(&g_net->vars[i], p, memory_order_relaxed); }
+static inline Port var_swap(u32 i, Port p) { COUNT(8); return atomic_exchange_explicit(&g_net->vars[i], p, memory_order_relaxed); }
 
 /* Maps a def-local port to the freshly allocated slots (src/hvm.c:346-362). */
 static inline Port relocate(Worker* w, Port p) {
@@ -647,9 +659,12 @@ int main(int argc, char** argv) {
   const char* path = NULL;
   for (int i = 1; i < argc; i++) {
     if (!strcmp(argv[i], "-t") && i + 1 < argc) threads = (u32)atoi(argv[++i]);
+    else if (!strcmp(argv[i], "-w")) g_count_bytes = 1;
+    else if (!strcmp(argv[i], "-n")) g_precise = 1;
     else path = argv[i];
   }
-  if (!path || threads < 1 || threads > 256) { fprintf(stderr, "usage: hvm_oracle [-t threads] <book.bin>\n"); return 2; }
+  if (!path || threads < 1 || threads > 256) { fprintf(stderr, "usage: hvm_oracle [-t threads] [-w] [-n] <book.bin>\n"); return 2; }
+  if (g_count_bytes && threads != 1) { fprintf(stderr, "-w counts with one worker only\n"); return 2; }
   FILE* f = fopen(path, "rb");
   if (!f) { perror(path); return 2; }
   fseek(f, 0, SEEK_END);
@@ -681,6 +696,9 @@ int main(int argc, char** argv) {
   u64 t0 = now_ns();
   boot(mk_pair(mk_port(REF, 0), ROOT));
   run_loop();
+  u64 t_norm = now_ns();
+  int counted = g_count_bytes;
+  g_count_bytes = 0;
   printf("Result: ");
   print_tree(follow(ROOT));
   printf("\n");
@@ -689,5 +707,7 @@ int main(int argc, char** argv) {
   printf("- ITRS: %" PRIu64 "\n", itrs);
   printf("- TIME: %.2fs\n", secs);
   printf("- MIPS: %.2f\n", (double)itrs / secs / 1000000.0);
+  if (g_precise) printf("- NORM_NS: %" PRIu64 "\n", t_norm - t0);
+  if (counted) printf("- BYTES: %" PRIu64 "\n", g_bytes);
   return 0;
 }

@@ -13,7 +13,9 @@ reference sources exist; the fixtures travel, the reference does not).
   configs.json             the same two fields for the seeded benchmark
                            workloads (lambdavm-rust_gb300/workloads.py), with
                            large results stored as a SHA-256 of their
-                           canonical form.
+                           canonical form, plus the algorithmic bytes of the
+                           evaluation counted by the oracle (-w), the
+                           roofline numerator.
 
 Usage: python tests/golden/make_golden.py [--reference /root/reference]
 """
@@ -36,6 +38,20 @@ sys.path.insert(0, ROOT)
 H = importlib.import_module("lambdavm-rust_gb300")
 W = importlib.import_module("lambdavm-rust_gb300.workloads")
 REF_BIN = os.path.join(ROOT, "oracle", "_ref", "hvm_ref")
+PORT_BIN = os.path.join(ROOT, "oracle", "_build", "hvm_oracle")
+
+
+def algorithmic_bytes(code: str) -> int:
+    """Word-touch bytes of the whole evaluation, counted by the oracle (-w)."""
+    buf = H.book_from_text(code)
+    with tempfile.NamedTemporaryFile(suffix=".bin", delete=False) as f:
+        buf.tofile(f.name)
+        path = f.name
+    try:
+        r = subprocess.run([PORT_BIN, "-w", path], capture_output=True, text=True, timeout=3600, check=True)
+    finally:
+        os.unlink(path)
+    return int(re.search(r"^- BYTES: (\d+)$", r.stdout, re.M).group(1))
 
 
 def run_ref(code: str) -> dict:
@@ -70,6 +86,7 @@ def main() -> None:
     ap.add_argument("--skip-configs", action="store_true")
     args = ap.parse_args()
     subprocess.run(["make", "-C", os.path.join(ROOT, "oracle"), "ref", f"REF_SRC={args.reference}/src"], check=True)
+    subprocess.run(["make", "-C", os.path.join(ROOT, "oracle")], check=True)
 
     progs = []
     files = sorted(glob.glob(os.path.join(args.reference, "tests", "programs", "**", "*.hvm"), recursive=True)
@@ -107,7 +124,8 @@ def main() -> None:
     for name, code in cases.items():
         r = run_ref(code)
         canon = H.canonical(r["result"])
-        entry = {"itrs": r["itrs"], "canonical_sha256": hashlib.sha256(canon.encode()).hexdigest()}
+        entry = {"itrs": r["itrs"], "canonical_sha256": hashlib.sha256(canon.encode()).hexdigest(),
+                 "algorithmic_bytes": algorithmic_bytes(code)}
         if len(r["result"]) <= 4096:
             entry["result"] = r["result"]
         out[name] = entry
