@@ -1,0 +1,353 @@
+#!/usr/bin/env python3
+"""Benchmark of the GB300 HVM2 evaluator.
+
+One step = one full evaluation of the benchmark net: clear the net, boot
+`@main ~ ROOT`, normalise, and run the readback expansion. The default
+workload is the single-net bitonic sort of 2^16 PCG32 u24 keys (the sorted
+tree is the normal form). Every step's interaction count is checked against
+the golden count of the reference's C runtime, and the first step's normal
+form against its golden SHA-256.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--workload NAME]
+  python bench.py --impl reference ...   # the CPU evaluator on the host cores
+
+Prints one JSON line (rank 0). `value` is interactions/s with the book
+resident in HBM; `e2e` is the same metric through the C-ABI calls a user
+makes (book upload from pinned host memory, evaluation, result readback)
+with the copies inside the timed region. Under torchrun each rank runs its
+own replica (one net per GPU: the evaluator does not shard a single net).
+"""
+from __future__ import annotations
+
+import argparse
+import ctypes
+import hashlib
+import importlib
+import json
+import os
+import re
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "interactions/s on 1 GB300, learned+batched vs plain kernel, bit-exact normal form"
+UNIT = "interactions/s"
+GOLDEN = os.path.join(ROOT, "tests", "golden", "configs.json")
+PEAKS = os.path.join(ROOT, "MEASURED_PEAKS.json")
+TRAFFIC = os.path.join(ROOT, "profiles", "turn_kernel_bitonic_2p14.md")
+ORACLE = os.path.join(ROOT, "oracle", "_build", "hvm_oracle")
+
+WORKLOADS = {
+    # name: (golden key, generator, description)
+    "bitonic_sort_2p16": ("bitonic_sort_2p16", lambda W: W.bitonic_sort(16),
+                          "bitonic sort of 2^16 PCG32 u24 keys, single net, sorted tree as normal form"),
+    "tree_sum_d20": ("tree_sum_d20", lambda W: W.tree_sum(20), "recursive tree sum d=20, single net"),
+    "skewed_fold_2p18": ("skewed_fold_2p18", lambda W: W.skewed_fold(18),
+                         "fold over 2^18 geometric-length countdowns, single net"),
+}
+
+
+def dist_env():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+class Dist:
+    """torch.distributed around the replicas (barrier, max over ranks)."""
+
+    def __init__(self, ws: int, rank: int, local: int, use_cuda: bool):
+        self.ws, self.rank, self.local = ws, rank, local
+        self.torch = None
+        if ws > 1:
+            import torch
+            import torch.distributed as td
+            self.torch = torch
+            backend = "nccl" if use_cuda else "gloo"
+            if use_cuda:
+                torch.cuda.set_device(local)
+            td.init_process_group(backend=backend)
+            self.td = td
+            self.dev = torch.device("cuda", local) if use_cuda else torch.device("cpu")
+
+    def barrier(self):
+        if self.ws > 1:
+            self.td.barrier()
+
+    def max(self, x: float) -> float:
+        if self.ws == 1:
+            return x
+        t = self.torch.tensor([x], dtype=self.torch.float64, device=self.dev)
+        self.td.all_reduce(t, op=self.td.ReduceOp.MAX)
+        return float(t.item())
+
+    def sum(self, x: float) -> float:
+        if self.ws == 1:
+            return x
+        t = self.torch.tensor([x], dtype=self.torch.float64, device=self.dev)
+        self.td.all_reduce(t, op=self.td.ReduceOp.SUM)
+        return float(t.item())
+
+    def close(self):
+        if self.ws > 1:
+            self.td.destroy_process_group()
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device: int):
+        self.device = device
+        self.proc = None
+        self.path = None
+
+    def start(self):
+        try:
+            fd, self.path = tempfile.mkstemp(suffix=".csv")
+            os.close(fd)
+            self.out = open(self.path, "w")
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.FIELDS}",
+                                          "--format=csv,noheader,nounits", "-lms", "100"],
+                                         stdout=self.out, stderr=subprocess.DEVNULL)
+        except OSError:
+            self.proc = None
+
+    def stop(self) -> dict | None:
+        if not self.proc:
+            return None
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        self.out.close()
+        rows = [l.split(",") for l in open(self.path).read().splitlines() if l.strip()]
+        os.unlink(self.path)
+        sm, mx, reasons = [], 0.0, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for r in rows:
+            r = [x.strip() for x in r]
+            if len(r) < 9:
+                continue
+            try:
+                sm.append(float(r[1]))
+                mx = max(mx, float(r[2]))
+            except ValueError:
+                continue
+            for name, v in zip(names, r[5:9]):
+                if v.lower() == "active":
+                    reasons.add(name)
+        if not sm:
+            return None
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": mx, "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def read_traffic_per_itr() -> float | None:
+    try:
+        m = re.search(r"traffic_bytes_per_interaction:\s*([0-9.]+)", open(TRAFFIC).read())
+        return float(m.group(1)) if m else None
+    except OSError:
+        return None
+
+
+def run_oracle(book, threads: int) -> tuple[int, float, str]:
+    with tempfile.NamedTemporaryFile(suffix=".bin", delete=False) as f:
+        book.tofile(f.name)
+        path = f.name
+    try:
+        out = subprocess.run([ORACLE, "-t", str(threads), "-n", path], capture_output=True, text=True,
+                             check=True).stdout
+    finally:
+        os.unlink(path)
+    itrs = int(re.search(r"^- ITRS: (\d+)$", out, re.M).group(1))
+    ns = int(re.search(r"^- NORM_NS: (\d+)$", out, re.M).group(1))
+    res = re.search(r"^Result: (.*)$", out, re.M).group(1)
+    return itrs, ns / 1e9, res
+
+
+def ensure_built():
+    pkg = importlib.import_module("lambdavm-rust_gb300")
+    if not os.path.exists(pkg.LIB_PATH) or not os.path.exists(ORACLE):
+        importlib.import_module("__graft_entry__").build()
+    return pkg
+
+
+def bench_reference(args, book, golden, desc, ws, rank):
+    """The reference's CPU evaluator (its work-stealing pthreads algorithm,
+    restated in oracle/hvm_oracle.c) on all host cores, same workload."""
+    if rank != 0:
+        return None
+    threads = os.cpu_count() or 1
+    times = []
+    for i in range(args.warmup + args.steps):
+        itrs, secs, _ = run_oracle(book, threads)
+        if itrs != golden["itrs"]:
+            raise SystemExit(f"oracle interaction count {itrs} != golden {golden['itrs']}")
+        if i >= args.warmup:
+            times.append(secs)
+    value = golden["itrs"] / statistics.mean(times)
+    return {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": statistics.mean(times) * 1e3,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u32", "data": "synthetic",
+        "config": {"workload": desc, "itrs_per_step": golden["itrs"]},
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
+                         "sample": f"full workload ({golden['itrs']} interactions) per step, {threads} worker threads"},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+
+
+def bench_gpu(args, hvm, book, golden, desc, ws, rank, local, dist):
+    import torch
+    torch.cuda.set_device(local)
+    rt = hvm.Runtime(device=local)
+
+    # Warm-up, with a full parity check of the first step.
+    rt.load(book)
+    for i in range(args.warmup):
+        st = rt.run()
+        if st.itrs != golden["itrs"]:
+            raise SystemExit(f"interaction count {st.itrs} != golden {golden['itrs']}")
+        if i == 0:
+            canon = hvm.canonical(rt.result())
+            if hashlib.sha256(canon.encode()).hexdigest() != golden["canonical_sha256"]:
+                raise SystemExit("normal form differs from the golden")
+
+    # value: book resident in HBM; each step clears the 6 GB net (which also
+    # flushes L2), boots, normalises and expands.
+    rt.reset_counters()
+    sampler = ClockSampler(local)
+    sampler.start()
+    dist.barrier()
+    torch.cuda.synchronize()
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    ev0.record()
+    itrs_total = 0
+    for _ in range(args.steps):
+        st = rt.run()
+        itrs_total += st.itrs
+        if st.itrs != golden["itrs"]:
+            raise SystemExit(f"interaction count {st.itrs} != golden {golden['itrs']}")
+    ev1.record()
+    torch.cuda.synchronize()
+    dist.barrier()
+    clocks = sampler.stop()
+    secs = ev0.elapsed_time(ev1) / 1e3
+    counters = st  # the last step's stats carry the counters accumulated since reset_counters
+    kernel_s = counters.kernel_ms / 1e3
+    turns_effective = counters.turns * args.steps  # turns per evaluation x steps
+    launches = counters.launches
+
+    # e2e: the C-ABI calls a user makes, with the book copied from pinned host
+    # memory and the result read back to the host inside the timed region.
+    pinned = torch.from_numpy(book.view("int32")).pin_memory()
+    rt.reset_counters()
+    dist.barrier()
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for _ in range(args.steps):
+        L = hvm.lib()
+        rc = L.hvm_gb300_load_book(rt._h, ctypes.cast(pinned.data_ptr(), ctypes.POINTER(ctypes.c_uint32)),
+                                   book.size)
+        if rc:
+            raise SystemExit(L.hvm_gb300_error(rt._h).decode())
+        st_e = rt.run()
+        res = rt.result()
+        if st_e.itrs != golden["itrs"] or not res:
+            raise SystemExit("e2e step failed its check")
+    e1.record()
+    torch.cuda.synchronize()
+    dist.barrier()
+    e2e_secs = e0.elapsed_time(e1) / 1e3
+    h2d = st_e.h2d_bytes // args.steps
+    d2h = st_e.d2h_bytes // args.steps
+
+    secs_max = dist.max(secs)
+    e2e_max = dist.max(e2e_secs)
+    value = dist.sum(itrs_total) / secs_max
+    e2e_value = dist.sum(golden["itrs"] * args.steps) / e2e_max
+    rt.close()
+    if rank != 0:
+        return None
+
+    peaks = json.load(open(PEAKS)) if os.path.exists(PEAKS) else {}
+    peak = peaks.get("hbm_gbs")
+    peak_note = "measured" if peak else "fallback"
+    if not peak:
+        peak = 6800.0
+    bpi = golden["algorithmic_bytes"] / golden["itrs"]
+    achieved = bpi * itrs_total / kernel_s / 1e9 if kernel_s > 0 else None
+    tpi = read_traffic_per_itr()
+    itrs_per_launch = itrs_total / max(1, turns_effective)
+    roofline = {
+        "bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+        "frac": achieved / peak if achieved else None,
+        "traffic": tpi * itrs_per_launch if tpi else None,
+        "peak_source": peak_note,
+        "kernel": "turn_kernel",
+        "algorithmic_bytes_per_interaction": bpi,
+        "interactions_per_launch": itrs_per_launch,
+        "avg_launch_ms": counters.kernel_ms / max(1, turns_effective),
+    }
+    # CPU baseline: the oracle port on this host's cores, one full evaluation.
+    threads = os.cpu_count() or 1
+    c_itrs, c_secs, _ = run_oracle(book, threads)
+    cpu = {"value": c_itrs / c_secs, "unit": UNIT, "cores": threads, "kind": "port",
+           "sample": f"one full evaluation of the same workload ({c_itrs} interactions), {threads} worker threads"}
+    return {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": secs_max / args.steps * 1e3, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "u32", "data": "synthetic",
+        "config": {"workload": desc, "itrs_per_step": golden["itrs"], "policy": "fixed",
+                   "threads": counters.threads, "parallelism": f"replicas x{ws}",
+                   "l2": "each step clears the 6 GB node/var space (> L2) before evaluating",
+                   "parity": "interaction count checked every step; normal form SHA-256 checked"},
+        "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
+        "gpu_launches": launches,
+        "roofline": roofline,
+        "cpu_baseline": cpu,
+        "clocks": clocks,
+    }
+
+
+def main():
+    ap = argparse.ArgumentParser(description=__doc__, formatter_class=argparse.RawDescriptionHelpFormatter)
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["gb300", "reference"], default="gb300")
+    ap.add_argument("--workload", choices=sorted(WORKLOADS), default="bitonic_sort_2p16")
+    args = ap.parse_args()
+    ws, rank, local = dist_env()
+    hvm = ensure_built()
+    W = importlib.import_module("lambdavm-rust_gb300.workloads")
+    key, make, desc = WORKLOADS[args.workload]
+    golden = json.load(open(GOLDEN))[key]
+    book = hvm.book_from_text(make(W))
+    if args.impl == "reference":
+        line = bench_reference(args, book, golden, desc, ws, rank)
+        if line:
+            print(json.dumps(line), flush=True)
+        return
+    dist = Dist(ws, rank, local, use_cuda=True)
+    try:
+        line = bench_gpu(args, hvm, book, golden, desc, ws, rank, local, dist)
+    finally:
+        dist.close()
+    if line:
+        print(json.dumps(line), flush=True)
+
+
+if __name__ == "__main__":
+    main()
