@@ -134,6 +134,36 @@ int hvm_gb300_trace(hvm_gb300_runtime* rt, hvm_gb300_turn* out, size_t cap, size
  * h2d/d2h bytes); they otherwise accumulate over the runtime's life. */
 void hvm_gb300_reset_counters(hvm_gb300_runtime* rt);
 
+/* ---- Allocation-free evaluation ---------------------------------------------------
+ *
+ * No counterpart in the reference. For callers that may not allocate device
+ * memory -- code that runs while a CUDA graph is being captured elsewhere in
+ * the process, or whose device memory belongs to another allocator or pool --
+ * this evaluates a small net inside one fixed device array of about 20 MB
+ * that the library holds on every GPU that loads it, until the process exits.
+ * It calls no cudaMalloc, cudaFree or other allocating routine.
+ *
+ * Limits of the fixed array: book <= 2^19 u32 words, <= 4096 definitions,
+ * <= 2^18 node/redex pairs in total, <= 32 nodes and <= 32 vars per
+ * definition (the reference CUDA loader's own limit is 64); net <= 2^20 node
+ * words and 2^20 var words, at most 8,192 words of each kind per thread of
+ * the fixed 2,048-thread grid; normal form <= 2^16 entries. A book beyond
+ * the book limits is rejected with a message in `err`; a net that outgrows
+ * the memory limits fails with "out of node memory".
+ *
+ * Same evaluation as hvm_gb300_run on the current device: boot @main, normalise,
+ * readback expansion. The normal form is returned breadth-first: out_ports[k]
+ * is a port with its var chain resolved; for a node port (CON, DUP, OPR, SWI)
+ * its two children are entries out_kids[k] and out_kids[k] + 1 (out_kids is
+ * meaningless for other ports). `*out_len` receives the entry count and
+ * `*out_itrs` the interaction count. Returns 0, or -1 with `err` set.
+ *
+ * Every call shares the array: calls that overlap on the GPU race. Each call
+ * clears what must start at zero. The first call on a device resolves the
+ * array's address with that device current; make it before any stream capture. */
+int hvm_gb300_run_noalloc(const uint32_t* book_buffer, size_t words, uint32_t* out_ports, uint32_t* out_kids,
+                          size_t out_cap, size_t* out_len, uint64_t* out_itrs, char* err, size_t err_cap);
+
 /* Last error message of `rt` ("" if none). */
 const char* hvm_gb300_error(const hvm_gb300_runtime* rt);
 

@@ -92,6 +92,7 @@ EXPORTED_SYMBOLS = (
     "hvm_gb300_result",
     "hvm_gb300_trace",
     "hvm_gb300_reset_counters",
+    "hvm_gb300_run_noalloc",
     "hvm_gb300_error",
     "hvm_gb300_destroy",
 )
@@ -122,6 +123,9 @@ def lib() -> ctypes.CDLL:
                                    ctypes.POINTER(ctypes.c_size_t)]
     L.hvm_gb300_trace.argtypes = [ctypes.c_void_p, ctypes.POINTER(Turn), ctypes.c_size_t,
                                   ctypes.POINTER(ctypes.c_size_t)]
+    L.hvm_gb300_run_noalloc.argtypes = [u32p, ctypes.c_size_t, u32p, u32p, ctypes.c_size_t,
+                                        ctypes.POINTER(ctypes.c_size_t), ctypes.POINTER(ctypes.c_uint64),
+                                        ctypes.c_char_p, ctypes.c_size_t]
     L.hvm_gb300_reset_counters.argtypes = [ctypes.c_void_p]
     L.hvm_gb300_reset_counters.restype = None
     L.hvm_gb300_error.argtypes = [ctypes.c_void_p]

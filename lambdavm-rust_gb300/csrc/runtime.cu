@@ -978,3 +978,314 @@ extern "C" void hvm_cu(const uint32_t* book_buffer) {
   fflush(stdout);
   hvm_gb300_destroy(r);
 }
+
+// ---- Allocation-free evaluation ------------------------------------------------------
+//
+// hvm_gb300_run_noalloc evaluates a small net without allocating any memory:
+// the whole net (node and var spaces, redex ring, page lists, control block,
+// book tables and the readback buffers) lives in one fixed device array of
+// NOALLOC_ARENA_BYTES. It serves callers that may not call cudaMalloc — code
+// running while a CUDA graph is being captured elsewhere in the process, a
+// host whose device memory is owned by another allocator or a pool that must
+// not fragment, or an embedding that has to guarantee the call cannot fail on
+// allocation. The array is held by every GPU that loads the library until the
+// process exits. All calls share it, so calls that overlap on the GPU race
+// with each other; each call clears what must start at zero before it runs.
+// The first call on a device resolves the array's device address
+// (cudaGetSymbolAddress) with that device current; make that first call
+// before any stream capture.
+
+namespace hvm {
+namespace noalloc {
+
+// Fixed capacities of the arena. The grid is fixed (16 blocks of 128 threads,
+// enough for small nets) so the page layout is fixed: 256-word pages, up to
+// 32 pages of each kind per thread.
+constexpr uint32_t BLOCKS = 16, THREADS = 128, NTHREADS = BLOCKS * THREADS, CAP = 8;
+constexpr uint32_t NODE_LOG2 = 20, VARS_LOG2 = 20, RING_LOG2 = 18, PAGE_LOG2 = 8, LIST_PAGES = 32;
+constexpr uint32_t MAX_BOOK_WORDS = 1u << 19, MAX_DEFS = 4096, MAX_PAIRS = 1u << 18;
+constexpr uint32_t MAX_DEF_NODES = 32, MAX_DEF_VARS = 32, MAX_TREE = 1u << 16;
+
+constexpr size_t align256(size_t x) { return (x + 255) & ~(size_t)255; }
+constexpr size_t OFF_NODE = 0;
+constexpr size_t OFF_VARS = OFF_NODE + align256(sizeof(Pair) << NODE_LOG2);
+constexpr size_t OFF_RING = OFF_VARS + align256(sizeof(Port) << VARS_LOG2);
+constexpr size_t OFF_LISTS = OFF_RING + align256(sizeof(Pair) << RING_LOG2);
+constexpr size_t LISTS_WORDS = 2ull * NTHREADS * (LIST_PAGES + 3);
+constexpr size_t OFF_RAW = OFF_LISTS + align256(LISTS_WORDS * sizeof(uint32_t));
+constexpr size_t OFF_DEFS = OFF_RAW + align256((size_t)MAX_BOOK_WORDS * sizeof(uint32_t));
+constexpr size_t OFF_RAWPOS = OFF_DEFS + align256((size_t)MAX_DEFS * sizeof(DefHdr));
+constexpr size_t OFF_BOOK = OFF_RAWPOS + align256((size_t)MAX_DEFS * sizeof(uint32_t));
+constexpr size_t OFF_OUT = OFF_BOOK + align256((size_t)MAX_PAIRS * sizeof(Pair));
+constexpr size_t OFF_KIDS = OFF_OUT + align256((size_t)MAX_TREE * sizeof(Port));
+constexpr size_t OFF_INFO = OFF_KIDS + align256((size_t)MAX_TREE * sizeof(uint32_t));
+constexpr size_t OFF_CTL = OFF_INFO + 256;
+constexpr size_t ARENA_BYTES = OFF_CTL + align256(sizeof(Ctl));
+
+}  // namespace noalloc
+}  // namespace hvm
+
+// The arena. In host code this name is a host-side stand-in, not a device
+// address: only the address from cudaGetSymbolAddress may be given to kernels.
+static __device__ __align__(256) unsigned char g_noalloc_arena[hvm::noalloc::ARENA_BYTES];
+
+namespace hvm {
+namespace noalloc {
+
+constexpr int MAX_DEVICES = 64;
+static unsigned char* g_arena_dev[MAX_DEVICES];  // device address of the arena, per device
+
+// Builds the device book tables from the raw buffer already in the arena:
+// thread 0 lays out the def headers (the host has validated the buffer),
+// then all threads copy each def's pairs to an 8-byte aligned table.
+__global__ void book_kernel(const uint32_t* raw, DefHdr* defs, uint32_t* rawpos, Pair* book) {
+  if (threadIdx.x == 0) {
+    uint32_t ndefs = raw[0], at = 1, off = 0;
+    for (uint32_t k = 0; k < ndefs; k++) {
+      uint32_t fid = raw[at];
+      uint32_t safe = raw[at + 65], rl = raw[at + 66], nl = raw[at + 67], vl = raw[at + 68];
+      defs[fid] = DefHdr{nl, rl, vl, safe ? 1u : 0u, raw[at + 69], off, 0, 0};
+      rawpos[fid] = at + DEF_HEADER_WORDS;
+      off += rl + nl;
+      at += DEF_HEADER_WORDS + 2 * (rl + nl);
+    }
+  }
+  __syncthreads();
+  uint32_t ndefs = raw[0];
+  for (uint32_t f = 0; f < ndefs; f++) {
+    const DefHdr h = defs[f];
+    const uint32_t* src = raw + rawpos[f];
+    for (uint32_t i = threadIdx.x; i < h.rbag_len + h.node_len; i += blockDim.x) {
+      book[h.off + i] = new_pair(src[2 * i], src[2 * i + 1]);
+    }
+  }
+}
+
+struct Ctx {
+  Dev d;
+  unsigned char* arena;
+  char* err;
+  size_t err_cap;
+};
+
+static int failf(Ctx& x, const char* msg, long long a = -1) {
+  if (x.err && x.err_cap) {
+    if (a >= 0) snprintf(x.err, x.err_cap, "%s (%lld)", msg, a);
+    else snprintf(x.err, x.err_cap, "%s", msg);
+  }
+  return -1;
+}
+
+static int cuda_ok(Ctx& x, cudaError_t e) {
+  if (e == cudaSuccess) return 0;
+  return failf(x, cudaGetErrorString(e));
+}
+
+static int read_ctl(Ctx& x, Ctl& h) { return cuda_ok(x, cudaMemcpy(&h, x.d.ctl, sizeof(Ctl), cudaMemcpyDeviceToHost)); }
+
+static int normalize(Ctx& x) {
+  Ctl h;
+  uint32_t batch = 4;
+  unsigned long long last_itrs = ~0ull, last_pending = ~0ull;
+  uint64_t stalled = 0, turns = 0;
+  for (;;) {
+    for (uint32_t i = 0; i < batch; i++) turn_kernel<8><<<BLOCKS, THREADS, (size_t)THREADS * CAP * sizeof(Pair)>>>(x.d, CAP);
+    if (cuda_ok(x, cudaGetLastError()) || read_ctl(x, h)) return -1;
+    turns += batch;
+    if (h.status) return failf(x, status_text(h.status), h.err_info);
+    if (h.base == h.in_end) return 0;
+    if (h.itrs == last_itrs && h.pending == last_pending) {
+      if (++stalled > 4096) return failf(x, "no progress: interaction count stalled with redexes pending");
+    } else {
+      stalled = 0;
+    }
+    if (turns > (1ull << 24)) return failf(x, "turn budget exhausted before normal form");
+    last_itrs = h.itrs;
+    last_pending = h.pending;
+    if (batch < 64) batch *= 2;
+  }
+}
+
+static int boot(Ctx& x, Pair redex) {
+  boot_kernel<<<1, 1>>>(x.d, redex, CAP);
+  return cuda_ok(x, cudaGetLastError());
+}
+
+static int vars_load(Ctx& x, uint32_t i, Port& v) {
+  return cuda_ok(x, cudaMemcpy(&v, x.d.vars + (i & x.d.vars_mask), sizeof(Port), cudaMemcpyDeviceToHost));
+}
+static int vars_store(Ctx& x, uint32_t i, Port v) {
+  return cuda_ok(x, cudaMemcpy(x.d.vars + (i & x.d.vars_mask), &v, sizeof(Port), cudaMemcpyHostToDevice));
+}
+static int node_load(Ctx& x, uint32_t i, Pair& v) {
+  return cuda_ok(x, cudaMemcpy(&v, x.d.node + i, sizeof(Pair), cudaMemcpyDeviceToHost));
+}
+
+// Read-only chase (src/hvm.c:781-790).
+static int peek(Ctx& x, Port p, Port& out) {
+  while (get_tag(p) == VAR) {
+    Port v;
+    if (vars_load(x, get_val(p), v)) return -1;
+    if (v == NONE || v == 0) break;
+    p = v;
+  }
+  out = p;
+  return 0;
+}
+
+// Normalises every REF the readback meets (src/hvm.c:1233-1243).
+static int expand(Ctx& x, Port p, Port& out) {
+  Port saved, got;
+  if (vars_load(x, ROOT_VAR, saved) || peek(x, p, got)) return -1;
+  while (get_tag(got) == REF) {
+    Port r;
+    if (boot(x, new_pair(got, ROOT)) || normalize(x) || vars_load(x, ROOT_VAR, r) || peek(x, r, got)) return -1;
+  }
+  if (vars_store(x, ROOT_VAR, saved)) return -1;
+  out = got;
+  return 0;
+}
+
+// The IO loop's constructor walk without IO builtins (src/run.c:65-97, 740-810).
+static int readback_walk(Ctx& x) {
+  Port root, lam, app, arg;
+  Pair n;
+  if (peek(x, ROOT, root) || expand(x, root, lam)) return -1;
+  if (get_tag(lam) != CON) return 0;
+  if (node_load(x, get_val(lam), n) || expand(x, get_fst(n), app)) return -1;
+  if (get_tag(app) != CON) return 0;
+  Pair app_n;
+  if (node_load(x, get_val(app), app_n) || expand(x, get_fst(app_n), arg)) return -1;
+  if (get_tag(arg) != NUM) return 0;
+  for (;;) {
+    if (expand(x, get_snd(app_n), app)) return -1;
+    if (get_tag(app) != CON) break;
+    if (node_load(x, get_val(app), app_n) || expand(x, get_fst(app_n), arg)) return -1;
+  }
+  return 0;
+}
+
+// Checks the caller's book in place against the arena's limits and the
+// reference loader's limits (src/hvm.c:1408-1453); ports must stay inside
+// their definition.
+static int validate(Ctx& x, const uint32_t* w, size_t words) {
+  if (!w || words < 1) return failf(x, "empty book buffer");
+  if (words > MAX_BOOK_WORDS) return failf(x, "book larger than the fixed arena allows (words)", (long long)words);
+  uint32_t ndefs = w[0];
+  if (ndefs == 0 || ndefs > MAX_DEFS) return failf(x, "book has more definitions than the fixed arena allows", ndefs);
+  size_t at = 1, pairs = 0;
+  uint32_t seen[MAX_DEFS / 32] = {0};  // every fid exactly once
+  for (uint32_t k = 0; k < ndefs; k++) {
+    if (at + DEF_HEADER_WORDS > words) return failf(x, "failed to load book: truncated");
+    uint32_t fid = w[at], rl = w[at + 66], nl = w[at + 67], vl = w[at + 68];
+    if (fid >= ndefs) return failf(x, "failed to load book: bad definition id", fid);
+    if (seen[fid / 32] & (1u << (fid % 32))) return failf(x, "failed to load book: duplicate definition id", fid);
+    seen[fid / 32] |= 1u << (fid % 32);
+    if (rl > DEF_RBAG_LEN) return failf(x, "definition has too many redexes", rl);
+    if (nl > MAX_DEF_NODES) return failf(x, "definition has more nodes than the fixed arena allows", nl);
+    if (vl > MAX_DEF_VARS) return failf(x, "definition has more vars than the fixed arena allows", vl);
+    size_t end = at + DEF_HEADER_WORDS + 2ull * (rl + nl);
+    if (end > words) return failf(x, "failed to load book: truncated");
+    auto ok = [&](Port p) {
+      Tag t = get_tag(p);
+      if (t >= CON) return get_val(p) < nl;
+      if (t == VAR) return get_val(p) < vl;
+      if (t == REF) return (get_val(p) & 0xFFFFFFFu) < ndefs;
+      return true;
+    };
+    bool good = ok(w[at + 69]);
+    for (size_t i = at + DEF_HEADER_WORDS; i < end; i++) good = good && ok(w[i]);
+    if (!good) return failf(x, "failed to load book: a port points outside its definition", fid);
+    pairs += rl + nl;
+    at = end;
+  }
+  if (pairs > MAX_PAIRS) return failf(x, "book has more pairs than the fixed arena allows", (long long)pairs);
+  return 0;
+}
+
+}  // namespace noalloc
+}  // namespace hvm
+
+extern "C" int hvm_gb300_run_noalloc(const uint32_t* book, size_t words, uint32_t* out_ports, uint32_t* out_kids,
+                                     size_t out_cap, size_t* out_len, uint64_t* out_itrs, char* err, size_t err_cap) {
+  using namespace hvm;
+  using namespace hvm::noalloc;
+  Ctx x{};
+  x.err = err;
+  x.err_cap = err_cap;
+  if (err && err_cap) err[0] = 0;
+  int dev = 0;
+  if (cuda_ok(x, cudaGetDevice(&dev))) return -1;
+  if (dev < 0 || dev >= MAX_DEVICES) return failf(x, "device ordinal out of range", dev);
+  if (!g_arena_dev[dev]) {
+    void* p = nullptr;
+    if (cuda_ok(x, cudaGetSymbolAddress(&p, g_noalloc_arena))) return -1;
+    g_arena_dev[dev] = (unsigned char*)p;
+  }
+  unsigned char* A = g_arena_dev[dev];
+  x.arena = A;
+  if (validate(x, book, words)) return -1;
+
+  // Device view of the arena.
+  Dev& d = x.d;
+  d.node = (Pair*)(A + OFF_NODE);
+  d.vars = (Port*)(A + OFF_VARS);
+  d.vars_mask = (1u << VARS_LOG2) - 1;
+  d.node_mask = (1u << NODE_LOG2) - 1;
+  d.ring = (Pair*)(A + OFF_RING);
+  d.ring_mask = (1ull << RING_LOG2) - 1;
+  uint32_t* lw = (uint32_t*)(A + OFF_LISTS);
+  for (PagedSpace* sp : {&d.nspace, &d.vspace}) {
+    sp->page_log2 = PAGE_LOG2;
+    sp->max_pages = LIST_PAGES;
+    sp->lists = lw; lw += (size_t)NTHREADS * LIST_PAGES;
+    sp->counts = lw; lw += NTHREADS;
+    sp->pos = lw; lw += NTHREADS;
+    sp->off = lw; lw += NTHREADS;
+  }
+  d.npool_end = 1u << (NODE_LOG2 - PAGE_LOG2);
+  d.vpool_end = 1u << (VARS_LOG2 - PAGE_LOG2);
+  d.nloc = nullptr;  // every def fits one chunk: the scratch tables are never used
+  d.vloc = nullptr;
+  d.nthreads = NTHREADS;
+  d.ndefs = book[0];
+  d.defs = (const DefHdr*)(A + OFF_DEFS);
+  d.book = (const Pair*)(A + OFF_BOOK);
+  d.ctl = (Ctl*)(A + OFF_CTL);
+
+  // Book: raw words in, then the device tables.
+  if (cuda_ok(x, cudaMemcpy(A + OFF_RAW, book, words * sizeof(uint32_t), cudaMemcpyHostToDevice))) return -1;
+  book_kernel<<<1, 256>>>((const uint32_t*)(A + OFF_RAW), (DefHdr*)(A + OFF_DEFS), (uint32_t*)(A + OFF_RAWPOS),
+                          (Pair*)(A + OFF_BOOK));
+  if (cuda_ok(x, cudaGetLastError())) return -1;
+
+  // Clear what must start at zero: the net, the control block.
+  if (cuda_ok(x, cudaMemset(A + OFF_NODE, 0, sizeof(Pair) << NODE_LOG2)) ||
+      cuda_ok(x, cudaMemset(A + OFF_VARS, 0, sizeof(Port) << VARS_LOG2)) ||
+      cuda_ok(x, cudaMemset(A + OFF_CTL, 0, sizeof(Ctl)))) return -1;
+  uint32_t frac = 128;
+  if (cuda_ok(x, cudaMemcpy(&d.ctl->stop_frac_q8, &frac, sizeof(frac), cudaMemcpyHostToDevice))) return -1;
+  reset_alloc_kernel<<<(NTHREADS + 255) / 256, 256>>>(d);
+  if (cuda_ok(x, cudaGetLastError())) return -1;
+
+  // Boot @main ~ ROOT, normalise, run the readback expansion.
+  if (boot(x, new_pair(new_port(REF, 0), ROOT)) || normalize(x) || readback_walk(x)) return -1;
+
+  // Serialise the normal form into the caller's arrays.
+  uint32_t* info = (uint32_t*)(A + OFF_INFO);
+  gather_kernel<<<1, 1024>>>(d, ROOT, (Port*)(A + OFF_OUT), (uint32_t*)(A + OFF_KIDS), MAX_TREE, info);
+  if (cuda_ok(x, cudaGetLastError())) return -1;
+  uint32_t hinfo[2];
+  if (cuda_ok(x, cudaMemcpy(hinfo, info, sizeof(hinfo), cudaMemcpyDeviceToHost))) return -1;
+  if (hinfo[1]) return failf(x, "normal form larger than the fixed arena's readback buffer", MAX_TREE);
+  if (out_len) *out_len = hinfo[0];
+  if (hinfo[0] > out_cap) return failf(x, "output arrays too small for the normal form", hinfo[0]);
+  if (out_ports && cuda_ok(x, cudaMemcpy(out_ports, A + OFF_OUT, hinfo[0] * sizeof(Port), cudaMemcpyDeviceToHost)))
+    return -1;
+  if (out_kids && cuda_ok(x, cudaMemcpy(out_kids, A + OFF_KIDS, hinfo[0] * sizeof(uint32_t), cudaMemcpyDeviceToHost)))
+    return -1;
+  Ctl h;
+  if (read_ctl(x, h)) return -1;
+  if (out_itrs) *out_itrs = h.itrs;
+  return 0;
+}
