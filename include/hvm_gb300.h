@@ -113,6 +113,24 @@ int hvm_gb300_run(hvm_gb300_runtime* rt, hvm_gb300_stats* stats);
  * "Result: " prefix). `out == NULL` queries the length (excluding the NUL). */
 int hvm_gb300_result(hvm_gb300_runtime* rt, char* out, size_t cap, size_t* len);
 
+/* ---- Batches ------------------------------------------------------------------
+ *
+ * No single counterpart in the reference, which evaluates one net per call
+ * (src/hvm.cu:2320): many independent nets are evaluated together by the same
+ * launches. Net k keeps its own ROOT var; the total interaction count is the
+ * sum of the nets' counts under the reference.
+ *
+ * hvm_gb300_load_batch: `books[k]` is net k's book buffer (`words[k]` its
+ * length, or words == NULL). hvm_gb300_run_batch: boots every net's @main,
+ * normalises all of them, runs each net's readback expansion.
+ * hvm_gb300_batch_roots: each net's normal-form root port with var chains
+ * resolved (a number for numeric results). hvm_gb300_batch_result: one net's
+ * normal form as text, like hvm_gb300_result. */
+int hvm_gb300_load_batch(hvm_gb300_runtime* rt, const uint32_t* const* books, const size_t* words, uint32_t n);
+int hvm_gb300_run_batch(hvm_gb300_runtime* rt, hvm_gb300_stats* stats);
+int hvm_gb300_batch_roots(hvm_gb300_runtime* rt, uint32_t* out, size_t cap);
+int hvm_gb300_batch_result(hvm_gb300_runtime* rt, uint32_t net, char* out, size_t cap, size_t* len);
+
 /* One evaluator turn as recorded on the device (no reference counterpart:
  * the reference's per-turn state is only visible through printf debugging,
  * src/hvm.cu:1729-1740). */

@@ -93,6 +93,10 @@ EXPORTED_SYMBOLS = (
     "hvm_gb300_trace",
     "hvm_gb300_reset_counters",
     "hvm_gb300_run_noalloc",
+    "hvm_gb300_load_batch",
+    "hvm_gb300_run_batch",
+    "hvm_gb300_batch_roots",
+    "hvm_gb300_batch_result",
     "hvm_gb300_error",
     "hvm_gb300_destroy",
 )
@@ -126,6 +130,12 @@ def lib() -> ctypes.CDLL:
     L.hvm_gb300_run_noalloc.argtypes = [u32p, ctypes.c_size_t, u32p, u32p, ctypes.c_size_t,
                                         ctypes.POINTER(ctypes.c_size_t), ctypes.POINTER(ctypes.c_uint64),
                                         ctypes.c_char_p, ctypes.c_size_t]
+    L.hvm_gb300_load_batch.argtypes = [ctypes.c_void_p, ctypes.POINTER(u32p), ctypes.POINTER(ctypes.c_size_t),
+                                       ctypes.c_uint32]
+    L.hvm_gb300_run_batch.argtypes = [ctypes.c_void_p, ctypes.POINTER(_Stats)]
+    L.hvm_gb300_batch_roots.argtypes = [ctypes.c_void_p, u32p, ctypes.c_size_t]
+    L.hvm_gb300_batch_result.argtypes = [ctypes.c_void_p, ctypes.c_uint32, ctypes.c_char_p, ctypes.c_size_t,
+                                         ctypes.POINTER(ctypes.c_size_t)]
     L.hvm_gb300_reset_counters.argtypes = [ctypes.c_void_p]
     L.hvm_gb300_reset_counters.restype = None
     L.hvm_gb300_error.argtypes = [ctypes.c_void_p]
@@ -229,12 +239,44 @@ class Runtime:
     def run(self) -> RunStats:
         st = _Stats()
         self._check(lib().hvm_gb300_run(self._h, ctypes.byref(st)))
+        return self._stats(st)
+
+    @staticmethod
+    def _stats(st) -> RunStats:
         return RunStats(itrs=st.itrs, leak=st.leak, turns=st.turns, retries=st.retries, seconds=st.seconds,
                         threads=st.threads, grid=st.grid, block=st.block,
                         rule_hist={RULE_NAMES[i]: int(st.rule_hist[i]) for i in range(8)},
                         prof=tuple(int(x) for x in st.prof), kernel_ms=st.kernel_ms,
                         turn_launches=st.turn_launches, launches=st.launches,
                         h2d_bytes=st.h2d_bytes, d2h_bytes=st.d2h_bytes)
+
+    def load_batch(self, books) -> None:
+        """Loads independent nets (book buffers or .hvm texts) as one batch."""
+        bufs = [np.ascontiguousarray(np.asarray(book_from_text(b) if isinstance(b, str) else b, dtype=np.uint32))
+                for b in books]
+        self._batch = bufs
+        u32p = ctypes.POINTER(ctypes.c_uint32)
+        ptrs = (u32p * len(bufs))(*[b.ctypes.data_as(u32p) for b in bufs])
+        sizes = (ctypes.c_size_t * len(bufs))(*[b.size for b in bufs])
+        self._check(lib().hvm_gb300_load_batch(self._h, ptrs, sizes, len(bufs)))
+
+    def run_batch(self) -> RunStats:
+        st = _Stats()
+        self._check(lib().hvm_gb300_run_batch(self._h, ctypes.byref(st)))
+        return self._stats(st)
+
+    def batch_roots(self) -> np.ndarray:
+        out = np.zeros(len(self._batch), dtype=np.uint32)
+        self._check(lib().hvm_gb300_batch_roots(self._h, out.ctypes.data_as(ctypes.POINTER(ctypes.c_uint32)),
+                                                out.size))
+        return out
+
+    def batch_result(self, net: int) -> str:
+        n = ctypes.c_size_t()
+        self._check(lib().hvm_gb300_batch_result(self._h, net, None, 0, ctypes.byref(n)))
+        out = ctypes.create_string_buffer(n.value + 1)
+        self._check(lib().hvm_gb300_batch_result(self._h, net, out, n.value + 1, ctypes.byref(n)))
+        return out.value.decode()
 
     def result(self) -> str:
         n = ctypes.c_size_t()

@@ -108,6 +108,7 @@ struct Dev {
   unsigned long long ring_mask;
   PagedSpace nspace, vspace;  // per-thread page lists (persist across turns)
   uint32_t npool_end, vpool_end;  // one past the last page id the pools may hand out
+  uint32_t extra_roots;       // nets in a batch - 1: vars ROOT_VAR - k (k <= extra_roots) are roots
   uint32_t* nloc;             // CALL scratch: [max_def_nodes][nthreads]
   uint32_t* vloc;             // CALL scratch: [max_def_vars][nthreads]
   uint32_t nthreads;
@@ -430,7 +431,8 @@ __device__ __forceinline__ void link_pair(const Dev& d, uint32_t gid, const Plan
 __device__ __forceinline__ bool plan_redex(const Dev& d, TState& t, Pair r, Plan& p) {
   Port a = get_fst(r), b = get_snd(r);
   Rule rule = get_rule(a, b);
-  if (get_tag(a) == REF && b == ROOT) rule = CALL;
+  // REF ~ ROOT is a call (src/hvm.c:1090-1092); a batch has one ROOT var per net.
+  if (get_tag(a) == REF && get_tag(b) == VAR && get_val(b) >= ROOT_VAR - d.extra_roots) rule = CALL;
   else if (should_swap(a, b)) { Port x = a; a = b; b = x; }
   p.a = a; p.b = b;
   p.counted = rule != LINK;

@@ -35,6 +35,10 @@ namespace hvm {
 
 // Capacity of each thread's page list (pages of one space a thread may own).
 constexpr uint32_t MAX_PAGES = 64;
+// Batches: nets per batch (each takes one ROOT var at the top of the var
+// space) and definitions over all nets (REF vals have 28 bits).
+constexpr uint32_t MAX_BATCH = 1u << 20;
+constexpr uint32_t MAX_BATCH_DEFS = 1u << 27;
 
 static const char* status_text(uint32_t s) {
   switch (s) {
@@ -308,7 +312,8 @@ __global__ void reset_alloc_kernel(Dev d) {
 // NONE and makes `redex` the only input of the next turn.
 __global__ void boot_kernel(Dev d, Pair redex, uint32_t cap) {
   Ctl* c = d.ctl;
-  d.vars[ROOT_VAR & d.vars_mask] = NONE;
+  const Port root = get_snd(redex);  // ROOT, or net k's ROOT var in a batch
+  if (get_tag(root) == VAR) d.vars[get_val(root) & d.vars_mask] = NONE;
   unsigned long long at = c->tail;
   d.ring[at & d.ring_mask] = redex;
   c->base = at;
@@ -322,6 +327,44 @@ __global__ void boot_kernel(Dev d, Pair redex, uint32_t cap) {
   fixed_policy(c, 1, 1, d.nthreads, cap);
   c->head = at + 1;
   __threadfence();
+}
+
+// Starts a batch: net k's redex `@main_k ~ ROOT_k` with ROOT_k = ROOT_VAR - k.
+__global__ void boot_batch_kernel(Dev d, const uint32_t* mains, uint32_t n, uint32_t cap) {
+  Ctl* c = d.ctl;
+  const unsigned long long at = c->tail;
+  for (uint32_t k = threadIdx.x; k < n; k += blockDim.x) {
+    d.vars[(ROOT_VAR - k) & d.vars_mask] = NONE;
+    d.ring[(at + k) & d.ring_mask] = new_pair(new_port(REF, mains[k]), new_port(VAR, ROOT_VAR - k));
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    c->base = at;
+    c->in_end = at + n;
+    c->tail = at + n;
+    c->pending = n;
+    c->blocks_done = 0;
+    c->dry = 0;
+    c->stop = 0;
+    c->budget = 0;
+    fixed_policy(c, n, n, d.nthreads, cap);
+    unsigned long long take = (unsigned long long)c->static_per_thread * d.nthreads;
+    c->head = at + (take < n ? take : n);
+    __threadfence();
+  }
+}
+
+// out[k] = net k's ROOT with its var chain resolved (read-only).
+__global__ void batch_roots_kernel(Dev d, Port* out, uint32_t n) {
+  uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= n) return;
+  Port p = new_port(VAR, ROOT_VAR - k);
+  for (uint32_t g = 0; g < (1u << 20) && get_tag(p) == VAR; g++) {
+    Port v = __ldcg(&d.vars[get_val(p) & d.vars_mask]);
+    if (v == NONE || v == 0) break;
+    p = v;
+  }
+  out[k] = p;
 }
 
 // Serialises the tree reachable from `root` in breadth-first order:
@@ -380,6 +423,11 @@ class Runtime {
   std::vector<HostDef> defs;
   Dev d{};
   Ctl* ctl = nullptr;
+  uint32_t nroots = 1;                 // nets in the loaded batch (1 for a single book)
+  std::vector<uint32_t> net_main;      // fid of each net's @main
+  std::vector<Port> roots;             // each net's resolved ROOT after run_batch
+  void* mem_roots = nullptr;
+  uint32_t roots_cap = 0;
   void* mem_node = nullptr; void* mem_vars = nullptr; void* mem_ring = nullptr;
   void* mem_cur = nullptr; void* mem_scratch = nullptr;
   void* mem_defs = nullptr; void* mem_book = nullptr; void* mem_trace = nullptr;
@@ -408,9 +456,10 @@ class Runtime {
   int fail(const std::string& m) { if (err.empty()) err = m; return -1; }
 
   void release() {
-    void* ps[] = {mem_node, mem_vars, mem_ring, mem_cur, mem_scratch, mem_defs, mem_book, g_out, g_kids, g_info, ctl, mem_trace};
+    void* ps[] = {mem_node, mem_vars, mem_ring, mem_cur, mem_scratch, mem_defs, mem_book, g_out, g_kids, g_info, ctl,
+                  mem_trace, mem_roots};
     for (void* p : ps) if (p) cudaFree(p);
-    mem_node = mem_vars = mem_ring = mem_cur = mem_scratch = mem_defs = mem_book = mem_trace = nullptr;
+    mem_node = mem_vars = mem_ring = mem_cur = mem_scratch = mem_defs = mem_book = mem_trace = mem_roots = nullptr;
     g_out = nullptr; g_kids = nullptr; g_info = nullptr; ctl = nullptr;
   }
 
@@ -487,6 +536,9 @@ class Runtime {
   int reset_net() {
     CK(cudaMemset(mem_node, 0, (1ull << cfg.node_log2) * sizeof(Pair)));
     CK(cudaMemset(mem_vars, 0, (1ull << cfg.vars_log2) * sizeof(Port)));
+    // The top `nroots` var words are ROOT vars: no page that holds one is handed out.
+    d.vpool_end = (uint32_t)(((1ull << cfg.vars_log2) - nroots) >> d.vspace.page_log2);
+    if (d.vpool_end < d.nthreads) return fail("var space too small for this batch");
     CK(cudaMemset(ctl, 0, sizeof(Ctl)));
     if (cfg.profile) { uint32_t one = 1; CK(cudaMemcpy(&ctl->prof_on, &one, sizeof(one), cudaMemcpyHostToDevice)); }
     uint32_t frac = cfg.stop_frac_q8 ? cfg.stop_frac_q8 : 128;
@@ -509,6 +561,49 @@ class Runtime {
 
   // Parses the book buffer (src/hvm.c:1408-1453 limits and messages).
   int load_book(const uint32_t* w, size_t words) {
+    std::vector<HostDef> parsed;
+    if (parse_book(w, words, parsed)) return -1;
+    defs = std::move(parsed);
+    nroots = 1;
+    return upload_book();
+  }
+
+  // Loads `n` independent nets as one batch: their books are concatenated,
+  // with each net's fids (and the REFs that name them) shifted past the
+  // previous nets' defs. Net k's `@main` becomes fid net_main[k].
+  int load_batch(const uint32_t* const* books, const size_t* words, uint32_t n) {
+    if (n == 0) return fail("empty batch");
+    if (n > MAX_BATCH) return fail("batch larger than " + std::to_string(MAX_BATCH) + " nets");
+    std::vector<HostDef> all;
+    std::vector<uint32_t> mains(n);
+    for (uint32_t k = 0; k < n; k++) {
+      std::vector<HostDef> one;
+      if (parse_book(books[k], words ? words[k] : 0, one)) {
+        err = "net " + std::to_string(k) + ": " + err;
+        return -1;
+      }
+      uint32_t shift = (uint32_t)all.size();
+      if ((uint64_t)shift + one.size() > MAX_BATCH_DEFS) return fail("batch has too many definitions");
+      auto remap = [&](Port p) {
+        if (get_tag(p) != REF) return p;
+        Val v = get_val(p);
+        return new_port(REF, (v & 0x10000000u) | ((v & 0xFFFFFFFu) + shift));
+      };
+      for (HostDef& h : one) {
+        h.root = remap(h.root);
+        for (Pair& q : h.rbag) q = new_pair(remap(get_fst(q)), remap(get_snd(q)));
+        for (Pair& q : h.node) q = new_pair(remap(get_fst(q)), remap(get_snd(q)));
+        all.push_back(std::move(h));
+      }
+      mains[k] = shift;
+    }
+    defs = std::move(all);
+    nroots = n;
+    net_main = mains;
+    return upload_book();
+  }
+
+  int parse_book(const uint32_t* w, size_t words, std::vector<HostDef>& defs) {
     defs.clear();
     if (!w) return fail("null book buffer");
     size_t at = 0;
@@ -560,7 +655,7 @@ class Runtime {
       for (Pair p : h.node) good = good && ok(get_fst(p)) && ok(get_snd(p));
       if (!good) return fail("failed to load book: def '" + h.name + "' has a port outside the def");
     }
-    return upload_book();
+    return 0;
   }
 
   int upload_book() {
@@ -683,15 +778,17 @@ class Runtime {
     return p;
   }
 
-  // Normalises every REF met by the readback (src/hvm.c:1233-1243).
-  int expand(Port p, Port* out) {
-    Port saved = vars_load(ROOT_VAR);
+  // Normalises every REF met by the readback (src/hvm.c:1233-1243). `root`
+  // is the net's ROOT var (ROOT, or ROOT_VAR - k for net k of a batch).
+  int expand(Port p, Port* out, Port root = ROOT) {
+    const uint32_t rv = get_val(root);
+    Port saved = vars_load(rv);
     Port got = peek(p);
     while (get_tag(got) == REF) {
-      if (boot(new_pair(got, ROOT)) || normalize()) return -1;
-      got = peek(vars_load(ROOT_VAR));
+      if (boot(new_pair(got, root)) || normalize()) return -1;
+      got = peek(vars_load(rv));
     }
-    vars_store(ROOT_VAR, saved);
+    vars_store(rv, saved);
     *out = got;
     return 0;
   }
@@ -699,27 +796,70 @@ class Runtime {
   struct Ctr { uint32_t tag; uint32_t nargs; Port args[16]; };
 
   // Lambda-encoded constructor readback (src/run.c:65-97).
-  int read_ctr(Port p, Ctr& c) {
+  int read_ctr(Port p, Ctr& c, Port root = ROOT) {
     c.tag = (uint32_t)-1;
     c.nargs = 0;
     Port lam, app, arg;
-    if (expand(p, &lam)) return -1;
+    if (expand(p, &lam, root)) return -1;
     if (get_tag(lam) != CON) return 0;
     Pair lam_n = node_load(get_val(lam));
-    if (expand(get_fst(lam_n), &app)) return -1;
+    if (expand(get_fst(lam_n), &app, root)) return -1;
     if (get_tag(app) != CON) return 0;
     Pair app_n = node_load(get_val(app));
-    if (expand(get_fst(app_n), &arg)) return -1;
+    if (expand(get_fst(app_n), &arg, root)) return -1;
     if (get_tag(arg) != NUM) return 0;
     c.tag = get_u24(get_val(arg));
     for (;;) {
-      if (expand(get_snd(app_n), &app)) return -1;
+      if (expand(get_snd(app_n), &app, root)) return -1;
       if (get_tag(app) != CON) break;
       app_n = node_load(get_val(app));
-      if (expand(get_fst(app_n), &arg)) return -1;
+      if (expand(get_fst(app_n), &arg, root)) return -1;
       if (c.nargs < 16) c.args[c.nargs] = arg;
       c.nargs++;
     }
+    return 0;
+  }
+
+  // Every net of a batch: boot @main_k ~ ROOT_k, normalise them together,
+  // then run each net's readback walk (which re-normalises REFs it meets).
+  int run_batch() {
+    if (defs.empty() || nroots < 1 || net_main.size() != nroots) return fail("no batch loaded");
+    if (reset_net()) return -1;
+    d.extra_roots = nroots - 1;
+    uint32_t* dm = nullptr;
+    CK(cudaMalloc(&dm, nroots * sizeof(uint32_t)));
+    CK(cudaMemcpy(dm, net_main.data(), nroots * sizeof(uint32_t), cudaMemcpyHostToDevice));
+    h2d_bytes += nroots * sizeof(uint32_t);
+    boot_batch_kernel<<<1, 1024>>>(d, dm, nroots, cap);
+    cudaError_t e = cudaGetLastError();
+    launches++;
+    cudaFree(dm);
+    CK(e);
+    if (normalize()) return -1;
+    if (read_roots()) return -1;
+    for (uint32_t k = 0; k < nroots; k++) {
+      Tag t = get_tag(roots[k]);
+      if (t != REF && t != CON) continue;  // the walk stops at once
+      Port root = new_port(VAR, ROOT_VAR - k);
+      Ctr c;
+      if (read_ctr(peek(root), c, root)) return -1;
+    }
+    return read_roots();
+  }
+
+  int read_roots() {
+    if (!mem_roots || roots_cap < nroots) {
+      if (mem_roots) cudaFree(mem_roots);
+      mem_roots = nullptr;
+      CK(cudaMalloc(&mem_roots, nroots * sizeof(Port)));
+      roots_cap = nroots;
+    }
+    batch_roots_kernel<<<(nroots + 255) / 256, 256>>>(d, (Port*)mem_roots, nroots);
+    CK(cudaGetLastError());
+    launches++;
+    roots.resize(nroots);
+    CK(cudaMemcpy(roots.data(), mem_roots, nroots * sizeof(Port), cudaMemcpyDeviceToHost));
+    d2h_bytes += nroots * sizeof(Port);
     return 0;
   }
 
@@ -727,6 +867,7 @@ class Runtime {
   int run_main() {
     if (defs.empty()) return fail("no book loaded");
     if (reset_net()) return -1;
+    d.extra_roots = 0;
     if (boot(new_pair(new_port(REF, 0), ROOT))) return -1;
     for (;;) {
       if (normalize()) return -1;
@@ -743,14 +884,14 @@ class Runtime {
 
   // Serialises the tree at ROOT and prints it in the reference's format
   // (src/hvm.c:1535-1699).
-  int result_text(std::string& s) {
+  int result_text(std::string& s, Port root = ROOT) {
     if (!g_info) {
       gather_cap = 1u << 24;
       CK(cudaMalloc((void**)&g_out, gather_cap * sizeof(Port)));
       CK(cudaMalloc((void**)&g_kids, gather_cap * sizeof(uint32_t)));
       CK(cudaMalloc((void**)&g_info, 2 * sizeof(uint32_t)));
     }
-    gather_kernel<<<1, 1024>>>(d, ROOT, g_out, g_kids, gather_cap, g_info);
+    gather_kernel<<<1, 1024>>>(d, root, g_out, g_kids, gather_cap, g_info);
     CK(cudaGetLastError());
     launches++;
     uint32_t info[2];
@@ -901,6 +1042,43 @@ extern "C" int hvm_gb300_run(hvm_gb300_runtime* r, hvm_gb300_stats* stats) {
   r->rt.err.clear();
   if (r->rt.run_main()) return -1;
   if (stats && r->rt.stats(stats)) return -1;
+  return 0;
+}
+
+extern "C" int hvm_gb300_load_batch(hvm_gb300_runtime* r, const uint32_t* const* books, const size_t* words,
+                                    uint32_t n) {
+  if (!r) return -1;
+  r->rt.err.clear();
+  return r->rt.load_batch(books, words, n);
+}
+
+extern "C" int hvm_gb300_run_batch(hvm_gb300_runtime* r, hvm_gb300_stats* stats) {
+  if (!r) return -1;
+  r->rt.err.clear();
+  if (r->rt.run_batch()) return -1;
+  if (stats && r->rt.stats(stats)) return -1;
+  return 0;
+}
+
+extern "C" int hvm_gb300_batch_roots(hvm_gb300_runtime* r, uint32_t* out, size_t cap) {
+  if (!r) return -1;
+  if (r->rt.roots.size() != r->rt.nroots) return r->rt.fail("no batch has run");
+  if (cap < r->rt.roots.size()) return r->rt.fail("output too small");
+  memcpy(out, r->rt.roots.data(), r->rt.roots.size() * sizeof(uint32_t));
+  return 0;
+}
+
+extern "C" int hvm_gb300_batch_result(hvm_gb300_runtime* r, uint32_t net, char* out, size_t cap, size_t* len) {
+  if (!r) return -1;
+  if (net >= r->rt.nroots) return r->rt.fail("net index out of range");
+  std::string s;
+  if (r->rt.result_text(s, hvm::new_port(hvm::VAR, hvm::ROOT_VAR - net))) return -1;
+  if (len) *len = s.size();
+  if (out) {
+    if (cap <= s.size()) { r->rt.fail("result buffer too small"); return -2; }
+    memcpy(out, s.data(), s.size());
+    out[s.size()] = 0;
+  }
   return 0;
 }
 

@@ -10,6 +10,9 @@ reference sources exist; the fixtures travel, the reference does not).
                              built in place by oracle/Makefile as
                              oracle/_ref/hvm_ref) on this repository's book
                              buffer.
+  batch_mixed_4096.json    per net of the 4096-net mixed batch
+                           (workloads.mixed_batch): its family and size, the
+                           reference C runtime's interaction count and result.
   configs.json             the same two fields for the seeded benchmark
                            workloads (lambdavm-rust_gb300/workloads.py), with
                            large results stored as a SHA-256 of their
@@ -70,6 +73,23 @@ def run_ref(code: str) -> dict:
     return {"result": res.group(1), "itrs": int(itrs.group(1))}
 
 
+def _batch_entry(item):
+    idx, code, info = item
+    r = run_ref(code)
+    return {"net": idx, **info, "itrs": r["itrs"], "result": r["result"]}
+
+
+def make_batch(count: int = 4096, workers: int = 4) -> None:
+    import multiprocessing as mp
+    nets = W.mixed_batch(count)
+    items = [(i, code, info) for i, (code, info) in enumerate(nets)]
+    with mp.get_context("spawn").Pool(workers) as pool:
+        out = pool.map(_batch_entry, items, chunksize=8)
+    with open(os.path.join(HERE, f"batch_mixed_{count}.json"), "w") as f:
+        json.dump({"count": count, "total_itrs": sum(e["itrs"] for e in out), "nets": out}, f)
+    print("batch", count, sum(e["itrs"] for e in out))
+
+
 def snapshot_result(ref: str, rel: str) -> str | None:
     key = rel.replace("tests/programs/", "").replace("examples/", "").replace("/", "__")
     for snap in glob.glob(os.path.join(ref, "tests", "snapshots", "*.snap")):
@@ -84,7 +104,11 @@ def main() -> None:
     ap = argparse.ArgumentParser()
     ap.add_argument("--reference", default="/root/reference")
     ap.add_argument("--skip-configs", action="store_true")
+    ap.add_argument("--only-batch", action="store_true")
     args = ap.parse_args()
+    if args.only_batch:
+        make_batch()
+        return
     subprocess.run(["make", "-C", os.path.join(ROOT, "oracle"), "ref", f"REF_SRC={args.reference}/src"], check=True)
     subprocess.run(["make", "-C", os.path.join(ROOT, "oracle")], check=True)
 
@@ -132,6 +156,7 @@ def main() -> None:
         print(name, entry["itrs"])
     with open(os.path.join(HERE, "configs.json"), "w") as f:
         json.dump(out, f, indent=1)
+    make_batch()
 
 
 if __name__ == "__main__":

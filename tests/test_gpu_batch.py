@@ -1,0 +1,64 @@
+"""Batched evaluation: many independent nets in the same launches. Each net's
+normal form must equal the reference's, and the batch's interaction count
+must equal the sum of the nets' counts under the reference."""
+from __future__ import annotations
+
+import json
+import os
+
+import pytest
+
+from conftest import GOLDEN
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def batch_golden():
+    with open(os.path.join(GOLDEN, "batch_mixed_4096.json")) as f:
+        return json.load(f)
+
+
+def numb_value(port: int) -> int:
+    assert port & 7 == 3, f"not a number: {port:#x}"
+    return (port >> 3) >> 5  # u24 payload
+
+
+def check_roots(roots, nets):
+    for k, (p, g) in enumerate(zip(roots, nets)):
+        assert numb_value(int(p)) == int(g["result"]), (k, g)
+
+
+def test_batch_prefix(hvm, workloads, batch_golden):
+    n = 96
+    nets = workloads.mixed_batch(4096)[:n]
+    gold = batch_golden["nets"][:n]
+    with hvm.Runtime(device=0) as rt:
+        rt.load_batch([code for code, _ in nets])
+        for _ in range(2):
+            st = rt.run_batch()
+            assert st.itrs == sum(g["itrs"] for g in gold)
+            check_roots(rt.batch_roots(), gold)
+        assert hvm.canonical(rt.batch_result(5)) == hvm.canonical(gold[5]["result"])
+
+
+def test_batch_of_reference_programs(hvm, ref_programs):
+    # Non-numeric normal forms and the readback expansion (which re-normalises
+    # REFs and adds interactions) per net of a batch.
+    progs = [p for p in ref_programs if "result" in p and p["itrs"] < 200_000]
+    with hvm.Runtime(device=0) as rt:
+        rt.load_batch([p["code"] for p in progs])
+        st = rt.run_batch()
+        assert st.itrs == sum(p["itrs"] for p in progs)
+        for k, p in enumerate(progs):
+            assert hvm.canonical(rt.batch_result(k)) == hvm.canonical(p["result"]), p["name"]
+
+
+@pytest.mark.slow
+def test_batch_4096(hvm, workloads, batch_golden):
+    nets = workloads.mixed_batch(4096)
+    with hvm.Runtime(device=0) as rt:
+        rt.load_batch([code for code, _ in nets])
+        st = rt.run_batch()
+        assert st.itrs == batch_golden["total_itrs"]
+        check_roots(rt.batch_roots(), batch_golden["nets"])
