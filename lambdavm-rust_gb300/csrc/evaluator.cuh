@@ -109,6 +109,7 @@ struct Dev {
   PagedSpace nspace, vspace;  // per-thread page lists (persist across turns)
   uint32_t npool_end, vpool_end;  // one past the last page id the pools may hand out
   uint32_t extra_roots;       // nets in a batch - 1: vars ROOT_VAR - k (k <= extra_roots) are roots
+  uint32_t tables;            // 1 when nloc/vloc hold CHUNK words per thread at least
   uint32_t* nloc;             // CALL scratch: [max_def_nodes][nthreads]
   uint32_t* vloc;             // CALL scratch: [max_def_vars][nthreads]
   uint32_t nthreads;
@@ -221,6 +222,7 @@ __device__ __forceinline__ void ld_cg_v4(const void* p, unsigned long long& a, u
 
 constexpr uint32_t CHUNK = 32;  // words per scanned chunk (256 B of nodes, 128 B of vars)
 constexpr uint32_t MAX_DRY_PAGES = 4;  // full cycles over a lane's pages before out-of-memory
+constexpr uint32_t SOFT_RUN_CHUNKS = 32;  // chunks a CALL scans for a contiguous run before taking single words
 
 // Bit i of the result is set when word base+i is free and may be handed out.
 template <bool VARS>
@@ -265,10 +267,11 @@ __device__ __forceinline__ uint32_t runs_of(uint32_t m, uint32_t n) {
 // written at once (vars as NONE, nodes as MARK) so no later scan can see them
 // free before their owner fills them.
 template <bool VARS>
-__device__ __forceinline__ uint32_t alloc_run(const Dev& d, TState& t, Alloc& a, uint32_t n) {
+__device__ __forceinline__ uint32_t alloc_run(const Dev& d, TState& t, Alloc& a, uint32_t n, uint32_t soft_limit = 0) {
   const PagedSpace& sp = VARS ? d.vspace : d.nspace;
   const uint32_t page_words = 1u << sp.page_log2;
   const uint32_t chunks_per_page = page_words / CHUNK;
+  uint32_t scanned = 0;
   for (uint32_t guard = 0; guard < (1u << 22); guard++) {
     uint32_t r = runs_of(a.mask, n);
     if (r) {
@@ -306,6 +309,9 @@ __device__ __forceinline__ uint32_t alloc_run(const Dev& d, TState& t, Alloc& a,
         a.page = __ldcg(&sp.lists[(size_t)t.gid * sp.max_pages + a.pos]);
       }
     }
+    // A soft request (a contiguous run the caller can do without) gives up
+    // after `soft_limit` chunks instead of growing or failing.
+    if (soft_limit && scanned++ >= soft_limit) return 0;
     a.chunk = (a.page << sp.page_log2) + a.off;
     a.off += CHUNK;
     a.mask = chunk_mask<VARS>(d, a.chunk);
@@ -572,11 +578,20 @@ __device__ __forceinline__ int lockstep_round(const Dev& d, TState& t, bool has,
       default: {  // CALL (src/hvm.c:865-898)
         p.contig = p.node_len <= CHUNK && p.vars_len <= CHUNK;
         if (p.contig) {
-          // Vars first (taken as NONE), then the nodes, written in place.
-          p.vbase = p.vars_len ? alloc_run<true>(d, t, t.va, p.vars_len) : 0;
-          p.nbase = p.node_len ? alloc_run<false>(d, t, t.na, p.node_len) : 0;
-          if ((p.vars_len && !p.vbase) || (p.node_len && !p.nbase)) { rc = IR_FATAL; break; }
-        } else {
+          // Vars first (taken as NONE), then the nodes: one contiguous run
+          // each, so relocation is base + index. In a fragmented space the
+          // runs may not be found quickly; then the words are taken one by
+          // one and relocated through the per-thread tables.
+          const uint32_t soft = d.tables ? SOFT_RUN_CHUNKS : 0;
+          p.vbase = p.vars_len ? alloc_run<true>(d, t, t.va, p.vars_len, soft) : 0;
+          p.nbase = (p.node_len && (p.vbase || !p.vars_len)) ? alloc_run<false>(d, t, t.na, p.node_len, soft) : 0;
+          if ((p.vars_len && !p.vbase) || (p.node_len && !p.nbase)) {
+            if (!d.tables) { rc = IR_FATAL; break; }
+            if (p.vbase) for (uint32_t i = 0; i < p.vars_len; i++) vstore(d, p.vbase + i, 0);  // give back
+            p.contig = false;
+          }
+        }
+        if (!p.contig) {
           for (uint32_t i = 0; i < p.node_len && rc == IR_DONE; i++) {
             uint32_t at = alloc_node(d, t);
             if (!at) rc = IR_FATAL;

@@ -681,7 +681,12 @@ class Runtime {
     CK(cudaMemcpy(mem_defs, hdr.data(), hdr.size() * sizeof(DefHdr), cudaMemcpyHostToDevice));
     CK(cudaMemcpy(mem_book, flat.data(), flat.size() * sizeof(Pair), cudaMemcpyHostToDevice));
     h2d_bytes += hdr.size() * sizeof(DefHdr) + flat.size() * sizeof(Pair);
+    // Relocation tables: for defs larger than a chunk, and as the fallback
+    // when a CALL finds no contiguous run; so at least CHUNK words each.
+    if (max_def_nodes < CHUNK) max_def_nodes = CHUNK;
+    if (max_def_vars < CHUNK) max_def_vars = CHUNK;
     CK(cudaMalloc(&mem_scratch, (size_t)(max_def_nodes + max_def_vars) * d.nthreads * sizeof(uint32_t)));
+    d.tables = 1;
     d.defs = (const DefHdr*)mem_defs;
     d.book = (const Pair*)mem_book;
     d.ndefs = (uint32_t)defs.size();
