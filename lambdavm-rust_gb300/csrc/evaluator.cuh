@@ -80,6 +80,7 @@ struct alignas(128) Ctl {
   unsigned long long hist[8];       // interactions per rule (diagnostic)
   unsigned long long prof[8];       // profile counters (when prof_on): see PROF_*
   unsigned int prof_on;
+  unsigned int oom_space, oom_pages, oom_dry, oom_pool_dry;  // diagnostics of the first out-of-memory
   unsigned int npool_next;          // next page id of the node pool
   unsigned int vpool_next;          // next page id of the var pool
   TurnRecord* trace;                // per-turn records (null = off)
@@ -287,7 +288,9 @@ __device__ __forceinline__ uint32_t alloc_run(const Dev& d, TState& t, Alloc& a,
     if (a.off >= page_words) {
       a.off = 0;
       bool grabbed = false;
-      if ((a.dry_chunks >= 2 * chunks_per_page || (a.count == 1 && a.dry_chunks >= chunks_per_page)) &&
+      // Only a hard request takes a fresh page: a soft one (a contiguous run)
+      // gives up instead, so pages are not taken for fragmentation alone.
+      if (!soft_limit && (a.dry_chunks >= 2 * chunks_per_page || (a.count == 1 && a.dry_chunks >= chunks_per_page)) &&
           a.count < sp.max_pages && !a.pool_dry) {
         uint32_t fresh = atomicAdd(pool_counter(d, VARS), 1u);
         if (fresh < (VARS ? d.vpool_end : d.npool_end)) {
@@ -304,7 +307,14 @@ __device__ __forceinline__ uint32_t alloc_run(const Dev& d, TState& t, Alloc& a,
       }
       if (!grabbed) {
         // Every owned page scanned several times over without room: full.
-        if (a.dry_chunks >= MAX_DRY_PAGES * chunks_per_page * a.count) return 0;
+        if (a.dry_chunks >= MAX_DRY_PAGES * chunks_per_page * a.count) {
+          if (atomicCAS(&d.ctl->oom_space, 0u, VARS ? 2u : 1u) == 0u) {
+            d.ctl->oom_pages = a.count;
+            d.ctl->oom_dry = a.dry_chunks;
+            d.ctl->oom_pool_dry = a.pool_dry ? 1u : 0u;
+          }
+          return 0;
+        }
         a.pos = a.pos + 1 == a.count ? 0 : a.pos + 1;
         a.page = __ldcg(&sp.lists[(size_t)t.gid * sp.max_pages + a.pos]);
       }

@@ -736,7 +736,15 @@ class Runtime {
         CK(cudaEventElapsedTime(&ms, events[2 * i], events[2 * i + 1]));
         kernel_ms += ms;
       }
-      if (h.status) return fail(std::string("device error: ") + status_text(h.status) + " (info " + std::to_string(h.err_info) + ")");
+      if (h.status) {
+        std::string m = std::string("device error: ") + status_text(h.status) + " (info " + std::to_string(h.err_info) + ")";
+        if (h.oom_space)
+          m += " [" + std::string(h.oom_space == 2 ? "var" : "node") + " pages owned " + std::to_string(h.oom_pages) +
+               ", dry chunks " + std::to_string(h.oom_dry) + ", pool " + (h.oom_pool_dry ? "empty" : "not empty") +
+               ", pools at " + std::to_string(h.npool_next) + "/" + std::to_string(d.npool_end) + " and " +
+               std::to_string(h.vpool_next) + "/" + std::to_string(d.vpool_end) + "]";
+        return fail(m);
+      }
       if (h.base == h.in_end) break;
       if (cfg.max_turns && turns_run >= cfg.max_turns) return fail("turn budget exhausted before normal form");
       // A net whose interaction count stops moving while redexes remain is
