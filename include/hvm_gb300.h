@@ -131,6 +131,12 @@ int hvm_gb300_run_batch(hvm_gb300_runtime* rt, hvm_gb300_stats* stats);
 int hvm_gb300_batch_roots(hvm_gb300_runtime* rt, uint32_t* out, size_t cap);
 int hvm_gb300_batch_result(hvm_gb300_runtime* rt, uint32_t net, char* out, size_t cap, size_t* len);
 
+/* Diagnostic counterpart of the reference's count_memory kernel
+ * (src/hvm.cu:2234-2255): out[0] live node words, out[1] live var words,
+ * out[2] node words taken but not yet written, out[3] / out[4] node / var
+ * pages handed out by the pools so far. */
+int hvm_gb300_count_live(hvm_gb300_runtime* rt, uint64_t* out);
+
 /* One evaluator turn as recorded on the device (no reference counterpart:
  * the reference's per-turn state is only visible through printf debugging,
  * src/hvm.cu:1729-1740). */

@@ -97,6 +97,7 @@ EXPORTED_SYMBOLS = (
     "hvm_gb300_run_batch",
     "hvm_gb300_batch_roots",
     "hvm_gb300_batch_result",
+    "hvm_gb300_count_live",
     "hvm_gb300_error",
     "hvm_gb300_destroy",
 )
@@ -136,6 +137,7 @@ def lib() -> ctypes.CDLL:
     L.hvm_gb300_batch_roots.argtypes = [ctypes.c_void_p, u32p, ctypes.c_size_t]
     L.hvm_gb300_batch_result.argtypes = [ctypes.c_void_p, ctypes.c_uint32, ctypes.c_char_p, ctypes.c_size_t,
                                          ctypes.POINTER(ctypes.c_size_t)]
+    L.hvm_gb300_count_live.argtypes = [ctypes.c_void_p, ctypes.POINTER(ctypes.c_uint64)]
     L.hvm_gb300_reset_counters.argtypes = [ctypes.c_void_p]
     L.hvm_gb300_reset_counters.restype = None
     L.hvm_gb300_error.argtypes = [ctypes.c_void_p]
@@ -284,6 +286,11 @@ class Runtime:
         out = ctypes.create_string_buffer(n.value + 1)
         self._check(lib().hvm_gb300_result(self._h, out, n.value + 1, ctypes.byref(n)))
         return out.value.decode()
+
+    def count_live(self) -> dict:
+        out = (ctypes.c_uint64 * 5)()
+        self._check(lib().hvm_gb300_count_live(self._h, out))
+        return {"nodes": out[0], "vars": out[1], "marked": out[2], "node_pages": out[3], "var_pages": out[4]}
 
     def reset_counters(self) -> None:
         lib().hvm_gb300_reset_counters(self._h)

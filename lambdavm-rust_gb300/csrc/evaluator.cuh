@@ -81,6 +81,10 @@ struct alignas(128) Ctl {
   unsigned long long prof[8];       // profile counters (when prof_on): see PROF_*
   unsigned int prof_on;
   unsigned int oom_space, oom_pages, oom_dry, oom_pool_dry;  // diagnostics of the first out-of-memory
+  // Free-page rings (node, var): pages returned by lanes that found them
+  // empty. Taken from [head, end) during a turn, returned at tail; `end`
+  // moves to `tail` between turns (the redex ring's discipline).
+  unsigned int nf_head, nf_tail, nf_end, vf_head, vf_tail, vf_end;
   unsigned int npool_next;          // next page id of the node pool
   unsigned int vpool_next;          // next page id of the var pool
   TurnRecord* trace;                // per-turn records (null = off)
@@ -111,6 +115,9 @@ struct Dev {
   uint32_t npool_end, vpool_end;  // one past the last page id the pools may hand out
   uint32_t extra_roots;       // nets in a batch - 1: vars ROOT_VAR - k (k <= extra_roots) are roots
   uint32_t tables;            // 1 when nloc/vloc hold CHUNK words per thread at least
+  uint32_t* nfree_ring;       // free-page rings (null: pages are never returned)
+  uint32_t* vfree_ring;
+  uint32_t nfree_mask, vfree_mask;
   uint32_t* nloc;             // CALL scratch: [max_def_nodes][nthreads]
   uint32_t* vloc;             // CALL scratch: [max_def_vars][nthreads]
   uint32_t nthreads;
@@ -144,6 +151,7 @@ struct Alloc {
   uint32_t mask;             // free words of that chunk not yet handed out
   uint32_t dry_chunks;       // chunks scanned since the last free word
   bool pool_dry;             // the page pool ran out during this turn
+  bool page_empty;           // every chunk of this page seen in this pass was entirely free
 };
 
 // ---- per-thread state ----------------------------------------------------------
@@ -284,25 +292,57 @@ __device__ __forceinline__ uint32_t alloc_run(const Dev& d, TState& t, Alloc& a,
       }
       return at;
     }
+    // Leaving a chunk that was entirely free and untouched keeps the page a
+    // candidate for return.
+    if (a.mask != 0xFFFFFFFFu) a.page_empty = false;
     // Next chunk: within the page, then the next owned page, then a new page.
     if (a.off >= page_words) {
       a.off = 0;
-      bool grabbed = false;
+      uint32_t* ring = VARS ? d.vfree_ring : d.nfree_ring;
+      bool moved = false;
+      if (a.page_empty && a.count > 1 && ring) {
+        // The whole page is free: give it back to the free-page ring and
+        // drop it from this lane's list.
+        unsigned int* tail = VARS ? &d.ctl->vf_tail : &d.ctl->nf_tail;
+        ring[atomicAdd(tail, 1u) & (VARS ? d.vfree_mask : d.nfree_mask)] = a.page;
+        uint32_t* list = sp.lists + (size_t)t.gid * sp.max_pages;
+        list[a.pos] = list[a.count - 1];
+        a.count--;
+        sp.counts[t.gid] = a.count;
+        if (a.pos >= a.count) a.pos = 0;
+        a.page = list[a.pos];
+        a.page_empty = true;
+        moved = true;  // scan the page that took its place
+      }
+      bool grabbed = moved;
       // Only a hard request takes a fresh page: a soft one (a contiguous run)
       // gives up instead, so pages are not taken for fragmentation alone.
-      if (!soft_limit && (a.dry_chunks >= 2 * chunks_per_page || (a.count == 1 && a.dry_chunks >= chunks_per_page)) &&
+      if (!moved && !soft_limit && (a.dry_chunks >= 2 * chunks_per_page || (a.count == 1 && a.dry_chunks >= chunks_per_page)) &&
           a.count < sp.max_pages && !a.pool_dry) {
-        uint32_t fresh = atomicAdd(pool_counter(d, VARS), 1u);
-        if (fresh < (VARS ? d.vpool_end : d.npool_end)) {
+        uint32_t fresh = 0xFFFFFFFFu;
+        if (ring) {  // a returned page first
+          unsigned int* head = VARS ? &d.ctl->vf_head : &d.ctl->nf_head;
+          unsigned int end = __ldcg(VARS ? &d.ctl->vf_end : &d.ctl->nf_end);
+          if (__ldcg(head) < end) {
+            unsigned int h = atomicAdd(head, 1u);
+            if (h < end) fresh = __ldcg(&ring[h & (VARS ? d.vfree_mask : d.nfree_mask)]);
+          }
+        }
+        if (fresh == 0xFFFFFFFFu) {
+          uint32_t f = atomicAdd(pool_counter(d, VARS), 1u);
+          if (f < (VARS ? d.vpool_end : d.npool_end)) fresh = f;
+        }
+        if (fresh != 0xFFFFFFFFu) {
           sp.lists[(size_t)t.gid * sp.max_pages + a.count] = fresh;
           a.pos = a.count;
           a.count++;
           sp.counts[t.gid] = a.count;
           a.page = fresh;
           a.dry_chunks = 0;
+          a.page_empty = true;
           grabbed = true;
         } else {
-          a.pool_dry = true;  // pool exhausted: keep cycling through owned pages
+          a.pool_dry = true;  // no page anywhere: keep cycling through owned pages
         }
       }
       if (!grabbed) {
@@ -317,6 +357,7 @@ __device__ __forceinline__ uint32_t alloc_run(const Dev& d, TState& t, Alloc& a,
         }
         a.pos = a.pos + 1 == a.count ? 0 : a.pos + 1;
         a.page = __ldcg(&sp.lists[(size_t)t.gid * sp.max_pages + a.pos]);
+        a.page_empty = true;
       }
     }
     // A soft request (a contiguous run the caller can do without) gives up
@@ -347,6 +388,7 @@ __device__ __forceinline__ void alloc_load(const PagedSpace& sp, uint32_t gid, A
   a.mask = 0;
   a.dry_chunks = 0;
   a.pool_dry = false;
+  a.page_empty = false;  // resumed mid-page: unknown
 }
 
 __device__ __forceinline__ void alloc_save(const PagedSpace& sp, uint32_t gid, const Alloc& a) {

@@ -282,6 +282,11 @@ __global__ void __launch_bounds__(128, MIN_BLOCKS_128 > 0 ? MIN_BLOCKS_128 : 1) 
       c->turns += 1;
       c->dry = 0;
       c->stop = 0;
+      // Free-page rings: the pages returned this turn become takeable.
+      c->nf_head = c->nf_head < c->nf_end ? c->nf_head : c->nf_end;
+      c->nf_end = c->nf_tail;
+      c->vf_head = c->vf_head < c->vf_end ? c->vf_head : c->vf_end;
+      c->vf_end = c->vf_tail;
       fixed_policy(c, pending, prev_pending, d.nthreads, cap);
       unsigned long long take = (unsigned long long)c->static_per_thread * d.nthreads;
       c->head = nb + (take < pending ? take : pending);
@@ -367,6 +372,27 @@ __global__ void batch_roots_kernel(Dev d, Port* out, uint32_t n) {
   out[k] = p;
 }
 
+// Counts live words of the net (the reference's count_memory debug kernel,
+// src/hvm.cu:2234-2255): out[0] += non-zero node words, out[1] += non-zero
+// var words, out[2] += node words still marked as taken-but-unwritten.
+__global__ void count_live_kernel(Dev d, uint64_t n_nodes, uint64_t n_vars, unsigned long long* out) {
+  unsigned long long a = 0, b = 0, m = 0;
+  for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n_nodes; i += (uint64_t)gridDim.x * blockDim.x) {
+    Pair v = d.node[i];
+    a += v != 0;
+    m += v == NODE_MARK;
+  }
+  for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n_vars; i += (uint64_t)gridDim.x * blockDim.x) {
+    b += d.vars[i] != 0;
+  }
+  for (int o = 16; o > 0; o >>= 1) {
+    a += __shfl_down_sync(0xFFFFFFFFu, a, o);
+    b += __shfl_down_sync(0xFFFFFFFFu, b, o);
+    m += __shfl_down_sync(0xFFFFFFFFu, m, o);
+  }
+  if ((threadIdx.x & 31) == 0) { atomicAdd(&out[0], a); atomicAdd(&out[1], b); atomicAdd(&out[2], m); }
+}
+
 // Serialises the tree reachable from `root` in breadth-first order:
 // out[k] is a port with its var chain resolved; for a node port, kids[k] is
 // the index of its first child (the second child follows it). One block.
@@ -430,7 +456,7 @@ class Runtime {
   uint32_t roots_cap = 0;
   void* mem_node = nullptr; void* mem_vars = nullptr; void* mem_ring = nullptr;
   void* mem_cur = nullptr; void* mem_scratch = nullptr;
-  void* mem_defs = nullptr; void* mem_book = nullptr; void* mem_trace = nullptr;
+  void* mem_defs = nullptr; void* mem_book = nullptr; void* mem_trace = nullptr; void* mem_free = nullptr;
   Port* g_out = nullptr; uint32_t* g_kids = nullptr; uint32_t* g_info = nullptr;
   uint32_t gather_cap = 0;
   uint32_t grid = 0, block = 0, cap = 0;
@@ -457,9 +483,9 @@ class Runtime {
 
   void release() {
     void* ps[] = {mem_node, mem_vars, mem_ring, mem_cur, mem_scratch, mem_defs, mem_book, g_out, g_kids, g_info, ctl,
-                  mem_trace, mem_roots};
+                  mem_trace, mem_roots, mem_free};
     for (void* p : ps) if (p) cudaFree(p);
-    mem_node = mem_vars = mem_ring = mem_cur = mem_scratch = mem_defs = mem_book = mem_trace = mem_roots = nullptr;
+    mem_node = mem_vars = mem_ring = mem_cur = mem_scratch = mem_defs = mem_book = mem_trace = mem_roots = mem_free = nullptr;
     g_out = nullptr; g_kids = nullptr; g_info = nullptr; ctl = nullptr;
   }
 
@@ -517,6 +543,15 @@ class Runtime {
     // Page lists + counts + positions + offsets, for both spaces.
     CK(cudaMalloc(&mem_cur, 2ull * nthreads * (MAX_PAGES + 3) * sizeof(uint32_t)));
     CK(cudaMalloc((void**)&ctl, sizeof(Ctl)));
+    {
+      // One free-page ring per space, as large as the space's page count.
+      uint64_t np = n_nodes >> d.nspace.page_log2, vp = n_vars >> d.vspace.page_log2;
+      CK(cudaMalloc(&mem_free, (np + vp) * sizeof(uint32_t)));
+      d.nfree_ring = (uint32_t*)mem_free;
+      d.vfree_ring = d.nfree_ring + np;
+      d.nfree_mask = (uint32_t)(np - 1);
+      d.vfree_mask = (uint32_t)(vp - 1);
+    }
     d.node = (Pair*)mem_node;
     d.vars = (Port*)mem_vars;
     d.ring = (Pair*)mem_ring;
@@ -1092,6 +1127,24 @@ extern "C" int hvm_gb300_batch_result(hvm_gb300_runtime* r, uint32_t net, char* 
     memcpy(out, s.data(), s.size());
     out[s.size()] = 0;
   }
+  return 0;
+}
+
+extern "C" int hvm_gb300_count_live(hvm_gb300_runtime* r, uint64_t* out3) {  // out3: 5 words
+  if (!r || !out3) return -1;
+  hvm::Runtime& rt = r->rt;
+  unsigned long long* dev = nullptr;
+  if (cudaMalloc(&dev, 3 * sizeof(unsigned long long)) != cudaSuccess) return rt.fail("cudaMalloc failed");
+  cudaMemset(dev, 0, 3 * sizeof(unsigned long long));
+  hvm::count_live_kernel<<<1024, 256>>>(rt.d, 1ull << rt.cfg.node_log2, 1ull << rt.cfg.vars_log2, dev);
+  unsigned long long h[3] = {0, 0, 0};
+  cudaError_t e = cudaMemcpy(h, dev, sizeof(h), cudaMemcpyDeviceToHost);
+  cudaFree(dev);
+  if (e != cudaSuccess) return rt.fail(cudaGetErrorString(e));
+  hvm::Ctl c;
+  if (rt.read_ctl(c)) return -1;
+  out3[0] = h[0]; out3[1] = h[1]; out3[2] = h[2];
+  out3[3] = c.npool_next; out3[4] = c.vpool_next;
   return 0;
 }
 
