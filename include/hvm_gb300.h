@@ -129,6 +129,17 @@ int hvm_gb300_result(hvm_gb300_runtime* rt, char* out, size_t cap, size_t* len);
 int hvm_gb300_load_batch(hvm_gb300_runtime* rt, const uint32_t* const* books, const size_t* words, uint32_t n);
 int hvm_gb300_run_batch(hvm_gb300_runtime* rt, hvm_gb300_stats* stats);
 int hvm_gb300_batch_roots(hvm_gb300_runtime* rt, uint32_t* out, size_t cap);
+
+/* Continuous batching over a loaded batch (serving): net k is admitted once
+ * `arrival_s[k]` seconds have passed (non-decreasing), while fewer than
+ * `max_inflight` nets are in flight (0 = no cap) and live node and var words
+ * stay under `live_frac` of their spaces; admitted nets share the turns with
+ * the nets already running. A net completes when its ROOT becomes a number
+ * (`done_s[k]` = seconds since the start, `result_ports[k]` = that port);
+ * nets with other normal forms complete when the batch is quiescent. The
+ * stats' itrs is the total over all nets. */
+int hvm_gb300_run_stream(hvm_gb300_runtime* rt, const double* arrival_s, uint32_t max_inflight, double live_frac,
+                         double* done_s, uint32_t* result_ports, hvm_gb300_stats* stats);
 int hvm_gb300_batch_result(hvm_gb300_runtime* rt, uint32_t net, char* out, size_t cap, size_t* len);
 
 /* Diagnostic counterpart of the reference's count_memory kernel
@@ -142,6 +153,7 @@ int hvm_gb300_count_live(hvm_gb300_runtime* rt, uint64_t* out);
  * src/hvm.cu:1729-1740). */
 typedef struct {
   uint64_t t_ns;        /* device clock when the turn closed */
+  int64_t live_nodes;   /* node words in use after the turn */
   uint64_t itrs;        /* cumulative interactions */
   uint64_t pending;     /* redexes left for the next turn */
   uint32_t dry;         /* threads that ran out of work */

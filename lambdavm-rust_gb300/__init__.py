@@ -49,6 +49,7 @@ class Config(ctypes.Structure):
 class Turn(ctypes.Structure):
     _fields_ = [
         ("t_ns", ctypes.c_uint64),
+        ("live_nodes", ctypes.c_int64),
         ("itrs", ctypes.c_uint64),
         ("pending", ctypes.c_uint64),
         ("dry", ctypes.c_uint32),
@@ -96,6 +97,7 @@ EXPORTED_SYMBOLS = (
     "hvm_gb300_load_batch",
     "hvm_gb300_run_batch",
     "hvm_gb300_batch_roots",
+    "hvm_gb300_run_stream",
     "hvm_gb300_batch_result",
     "hvm_gb300_count_live",
     "hvm_gb300_error",
@@ -135,6 +137,9 @@ def lib() -> ctypes.CDLL:
                                        ctypes.c_uint32]
     L.hvm_gb300_run_batch.argtypes = [ctypes.c_void_p, ctypes.POINTER(_Stats)]
     L.hvm_gb300_batch_roots.argtypes = [ctypes.c_void_p, u32p, ctypes.c_size_t]
+    L.hvm_gb300_run_stream.argtypes = [ctypes.c_void_p, ctypes.POINTER(ctypes.c_double), ctypes.c_uint32,
+                                       ctypes.c_double, ctypes.POINTER(ctypes.c_double), u32p,
+                                       ctypes.POINTER(_Stats)]
     L.hvm_gb300_batch_result.argtypes = [ctypes.c_void_p, ctypes.c_uint32, ctypes.c_char_p, ctypes.c_size_t,
                                          ctypes.POINTER(ctypes.c_size_t)]
     L.hvm_gb300_count_live.argtypes = [ctypes.c_void_p, ctypes.POINTER(ctypes.c_uint64)]
@@ -266,6 +271,20 @@ class Runtime:
         st = _Stats()
         self._check(lib().hvm_gb300_run_batch(self._h, ctypes.byref(st)))
         return self._stats(st)
+
+    def run_stream(self, arrival_s=None, max_inflight: int = 0, live_frac: float = 0.25):
+        """Continuous batching over the loaded batch; returns (stats, done_s, result_ports)."""
+        n = len(self._batch)
+        arr = np.zeros(n, dtype=np.float64) if arrival_s is None else np.ascontiguousarray(arrival_s, dtype=np.float64)
+        done = np.zeros(n, dtype=np.float64)
+        res = np.zeros(n, dtype=np.uint32)
+        st = _Stats()
+        self._check(lib().hvm_gb300_run_stream(self._h, arr.ctypes.data_as(ctypes.POINTER(ctypes.c_double)),
+                                               max_inflight, live_frac,
+                                               done.ctypes.data_as(ctypes.POINTER(ctypes.c_double)),
+                                               res.ctypes.data_as(ctypes.POINTER(ctypes.c_uint32)),
+                                               ctypes.byref(st)))
+        return self._stats(st), done, res
 
     def batch_roots(self) -> np.ndarray:
         out = np.zeros(len(self._batch), dtype=np.uint32)

@@ -44,6 +44,7 @@ struct DefHdr {
 // One record per completed turn, written by the turn's last block.
 struct TurnRecord {
   unsigned long long t_ns;          // %globaltimer when the turn closed
+  long long live_nodes;             // node words in use after the turn
   unsigned long long itrs;          // cumulative interactions
   unsigned long long pending;       // redexes in the ring for the next turn
   unsigned int dry, stopped;        // dry threads at close; 1 if ended by the dry rule
@@ -85,6 +86,7 @@ struct alignas(128) Ctl {
   // empty. Taken from [head, end) during a turn, returned at tail; `end`
   // moves to `tail` between turns (the redex ring's discipline).
   unsigned int nf_head, nf_tail, nf_end, vf_head, vf_tail, vf_end;
+  long long live_nodes, live_vars;  // words in use, summed at the end of each turn
   unsigned int npool_next;          // next page id of the node pool
   unsigned int vpool_next;          // next page id of the var pool
   TurnRecord* trace;                // per-turn records (null = off)
@@ -164,6 +166,7 @@ struct TState {
   Alloc na, va;               // node / var allocators
   unsigned long long base;    // ring index of this turn's first input (overflow check)
   unsigned long long itrs, leak, retries;
+  int live_nodes, live_vars;  // words taken minus words freed in this turn
   unsigned long long hist[8];
   bool dead;                  // set after a fatal status: stop interacting
 };
@@ -290,6 +293,7 @@ __device__ __forceinline__ uint32_t alloc_run(const Dev& d, TState& t, Alloc& a,
       for (uint32_t i = 0; i < n; i++) {
         if (VARS) vstore(d, at + i, NONE); else nstore(d, at + i, NODE_MARK);
       }
+      if (VARS) t.live_vars += n; else t.live_nodes += n;
       return at;
     }
     // Leaving a chunk that was entirely free and untouched keeps the page a
@@ -541,7 +545,7 @@ __device__ __forceinline__ void slot_result(const Dev& d, TState& t, Slot& s, ui
   const bool enter_step = !s.entered && get_tag(s.Y) == VAR;
   if (enter_step) {
     if (got == NONE || got == 0) s.entered = true;
-    else { vstore(d, addr, 0); s.Y = got; }
+    else { vstore(d, addr, 0); t.live_vars--; s.Y = got; }
   } else if (got == NONE) {
     s.busy = false;  // the other side will find Y here
   } else if (got == 0) {
@@ -549,6 +553,7 @@ __device__ __forceinline__ void slot_result(const Dev& d, TState& t, Slot& s, ui
   } else {
     // The other side had published `got` for X: take X and wire got ~ Y.
     vstore(d, addr, 0);
+    t.live_vars--;
     s.X = got;
     s.entered = false;
     if (get_tag(s.X) != VAR && get_tag(s.Y) == VAR) { Port z = s.X; s.X = s.Y; s.Y = z; }
@@ -582,6 +587,7 @@ __device__ __forceinline__ int lockstep_round(const Dev& d, TState& t, bool has,
   if (rc == IR_DONE && rule != IDLE_RULE) {
     if (needA) nstore(d, get_val(p.a), 0);
     if (needB) nstore(d, get_val(p.b), 0);
+    t.live_nodes -= (needA ? 1 : 0) + (needB ? 1 : 0);
     switch (rule) {
       case LINK: p.nlinks = 1; break;
       case VOID: p.nlinks = 0; break;
@@ -639,7 +645,10 @@ __device__ __forceinline__ int lockstep_round(const Dev& d, TState& t, bool has,
           p.nbase = (p.node_len && (p.vbase || !p.vars_len)) ? alloc_run<false>(d, t, t.na, p.node_len, soft) : 0;
           if ((p.vars_len && !p.vbase) || (p.node_len && !p.nbase)) {
             if (!d.tables) { rc = IR_FATAL; break; }
-            if (p.vbase) for (uint32_t i = 0; i < p.vars_len; i++) vstore(d, p.vbase + i, 0);  // give back
+            if (p.vbase) {  // give back
+              for (uint32_t i = 0; i < p.vars_len; i++) vstore(d, p.vbase + i, 0);
+              t.live_vars -= p.vars_len;
+            }
             p.contig = false;
           }
         }

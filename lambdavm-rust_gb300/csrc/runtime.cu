@@ -139,6 +139,7 @@ __global__ void __launch_bounds__(128, MIN_BLOCKS_128 > 0 ? MIN_BLOCKS_128 : 1) 
   alloc_load<true>(d.vspace, t.gid, t.va);
   t.base = base;
   t.itrs = t.leak = t.retries = 0;
+  t.live_nodes = t.live_vars = 0;
   for (int i = 0; i < 8; i++) t.hist[i] = 0;
   t.dead = false;
 
@@ -234,6 +235,16 @@ __global__ void __launch_bounds__(128, MIN_BLOCKS_128 > 0 ? MIN_BLOCKS_128 : 1) 
 
   // Counters: reduced per warp, then per block in shared memory, then one
   // global atomic per counter per block.
+  // Live-word deltas: one atomic per warp.
+  {
+    long long ln = t.live_nodes, lv = t.live_vars;
+    for (int o = 16; o > 0; o >>= 1) {
+      ln += __shfl_down_sync(0xFFFFFFFFu, ln, o);
+      lv += __shfl_down_sync(0xFFFFFFFFu, lv, o);
+    }
+    if (lane == 0 && ln) atomicAdd((unsigned long long*)&c->live_nodes, (unsigned long long)ln);
+    if (lane == 0 && lv) atomicAdd((unsigned long long*)&c->live_vars, (unsigned long long)lv);
+  }
   __shared__ unsigned long long blk_cnt[11];
   if (threadIdx.x < 11) blk_cnt[threadIdx.x] = 0;
   __syncthreads();
@@ -268,6 +279,7 @@ __global__ void __launch_bounds__(128, MIN_BLOCKS_128 > 0 ? MIN_BLOCKS_128 : 1) 
         asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(now));
         TurnRecord r;
         r.t_ns = now;
+        r.live_nodes = c->live_nodes;
         r.itrs = c->itrs;
         r.pending = pending;
         r.dry = c->dry;
@@ -357,6 +369,46 @@ __global__ void boot_batch_kernel(Dev d, const uint32_t* mains, uint32_t n, uint
     c->head = at + (take < n ? take : n);
     __threadfence();
   }
+}
+
+// Admits nets first .. first+k-1 of a loaded batch between two turns: each
+// one's `@main ~ ROOT_net` joins the next turn's input, and the turn
+// parameters are recomputed for the larger input.
+__global__ void admit_kernel(Dev d, const uint32_t* mains, uint32_t first, uint32_t k, uint32_t cap) {
+  Ctl* c = d.ctl;
+  const unsigned long long at = c->tail;
+  for (uint32_t i = threadIdx.x; i < k; i += blockDim.x) {
+    uint32_t net = first + i;
+    d.vars[(ROOT_VAR - net) & d.vars_mask] = NONE;
+    d.ring[(at + i) & d.ring_mask] = new_pair(new_port(REF, mains[net]), new_port(VAR, ROOT_VAR - net));
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    unsigned long long prev = c->pending;
+    c->tail = at + k;
+    c->in_end = at + k;
+    c->pending = c->in_end - c->base;
+    c->blocks_done = 0;
+    c->dry = 0;
+    c->stop = 0;
+    fixed_policy(c, c->pending, prev, d.nthreads, cap);
+    unsigned long long take = (unsigned long long)c->static_per_thread * d.nthreads;
+    c->head = c->base + (take < c->pending ? take : c->pending);
+    __threadfence();
+  }
+}
+
+// out[i] = net nets[i]'s ROOT with its var chain resolved (read-only).
+__global__ void active_roots_kernel(Dev d, const uint32_t* nets, Port* out, uint32_t n) {
+  uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  Port p = new_port(VAR, ROOT_VAR - nets[i]);
+  for (uint32_t g = 0; g < (1u << 20) && get_tag(p) == VAR; g++) {
+    Port v = __ldcg(&d.vars[get_val(p) & d.vars_mask]);
+    if (v == NONE || v == 0) break;
+    p = v;
+  }
+  out[i] = p;
 }
 
 // out[k] = net k's ROOT with its var chain resolved (read-only).
@@ -454,6 +506,8 @@ class Runtime {
   std::vector<Port> roots;             // each net's resolved ROOT after run_batch
   void* mem_roots = nullptr;
   uint32_t roots_cap = 0;
+  void* mem_mains = nullptr;
+  uint32_t mains_cap = 0;
   void* mem_node = nullptr; void* mem_vars = nullptr; void* mem_ring = nullptr;
   void* mem_cur = nullptr; void* mem_scratch = nullptr;
   void* mem_defs = nullptr; void* mem_book = nullptr; void* mem_trace = nullptr; void* mem_free = nullptr;
@@ -483,9 +537,10 @@ class Runtime {
 
   void release() {
     void* ps[] = {mem_node, mem_vars, mem_ring, mem_cur, mem_scratch, mem_defs, mem_book, g_out, g_kids, g_info, ctl,
-                  mem_trace, mem_roots, mem_free};
+                  mem_trace, mem_roots, mem_free, mem_mains};
     for (void* p : ps) if (p) cudaFree(p);
-    mem_node = mem_vars = mem_ring = mem_cur = mem_scratch = mem_defs = mem_book = mem_trace = mem_roots = mem_free = nullptr;
+    mem_node = mem_vars = mem_ring = mem_cur = mem_scratch = mem_defs = mem_book = mem_trace = mem_roots = mem_free =
+        mem_mains = nullptr;
     g_out = nullptr; g_kids = nullptr; g_info = nullptr; ctl = nullptr;
   }
 
@@ -895,6 +950,115 @@ class Runtime {
     return read_roots();
   }
 
+  // Continuous batching over a loaded batch: net k is admitted once the host
+  // clock passes arrival[k] (seconds from the start; non-decreasing), while
+  // fewer than `max_inflight` nets are in flight and live node and var words
+  // stay under `live_frac` of their spaces. Turns run in small batches; after
+  // each, the roots of in-flight nets are checked and a net whose ROOT has
+  // become a number is complete (done[k] = host seconds, result[k] = port).
+  // When every net is admitted and the ring is empty, the rest complete with
+  // whatever their ROOT holds, after the readback expansion.
+  int run_stream(const double* arrival, uint32_t max_inflight, double live_frac, double* done, Port* result) {
+    if (defs.empty() || net_main.size() != nroots) return fail("no batch loaded");
+    if (reset_net()) return -1;
+    d.extra_roots = nroots - 1;
+    if (!mem_mains || mains_cap < nroots) {
+      if (mem_mains) cudaFree(mem_mains);
+      mem_mains = nullptr;
+      CK(cudaMalloc(&mem_mains, 2ull * nroots * sizeof(uint32_t)));
+      mains_cap = nroots;
+    }
+    uint32_t* dm = (uint32_t*)mem_mains;
+    uint32_t* dact = dm + nroots;
+    CK(cudaMemcpy(dm, net_main.data(), nroots * sizeof(uint32_t), cudaMemcpyHostToDevice));
+    h2d_bytes += nroots * sizeof(uint32_t);
+    if (read_roots_alloc()) return -1;
+    const long long node_limit = (long long)(live_frac * (double)(1ull << cfg.node_log2));
+    const long long var_limit = (long long)(live_frac * (double)(1ull << cfg.vars_log2));
+    std::vector<uint32_t> active;
+    std::vector<Port> ports;
+    uint32_t next = 0;
+    Ctl h;
+    memset(&h, 0, sizeof(h));
+    auto t0 = std::chrono::steady_clock::now();
+    auto now_s = [&]() { return std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count(); };
+    uint64_t polls = 0;
+    for (;;) {
+      double now = now_s();
+      // Admission.
+      uint32_t k = 0;
+      while (next + k < nroots && arrival[next + k] <= now && active.size() + k < max_inflight &&
+             h.live_nodes < node_limit && h.live_vars < var_limit && k < 4096)
+        k++;
+      if (k) {
+        admit_kernel<<<1, 1024>>>(d, dm, next, k, cap);
+        CK(cudaGetLastError());
+        launches++;
+        for (uint32_t i = 0; i < k; i++) active.push_back(next + i);
+        next += k;
+      }
+      // A few turns, then the control block.
+      const uint32_t batch = 4;
+      for (uint32_t i = 0; i < batch; i++) turn_fn<<<grid, block, smem>>>(d, cap);
+      CK(cudaGetLastError());
+      turn_launches += batch;
+      launches += batch;
+      if (read_ctl(h)) return -1;
+      if (h.status) return fail(std::string("device error: ") + status_text(h.status));
+      // Completions.
+      if (!active.empty()) {
+        CK(cudaMemcpy(dact, active.data(), active.size() * sizeof(uint32_t), cudaMemcpyHostToDevice));
+        active_roots_kernel<<<((uint32_t)active.size() + 255) / 256, 256>>>(d, dact, (Port*)mem_roots,
+                                                                          (uint32_t)active.size());
+        CK(cudaGetLastError());
+        launches++;
+        ports.resize(active.size());
+        CK(cudaMemcpy(ports.data(), mem_roots, active.size() * sizeof(Port), cudaMemcpyDeviceToHost));
+        h2d_bytes += active.size() * sizeof(uint32_t);
+        d2h_bytes += active.size() * sizeof(Port);
+        double t = now_s();
+        size_t w = 0;
+        for (size_t i = 0; i < active.size(); i++) {
+          if (get_tag(ports[i]) == NUM) {
+            done[active[i]] = t;
+            result[active[i]] = ports[i];
+          } else {
+            active[w++] = active[i];
+          }
+        }
+        active.resize(w);
+      }
+      polls++;
+      const bool quiet = h.base == h.in_end;
+      if (quiet && next == nroots) break;
+      if (quiet && active.empty() && next < nroots && arrival[next] > now_s()) {
+        // Idle until the next arrival.
+        while (arrival[next] > now_s()) {}
+      }
+      if (cfg.max_turns && turn_launches >= cfg.max_turns) return fail("turn budget exhausted before normal form");
+    }
+    // Quiescent: nets whose ROOT is not a number finish with the readback walk.
+    for (uint32_t net : active) {
+      Port root = new_port(VAR, ROOT_VAR - net);
+      Ctr c;
+      if (read_ctr(peek(root), c, root)) return -1;
+      done[net] = now_s();
+      result[net] = peek(root);
+    }
+    norm_calls++;
+    return 0;
+  }
+
+  int read_roots_alloc() {
+    if (!mem_roots || roots_cap < nroots) {
+      if (mem_roots) cudaFree(mem_roots);
+      mem_roots = nullptr;
+      CK(cudaMalloc(&mem_roots, nroots * sizeof(Port)));
+      roots_cap = nroots;
+    }
+    return 0;
+  }
+
   int read_roots() {
     if (!mem_roots || roots_cap < nroots) {
       if (mem_roots) cudaFree(mem_roots);
@@ -1104,6 +1268,20 @@ extern "C" int hvm_gb300_run_batch(hvm_gb300_runtime* r, hvm_gb300_stats* stats)
   if (!r) return -1;
   r->rt.err.clear();
   if (r->rt.run_batch()) return -1;
+  if (stats && r->rt.stats(stats)) return -1;
+  return 0;
+}
+
+extern "C" int hvm_gb300_run_stream(hvm_gb300_runtime* r, const double* arrival_s, uint32_t max_inflight,
+                                    double live_frac, double* done_s, uint32_t* result_ports,
+                                    hvm_gb300_stats* stats) {
+  if (!r || !arrival_s || !done_s || !result_ports) return -1;
+  r->rt.err.clear();
+  auto t0 = std::chrono::steady_clock::now();
+  if (r->rt.run_stream(arrival_s, max_inflight ? max_inflight : 0xFFFFFFFFu, live_frac > 0 ? live_frac : 1.0, done_s,
+                       result_ports))
+    return -1;
+  r->rt.norm_seconds += std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
   if (stats && r->rt.stats(stats)) return -1;
   return 0;
 }

@@ -54,11 +54,42 @@ def test_batch_of_reference_programs(hvm, ref_programs):
             assert hvm.canonical(rt.batch_result(k)) == hvm.canonical(p["result"]), p["name"]
 
 
+def test_stream_prefix_matches_goldens(hvm, workloads, batch_golden):
+    # Continuous batching: at most 16 nets in flight, the rest admitted as
+    # others complete; every result and the total count still match.
+    n = 96
+    nets = workloads.mixed_batch(4096)[:n]
+    gold = batch_golden["nets"][:n]
+    with hvm.Runtime(device=0) as rt:
+        rt.load_batch([code for code, _ in nets])
+        st, done, res = rt.run_stream(max_inflight=16)
+        assert st.itrs == sum(g["itrs"] for g in gold)
+        check_roots(res, gold)
+        assert (done > 0).all()
+
+
+def test_stream_alone_and_in_the_mix(hvm, workloads, batch_golden):
+    # A net's result is the same alone and admitted among others while they run.
+    nets = workloads.mixed_batch(4096)[:24]
+    gold = batch_golden["nets"][:24]
+    with hvm.Runtime(device=0) as rt:
+        for k in (1, 2, 4):
+            rt.load(nets[k][0])
+            st = rt.run()
+            assert st.itrs == gold[k]["itrs"]
+            assert hvm.canonical(rt.result()) == hvm.canonical(gold[k]["result"])
+        rt.load_batch([code for code, _ in nets])
+        arrivals = [0.0] * 8 + [0.002 * i for i in range(16)]  # late arrivals join running nets
+        st, done, res = rt.run_stream(arrival_s=arrivals, max_inflight=12)
+        check_roots(res, gold)
+        assert st.itrs == sum(g["itrs"] for g in gold)
+
+
 @pytest.mark.slow
 def test_batch_4096(hvm, workloads, batch_golden):
     nets = workloads.mixed_batch(4096)
     with hvm.Runtime(device=0) as rt:
         rt.load_batch([code for code, _ in nets])
-        st = rt.run_batch()
+        st, done, res = rt.run_stream(max_inflight=1536, live_frac=0.25)
         assert st.itrs == batch_golden["total_itrs"]
-        check_roots(rt.batch_roots(), batch_golden["nets"])
+        check_roots(res, batch_golden["nets"])
