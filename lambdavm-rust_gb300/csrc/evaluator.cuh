@@ -684,8 +684,11 @@ __device__ __forceinline__ int lockstep_round(const Dev& d, TState& t, bool has,
 
   long long c2 = 0, c3 = 0;
   if (wp) { __syncwarp(); c2 = clock64(); }
-  // 5. one fence for the warp if any lane created words
-  if (__any_sync(0xFFFFFFFFu, made)) __threadfence();
+  // 5. Fresh words only need to be visible to other threads before the first
+  //    exchange that could publish them; pairs wired without an exchange
+  //    (redexes pushed to the lane's own deque) need no fence. So the fence
+  //    is taken once, lazily, before the first exchange step below.
+  bool fence_due = __any_sync(0xFFFFFFFFu, made);
   if (wp) c3 = clock64();
   uint32_t steps = 0;
 
@@ -699,6 +702,7 @@ __device__ __forceinline__ int lockstep_round(const Dev& d, TState& t, bool has,
     slot_fill(d, t, p, next, s0);
     slot_fill(d, t, p, next, s1);
     if (!__any_sync(0xFFFFFFFFu, s0.busy || s1.busy)) break;
+    if (fence_due) { __threadfence(); fence_due = false; }
     steps++;
     uint32_t a0, a1;
     Port q0, q1;

@@ -163,6 +163,8 @@ __global__ void __launch_bounds__(128, MIN_BLOCKS_128 > 0 ? MIN_BLOCKS_128 : 1) 
     unsigned want = __ballot_sync(0xFFFFFFFFu, t.len == 0);
     unsigned give = __ballot_sync(0xFFFFFFFFu, t.len >= 2);
     if (want && give) {
+      // Redexes created without a fence become visible to the taker first.
+      __threadfence();
       unsigned m = min(__popc(want), __popc(give));
       unsigned rw = __popc(want & lt_mask), rg = __popc(give & lt_mask);
       bool recv = ((want >> lane) & 1) && rw < m;
@@ -1339,6 +1341,7 @@ extern "C" int hvm_gb300_trace(hvm_gb300_runtime* r, hvm_gb300_turn* out, size_t
     return r->rt.fail("trace copy failed");
   for (size_t i = 0; i < k; i++) {
     out[i].t_ns = tmp[i].t_ns;
+    out[i].live_nodes = tmp[i].live_nodes;
     out[i].itrs = tmp[i].itrs;
     out[i].pending = tmp[i].pending;
     out[i].dry = tmp[i].dry;
