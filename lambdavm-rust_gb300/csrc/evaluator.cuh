@@ -167,6 +167,7 @@ struct TState {
   unsigned long long base;    // ring index of this turn's first input (overflow check)
   unsigned long long itrs, leak, retries;
   int live_nodes, live_vars;  // words taken minus words freed in this turn
+  bool dirty;                 // wrote fresh words not yet ordered by a fence
   unsigned long long hist[8];
   bool dead;                  // set after a fatal status: stop interacting
 };
@@ -235,6 +236,7 @@ __device__ __forceinline__ void ld_cg_v4(const void* p, unsigned long long& a, u
 constexpr uint32_t CHUNK = 32;  // words per scanned chunk (256 B of nodes, 128 B of vars)
 constexpr uint32_t MAX_DRY_PAGES = 4;  // full cycles over a lane's pages before out-of-memory
 constexpr uint32_t SOFT_RUN_CHUNKS = 32;  // chunks a CALL scans for a contiguous run before taking single words
+constexpr uint32_t SOFT_GRAB_PAGES = 8;   // a contiguous-run request may take pages up to this many owned
 
 // Bit i of the result is set when word base+i is free and may be handed out.
 template <bool VARS>
@@ -319,9 +321,9 @@ __device__ __forceinline__ uint32_t alloc_run(const Dev& d, TState& t, Alloc& a,
         moved = true;  // scan the page that took its place
       }
       bool grabbed = moved;
-      // Only a hard request takes a fresh page: a soft one (a contiguous run)
-      // gives up instead, so pages are not taken for fragmentation alone.
-      if (!moved && !soft_limit && (a.dry_chunks >= 2 * chunks_per_page || (a.count == 1 && a.dry_chunks >= chunks_per_page)) &&
+      // A soft request (a contiguous run) takes a page only while the lane
+      // owns few, so pages are not hoarded for fragmentation alone.
+      if (!moved && (!soft_limit || a.count < SOFT_GRAB_PAGES) && (a.dry_chunks >= 2 * chunks_per_page || (a.count == 1 && a.dry_chunks >= chunks_per_page)) &&
           a.count < sp.max_pages && !a.pool_dry) {
         uint32_t fresh = 0xFFFFFFFFu;
         if (ring) {  // a returned page first
@@ -688,7 +690,8 @@ __device__ __forceinline__ int lockstep_round(const Dev& d, TState& t, bool has,
   //    exchange that could publish them; pairs wired without an exchange
   //    (redexes pushed to the lane's own deque) need no fence. So the fence
   //    is taken once, lazily, before the first exchange step below.
-  bool fence_due = __any_sync(0xFFFFFFFFu, made);
+  if (made) t.dirty = true;
+  bool fence_due = __any_sync(0xFFFFFFFFu, t.dirty);
   if (wp) c3 = clock64();
   uint32_t steps = 0;
 
@@ -702,7 +705,7 @@ __device__ __forceinline__ int lockstep_round(const Dev& d, TState& t, bool has,
     slot_fill(d, t, p, next, s0);
     slot_fill(d, t, p, next, s1);
     if (!__any_sync(0xFFFFFFFFu, s0.busy || s1.busy)) break;
-    if (fence_due) { __threadfence(); fence_due = false; }
+    if (fence_due) { __threadfence(); fence_due = false; t.dirty = false; }
     steps++;
     uint32_t a0, a1;
     Port q0, q1;

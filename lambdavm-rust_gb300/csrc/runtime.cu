@@ -140,6 +140,7 @@ __global__ void __launch_bounds__(128, MIN_BLOCKS_128 > 0 ? MIN_BLOCKS_128 : 1) 
   t.base = base;
   t.itrs = t.leak = t.retries = 0;
   t.live_nodes = t.live_vars = 0;
+  t.dirty = false;
   for (int i = 0; i < 8; i++) t.hist[i] = 0;
   t.dead = false;
 
@@ -163,8 +164,9 @@ __global__ void __launch_bounds__(128, MIN_BLOCKS_128 > 0 ? MIN_BLOCKS_128 : 1) 
     unsigned want = __ballot_sync(0xFFFFFFFFu, t.len == 0);
     unsigned give = __ballot_sync(0xFFFFFFFFu, t.len >= 2);
     if (want && give) {
-      // Redexes created without a fence become visible to the taker first.
-      __threadfence();
+      // A giving lane whose fresh words are not yet fenced publishes them
+      // before another lane can take a redex that points at them.
+      if (__any_sync(0xFFFFFFFFu, ((give >> lane) & 1) && t.dirty)) { __threadfence(); t.dirty = false; }
       unsigned m = min(__popc(want), __popc(give));
       unsigned rw = __popc(want & lt_mask), rg = __popc(give & lt_mask);
       bool recv = ((want >> lane) & 1) && rw < m;
