@@ -134,12 +134,13 @@ int hvm_gb300_batch_roots(hvm_gb300_runtime* rt, uint32_t* out, size_t cap);
  * `arrival_s[k]` seconds have passed (non-decreasing), while fewer than
  * `max_inflight` nets are in flight (0 = no cap) and live node and var words
  * stay under `live_frac` of their spaces; admitted nets share the turns with
- * the nets already running. A net completes when its ROOT becomes a number
+ * the nets already running. `order` 0 admits arrived nets first come, first
+ * served; 1 admits the smallest book first. A net completes when its ROOT becomes a number
  * (`done_s[k]` = seconds since the start, `result_ports[k]` = that port);
  * nets with other normal forms complete when the batch is quiescent. The
  * stats' itrs is the total over all nets. */
 int hvm_gb300_run_stream(hvm_gb300_runtime* rt, const double* arrival_s, uint32_t max_inflight, double live_frac,
-                         double* done_s, uint32_t* result_ports, hvm_gb300_stats* stats);
+                         uint32_t order, double* done_s, uint32_t* result_ports, hvm_gb300_stats* stats);
 int hvm_gb300_batch_result(hvm_gb300_runtime* rt, uint32_t net, char* out, size_t cap, size_t* len);
 
 /* Diagnostic counterpart of the reference's count_memory kernel

@@ -138,7 +138,7 @@ def lib() -> ctypes.CDLL:
     L.hvm_gb300_run_batch.argtypes = [ctypes.c_void_p, ctypes.POINTER(_Stats)]
     L.hvm_gb300_batch_roots.argtypes = [ctypes.c_void_p, u32p, ctypes.c_size_t]
     L.hvm_gb300_run_stream.argtypes = [ctypes.c_void_p, ctypes.POINTER(ctypes.c_double), ctypes.c_uint32,
-                                       ctypes.c_double, ctypes.POINTER(ctypes.c_double), u32p,
+                                       ctypes.c_double, ctypes.c_uint32, ctypes.POINTER(ctypes.c_double), u32p,
                                        ctypes.POINTER(_Stats)]
     L.hvm_gb300_batch_result.argtypes = [ctypes.c_void_p, ctypes.c_uint32, ctypes.c_char_p, ctypes.c_size_t,
                                          ctypes.POINTER(ctypes.c_size_t)]
@@ -272,7 +272,7 @@ class Runtime:
         self._check(lib().hvm_gb300_run_batch(self._h, ctypes.byref(st)))
         return self._stats(st)
 
-    def run_stream(self, arrival_s=None, max_inflight: int = 0, live_frac: float = 0.25):
+    def run_stream(self, arrival_s=None, max_inflight: int = 0, live_frac: float = 0.25, order: int = 0):
         """Continuous batching over the loaded batch; returns (stats, done_s, result_ports)."""
         n = len(self._batch)
         arr = np.zeros(n, dtype=np.float64) if arrival_s is None else np.ascontiguousarray(arrival_s, dtype=np.float64)
@@ -280,7 +280,7 @@ class Runtime:
         res = np.zeros(n, dtype=np.uint32)
         st = _Stats()
         self._check(lib().hvm_gb300_run_stream(self._h, arr.ctypes.data_as(ctypes.POINTER(ctypes.c_double)),
-                                               max_inflight, live_frac,
+                                               max_inflight, live_frac, order,
                                                done.ctypes.data_as(ctypes.POINTER(ctypes.c_double)),
                                                res.ctypes.data_as(ctypes.POINTER(ctypes.c_uint32)),
                                                ctypes.byref(st)))

@@ -20,6 +20,7 @@
 //     single-word reads, and the final tree is serialised by one gather
 //     kernel instead of a device printf (src/hvm.cu:2290-2297).
 #include <cuda_runtime.h>
+#include <algorithm>
 #include <chrono>
 #include <cstdio>
 #include <cstdlib>
@@ -86,8 +87,11 @@ __device__ void fixed_policy(Ctl* c, unsigned long long pending, unsigned long l
   if (pending < nthreads) {
     s = 1;
     chunk = 1;
+    // Sequential or slowly growing work keeps doubling the budget; a jump in
+    // the number of redexes (fresh parallelism) starts short turns again.
     uint32_t prev = c->budget;
-    budget = (pending <= prev_pending && prev >= 64) ? (prev < (1u << 16) ? prev * 2 : prev) : 64;
+    bool jump = pending > 2 * prev_pending + 64;
+    budget = (!jump && prev >= 64) ? (prev < (1u << 16) ? prev * 2 : prev) : 64;
   } else {
     unsigned long long per = pending / nthreads;
     s = (uint32_t)(per < cap / 2 ? per : cap / 2);
@@ -375,14 +379,14 @@ __global__ void boot_batch_kernel(Dev d, const uint32_t* mains, uint32_t n, uint
   }
 }
 
-// Admits nets first .. first+k-1 of a loaded batch between two turns: each
+// Admits nets nets[0..k) of a loaded batch between two turns: each
 // one's `@main ~ ROOT_net` joins the next turn's input, and the turn
 // parameters are recomputed for the larger input.
-__global__ void admit_kernel(Dev d, const uint32_t* mains, uint32_t first, uint32_t k, uint32_t cap) {
+__global__ void admit_kernel(Dev d, const uint32_t* mains, const uint32_t* nets, uint32_t k, uint32_t cap) {
   Ctl* c = d.ctl;
   const unsigned long long at = c->tail;
   for (uint32_t i = threadIdx.x; i < k; i += blockDim.x) {
-    uint32_t net = first + i;
+    uint32_t net = nets[i];
     d.vars[(ROOT_VAR - net) & d.vars_mask] = NONE;
     d.ring[(at + i) & d.ring_mask] = new_pair(new_port(REF, mains[net]), new_port(VAR, ROOT_VAR - net));
   }
@@ -962,18 +966,20 @@ class Runtime {
   // become a number is complete (done[k] = host seconds, result[k] = port).
   // When every net is admitted and the ring is empty, the rest complete with
   // whatever their ROOT holds, after the readback expansion.
-  int run_stream(const double* arrival, uint32_t max_inflight, double live_frac, double* done, Port* result) {
+  int run_stream(const double* arrival, uint32_t max_inflight, double live_frac, double* done, Port* result,
+                 uint32_t order = 0) {
     if (defs.empty() || net_main.size() != nroots) return fail("no batch loaded");
     if (reset_net()) return -1;
     d.extra_roots = nroots - 1;
     if (!mem_mains || mains_cap < nroots) {
       if (mem_mains) cudaFree(mem_mains);
       mem_mains = nullptr;
-      CK(cudaMalloc(&mem_mains, 2ull * nroots * sizeof(uint32_t)));
+      CK(cudaMalloc(&mem_mains, 3ull * nroots * sizeof(uint32_t)));
       mains_cap = nroots;
     }
     uint32_t* dm = (uint32_t*)mem_mains;
-    uint32_t* dact = dm + nroots;
+    uint32_t* dact = dm + nroots;        // nets being admitted
+    uint32_t* dlive = dm + 2ull * nroots;  // nets in flight
     CK(cudaMemcpy(dm, net_main.data(), nroots * sizeof(uint32_t), cudaMemcpyHostToDevice));
     h2d_bytes += nroots * sizeof(uint32_t);
     if (read_roots_alloc()) return -1;
@@ -981,7 +987,25 @@ class Runtime {
     const long long var_limit = (long long)(live_frac * (double)(1ull << cfg.vars_log2));
     std::vector<uint32_t> active;
     std::vector<Port> ports;
-    uint32_t next = 0;
+    uint32_t next = 0;         // nets [0, next) have arrived and been queued
+    // Arrived nets wait in `ready`; order 0 admits them first come, first
+    // served; order 1 admits the smallest book first (among those arrived),
+    // which starts the light, often long-running nets early in a batch.
+    std::vector<uint32_t> ready;
+    size_t ready_head = 0;
+    uint32_t admitted_total = 0;
+    auto book_words = [&](uint32_t net) -> uint64_t {
+      uint32_t lo = net_main[net], hi = net + 1 < nroots ? net_main[net + 1] : (uint32_t)defs.size();
+      uint64_t w = 0;
+      for (uint32_t f = lo; f < hi; f++) w += defs[f].node_len + defs[f].rbag_len;
+      return w;
+    };
+    std::vector<uint64_t> weight;
+    if (order == 1) {
+      weight.resize(nroots);
+      for (uint32_t k = 0; k < nroots; k++) weight[k] = book_words(k);
+    }
+    std::vector<uint32_t> admit;
     Ctl h;
     memset(&h, 0, sizeof(h));
     auto t0 = std::chrono::steady_clock::now();
@@ -989,17 +1013,25 @@ class Runtime {
     uint64_t polls = 0;
     for (;;) {
       double now = now_s();
-      // Admission.
-      uint32_t k = 0;
-      while (next + k < nroots && arrival[next + k] <= now && active.size() + k < max_inflight &&
-             h.live_nodes < node_limit && h.live_vars < var_limit && k < 4096)
-        k++;
-      if (k) {
-        admit_kernel<<<1, 1024>>>(d, dm, next, k, cap);
+      // Arrivals join the ready queue; admission takes from it.
+      size_t before = ready.size();
+      while (next < nroots && arrival[next] <= now) ready.push_back(next++);
+      if (order == 1 && ready.size() > before) {
+        std::stable_sort(ready.begin() + ready_head, ready.end(),
+                         [&](uint32_t x, uint32_t y) { return weight[x] < weight[y]; });
+      }
+      admit.clear();
+      while (ready_head < ready.size() && active.size() + admit.size() < max_inflight &&
+             h.live_nodes < node_limit && h.live_vars < var_limit && admit.size() < 4096)
+        admit.push_back(ready[ready_head++]);
+      if (!admit.empty()) {
+        CK(cudaMemcpy(dact, admit.data(), admit.size() * sizeof(uint32_t), cudaMemcpyHostToDevice));
+        h2d_bytes += admit.size() * sizeof(uint32_t);
+        admit_kernel<<<1, 1024>>>(d, dm, dact, (uint32_t)admit.size(), cap);
         CK(cudaGetLastError());
         launches++;
-        for (uint32_t i = 0; i < k; i++) active.push_back(next + i);
-        next += k;
+        for (uint32_t net : admit) active.push_back(net);
+        admitted_total += (uint32_t)admit.size();
       }
       // A few turns, then the control block.
       const uint32_t batch = 4;
@@ -1011,8 +1043,8 @@ class Runtime {
       if (h.status) return fail(std::string("device error: ") + status_text(h.status));
       // Completions.
       if (!active.empty()) {
-        CK(cudaMemcpy(dact, active.data(), active.size() * sizeof(uint32_t), cudaMemcpyHostToDevice));
-        active_roots_kernel<<<((uint32_t)active.size() + 255) / 256, 256>>>(d, dact, (Port*)mem_roots,
+        CK(cudaMemcpy(dlive, active.data(), active.size() * sizeof(uint32_t), cudaMemcpyHostToDevice));
+        active_roots_kernel<<<((uint32_t)active.size() + 255) / 256, 256>>>(d, dlive, (Port*)mem_roots,
                                                                           (uint32_t)active.size());
         CK(cudaGetLastError());
         launches++;
@@ -1034,8 +1066,8 @@ class Runtime {
       }
       polls++;
       const bool quiet = h.base == h.in_end;
-      if (quiet && next == nroots) break;
-      if (quiet && active.empty() && next < nroots && arrival[next] > now_s()) {
+      if (quiet && admitted_total == nroots) break;
+      if (quiet && active.empty() && ready_head == ready.size() && next < nroots && arrival[next] > now_s()) {
         // Idle until the next arrival.
         while (arrival[next] > now_s()) {}
       }
@@ -1277,13 +1309,13 @@ extern "C" int hvm_gb300_run_batch(hvm_gb300_runtime* r, hvm_gb300_stats* stats)
 }
 
 extern "C" int hvm_gb300_run_stream(hvm_gb300_runtime* r, const double* arrival_s, uint32_t max_inflight,
-                                    double live_frac, double* done_s, uint32_t* result_ports,
+                                    double live_frac, uint32_t order, double* done_s, uint32_t* result_ports,
                                     hvm_gb300_stats* stats) {
   if (!r || !arrival_s || !done_s || !result_ports) return -1;
   r->rt.err.clear();
   auto t0 = std::chrono::steady_clock::now();
   if (r->rt.run_stream(arrival_s, max_inflight ? max_inflight : 0xFFFFFFFFu, live_frac > 0 ? live_frac : 1.0, done_s,
-                       result_ports))
+                       result_ports, order))
     return -1;
   r->rt.norm_seconds += std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
   if (stats && r->rt.stats(stats)) return -1;
