@@ -42,6 +42,8 @@ PEAKS = os.path.join(ROOT, "MEASURED_PEAKS.json")
 TRAFFIC = os.path.join(ROOT, "profiles", "turn_kernel_bitonic_2p14.md")
 ORACLE = os.path.join(ROOT, "oracle", "_build", "hvm_oracle")
 
+BATCH_GOLDEN = os.path.join(ROOT, "tests", "golden", "batch_mixed_4096.json")
+
 WORKLOADS = {
     # name: (golden key, generator, description)
     "bitonic_sort_2p16": ("bitonic_sort_2p16", lambda W: W.bitonic_sort(16),
@@ -49,7 +51,88 @@ WORKLOADS = {
     "tree_sum_d20": ("tree_sum_d20", lambda W: W.tree_sum(20), "recursive tree sum d=20, single net"),
     "skewed_fold_2p18": ("skewed_fold_2p18", lambda W: W.skewed_fold(18),
                          "fold over 2^18 geometric-length countdowns, single net"),
+    "batch_mixed_4096": (None, None, "4096 independent nets (1/3 tree sums d 8..18, 1/3 bitonic sorts of 2^6..2^12 "
+                                     "keys then summed, 1/3 countdowns 10..1e5), continuous batching"),
+    "serving": (None, None, "Poisson arrivals of nets drawn from the 4096-net mixed pool, continuous batching"),
 }
+
+# Continuous-batching settings for the mixed batch (admission cap and live-memory
+# limit keep the concurrent nets' memory within the 2^29-word spaces).
+BATCH_INFLIGHT = 512
+BATCH_LIVE_FRAC = 0.25
+
+
+def numb_u24(port: int) -> int | None:
+    return ((int(port) >> 3) >> 5) if int(port) & 7 == 3 else None
+
+
+def batch_check(res, gold_nets) -> bool:
+    return all(numb_u24(p) == int(g["result"]) for p, g in zip(res, gold_nets))
+
+
+def bench_batch(hvm, W, args, plain_sample: int = 128) -> dict:
+    """Config 4: the 4096-net mixed batch through continuous batching, and the
+    plain path (one net per evaluation) on an evenly spaced sample of it."""
+    gold = json.load(open(BATCH_GOLDEN))
+    nets = W.mixed_batch(gold["count"])
+    books = [hvm.book_from_text(code) for code, _ in nets]
+    rt = hvm.Runtime(device=0)
+    rt.load_batch(books)
+    for _ in range(max(1, args.warmup // 3)):
+        st, done, res = rt.run_stream(max_inflight=BATCH_INFLIGHT, live_frac=BATCH_LIVE_FRAC)
+    secs, ok = [], True
+    for _ in range(max(1, args.steps // 10)):
+        t0 = time.perf_counter()
+        st, done, res = rt.run_stream(max_inflight=BATCH_INFLIGHT, live_frac=BATCH_LIVE_FRAC)
+        secs.append(time.perf_counter() - t0)
+        ok = ok and st.itrs == gold["total_itrs"] and batch_check(res, gold["nets"])
+    batched = gold["total_itrs"] / statistics.median(secs)
+    # plain: nets one at a time through the single-net path
+    step = max(1, len(books) // plain_sample)
+    t0 = time.perf_counter()
+    p_itrs = 0
+    for k in range(0, len(books), step):
+        rt.load(books[k])
+        s = rt.run()
+        p_itrs += s.itrs
+        ok = ok and s.itrs == gold["nets"][k]["itrs"]
+    plain = p_itrs / (time.perf_counter() - t0)
+    rt.close()
+    return {"nets": gold["count"], "itrs": gold["total_itrs"], "value": batched, "unit": UNIT,
+            "seconds": statistics.median(secs), "p50_done_s": float(sorted(done)[len(done) // 2]),
+            "max_done_s": float(done.max()), "max_inflight": BATCH_INFLIGHT, "live_frac": BATCH_LIVE_FRAC,
+            "plain_kernel": {"value": plain, "sample_nets": len(range(0, len(books), step)),
+                             "note": "same nets, one per evaluation (single-net path)"},
+            "batched_over_plain": batched / plain, "parity": bool(ok), "policy": "fixed"}
+
+
+def bench_serving(hvm, W, rates=(1e2, 1e3, 1e4, 1e5), seconds: float = 2.0, max_requests: int = 100_000) -> dict:
+    """Config 5: Poisson arrivals at each rate for about `seconds` of arrivals
+    (at most `max_requests`), nets drawn from the 4096-net pool; latency =
+    completion - arrival on the host clock; every response checked against
+    the reference's result for its net."""
+    gold = json.load(open(BATCH_GOLDEN))
+    nets = W.mixed_batch(gold["count"])
+    books = [hvm.book_from_text(code) for code, _ in nets]
+    rt = hvm.Runtime(device=0)
+    out = []
+    for rate in rates:
+        n = int(min(max_requests, max(50, rate * seconds)))
+        arrivals, tmpl = W.serving_requests(n, rate)
+        rt.load_batch(books)
+        rt.set_requests(tmpl)
+        t0 = time.perf_counter()
+        st, done, res = rt.run_stream(arrival_s=arrivals, max_inflight=BATCH_INFLIGHT, live_frac=BATCH_LIVE_FRAC)
+        wall = time.perf_counter() - t0
+        lat = sorted(float(d - a) for d, a in zip(done, arrivals))
+        ok = all(numb_u24(p) == int(gold["nets"][t]["result"]) for p, t in zip(res, tmpl))
+        itrs_expected = sum(gold["nets"][t]["itrs"] for t in tmpl)
+        out.append({"rate_per_s": rate, "requests": n, "wall_s": wall, "itrs": st.itrs,
+                    "itrs_per_s": st.itrs / wall, "p50_latency_s": lat[len(lat) // 2],
+                    "p99_latency_s": lat[min(len(lat) - 1, int(len(lat) * 0.99))],
+                    "parity": bool(ok and st.itrs == itrs_expected)})
+    rt.close()
+    return {"rates": out}
 
 
 def dist_env():
@@ -328,11 +411,33 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["gb300", "reference"], default="gb300")
     ap.add_argument("--workload", choices=sorted(WORKLOADS), default="bitonic_sort_2p16")
+    ap.add_argument("--no-batch", action="store_true", help="skip the 4096-net batch report of the default line")
     args = ap.parse_args()
     ws, rank, local = dist_env()
     hvm = ensure_built()
     W = importlib.import_module("lambdavm-rust_gb300.workloads")
     key, make, desc = WORKLOADS[args.workload]
+    if args.workload in ("batch_mixed_4096", "serving"):
+        if args.impl == "reference" or rank != 0:
+            if rank == 0:
+                print(json.dumps({"impl": "reference", "unavailable": "the CPU arm runs the single-net workloads"}))
+            return
+        import torch
+        torch.cuda.set_device(local)
+        if args.workload == "batch_mixed_4096":
+            b = bench_batch(hvm, W, args)
+            line = {"metric": METRIC, "value": b["value"], "unit": UNIT, "n_gpus": 1, "steps": max(1, args.steps // 10),
+                    "warmup": max(1, args.warmup // 3), "ms_per_step": b["seconds"] * 1e3, "higher_is_better": True,
+                    "scaling": "weak", "vs_baseline": None, "dtype": "u32", "data": "synthetic",
+                    "config": {"workload": desc, **{k: v for k, v in b.items() if k not in ("value", "unit")}}}
+        else:
+            sv = bench_serving(hvm, W)
+            best = max(r["itrs_per_s"] for r in sv["rates"])
+            line = {"metric": METRIC, "value": best, "unit": UNIT, "n_gpus": 1, "steps": 1, "warmup": 0,
+                    "ms_per_step": None, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+                    "dtype": "u32", "data": "synthetic", "config": {"workload": desc, **sv}}
+        print(json.dumps(line), flush=True)
+        return
     golden = json.load(open(GOLDEN))[key]
     book = hvm.book_from_text(make(W))
     if args.impl == "reference":
@@ -343,6 +448,8 @@ def main():
     dist = Dist(ws, rank, local, use_cuda=True)
     try:
         line = bench_gpu(args, hvm, book, golden, desc, ws, rank, local, dist)
+        if line is not None and not args.no_batch:
+            line["batched"] = bench_batch(hvm, W, args)
     finally:
         dist.close()
     if line:

@@ -130,6 +130,12 @@ int hvm_gb300_load_batch(hvm_gb300_runtime* rt, const uint32_t* const* books, co
 int hvm_gb300_run_batch(hvm_gb300_runtime* rt, hvm_gb300_stats* stats);
 int hvm_gb300_batch_roots(hvm_gb300_runtime* rt, uint32_t* out, size_t cap);
 
+/* Turns the loaded batch into request templates: afterwards the batch has
+ * `n` nets, net r being a fresh copy of loaded net templates[r] (sharing its
+ * definitions, with its own ROOT). Used to serve many requests of a few
+ * programs without loading a book per request. */
+int hvm_gb300_set_requests(hvm_gb300_runtime* rt, const uint32_t* templates, uint32_t n);
+
 /* Continuous batching over a loaded batch (serving): net k is admitted once
  * `arrival_s[k]` seconds have passed (non-decreasing), while fewer than
  * `max_inflight` nets are in flight (0 = no cap) and live node and var words

@@ -98,6 +98,7 @@ EXPORTED_SYMBOLS = (
     "hvm_gb300_run_batch",
     "hvm_gb300_batch_roots",
     "hvm_gb300_run_stream",
+    "hvm_gb300_set_requests",
     "hvm_gb300_batch_result",
     "hvm_gb300_count_live",
     "hvm_gb300_error",
@@ -137,6 +138,7 @@ def lib() -> ctypes.CDLL:
                                        ctypes.c_uint32]
     L.hvm_gb300_run_batch.argtypes = [ctypes.c_void_p, ctypes.POINTER(_Stats)]
     L.hvm_gb300_batch_roots.argtypes = [ctypes.c_void_p, u32p, ctypes.c_size_t]
+    L.hvm_gb300_set_requests.argtypes = [ctypes.c_void_p, u32p, ctypes.c_uint32]
     L.hvm_gb300_run_stream.argtypes = [ctypes.c_void_p, ctypes.POINTER(ctypes.c_double), ctypes.c_uint32,
                                        ctypes.c_double, ctypes.c_uint32, ctypes.POINTER(ctypes.c_double), u32p,
                                        ctypes.POINTER(_Stats)]
@@ -271,6 +273,12 @@ class Runtime:
         st = _Stats()
         self._check(lib().hvm_gb300_run_batch(self._h, ctypes.byref(st)))
         return self._stats(st)
+
+    def set_requests(self, templates) -> None:
+        """Makes request r a copy of loaded net templates[r] (serving)."""
+        t = np.ascontiguousarray(templates, dtype=np.uint32)
+        self._check(lib().hvm_gb300_set_requests(self._h, t.ctypes.data_as(ctypes.POINTER(ctypes.c_uint32)), t.size))
+        self._batch = [None] * t.size
 
     def run_stream(self, arrival_s=None, max_inflight: int = 0, live_frac: float = 0.25, order: int = 0):
         """Continuous batching over the loaded batch; returns (stats, done_s, result_ports)."""

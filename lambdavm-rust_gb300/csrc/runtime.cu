@@ -511,6 +511,7 @@ class Runtime {
   Ctl* ctl = nullptr;
   uint32_t nroots = 1;                 // nets in the loaded batch (1 for a single book)
   std::vector<uint32_t> net_main;      // fid of each net's @main
+  std::vector<uint32_t> template_main; // the loaded nets' mains, once requests refer to them
   std::vector<Port> roots;             // each net's resolved ROOT after run_batch
   void* mem_roots = nullptr;
   uint32_t roots_cap = 0;
@@ -698,7 +699,25 @@ class Runtime {
     defs = std::move(all);
     nroots = n;
     net_main = mains;
+    template_main.clear();
     return upload_book();
+  }
+
+  // Serving: `n` requests, request r being a copy of loaded net tmpl[r]. The
+  // copies share that net's definitions (defs are read-only templates) and
+  // each gets its own ROOT var, so nets of the batch become request templates.
+  int set_requests(const uint32_t* tmpl, uint32_t n) {
+    if (net_main.empty()) return fail("no batch loaded");
+    if (n == 0 || n > MAX_BATCH) return fail("request count out of range");
+    if (template_main.empty()) template_main = net_main;
+    std::vector<uint32_t> mains(n);
+    for (uint32_t r = 0; r < n; r++) {
+      if (tmpl[r] >= template_main.size()) return fail("request template out of range");
+      mains[r] = template_main[tmpl[r]];
+    }
+    net_main = mains;
+    nroots = n;
+    return 0;
   }
 
   int parse_book(const uint32_t* w, size_t words, std::vector<HostDef>& defs) {
@@ -994,8 +1013,12 @@ class Runtime {
     std::vector<uint32_t> ready;
     size_t ready_head = 0;
     uint32_t admitted_total = 0;
+    // A net's weight: the size of the def block its @main starts.
+    const std::vector<uint32_t>& blocks = template_main.empty() ? net_main : template_main;
     auto book_words = [&](uint32_t net) -> uint64_t {
-      uint32_t lo = net_main[net], hi = net + 1 < nroots ? net_main[net + 1] : (uint32_t)defs.size();
+      uint32_t lo = net_main[net];
+      auto it = std::upper_bound(blocks.begin(), blocks.end(), lo);
+      uint32_t hi = it == blocks.end() ? (uint32_t)defs.size() : *it;
       uint64_t w = 0;
       for (uint32_t f = lo; f < hi; f++) w += defs[f].node_len + defs[f].rbag_len;
       return w;
@@ -1320,6 +1343,12 @@ extern "C" int hvm_gb300_run_stream(hvm_gb300_runtime* r, const double* arrival_
   r->rt.norm_seconds += std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
   if (stats && r->rt.stats(stats)) return -1;
   return 0;
+}
+
+extern "C" int hvm_gb300_set_requests(hvm_gb300_runtime* r, const uint32_t* templates, uint32_t n) {
+  if (!r || !templates) return -1;
+  r->rt.err.clear();
+  return r->rt.set_requests(templates, n);
 }
 
 extern "C" int hvm_gb300_batch_roots(hvm_gb300_runtime* r, uint32_t* out, size_t cap) {

@@ -217,3 +217,21 @@ def mixed_batch(count: int = 4096, seed: int = 0x4D495845) -> list[tuple[str, di
             length = int(round(math.exp(math.log(10) + u * (math.log(1e5) - math.log(10)))))
             nets.append((countdown(length), {"family": "countdown", "length": length}))
     return nets
+
+
+def poisson_arrivals(count: int, rate: float, seed: int = 0x5E21E) -> list[float]:
+    """Arrival times (seconds) of a Poisson process of `rate` requests/s."""
+    rng = PCG32(seed, PCG_DEFAULT_SEQ)
+    t, out = 0.0, []
+    for _ in range(count):
+        t += -math.log1p(-rng.uniform()) / rate
+        out.append(t)
+    return out
+
+
+def serving_requests(count: int, rate: float, pool: int = 4096, seed: int = 0x5E21E) -> tuple[list[float], list[int]]:
+    """`count` requests arriving as a Poisson process of `rate`/s, each a net
+    drawn uniformly from the first `pool` nets of mixed_batch (the config-4
+    families). Returns (arrival times, template index per request)."""
+    rng = PCG32(seed ^ 0xA5A5A5A5, PCG_DEFAULT_SEQ)
+    return poisson_arrivals(count, rate, seed), [rng.next() % pool for _ in range(count)]

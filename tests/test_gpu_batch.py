@@ -93,3 +93,20 @@ def test_batch_4096(hvm, workloads, batch_golden):
         st, done, res = rt.run_stream(max_inflight=1536, live_frac=0.25)
         assert st.itrs == batch_golden["total_itrs"]
         check_roots(res, batch_golden["nets"])
+
+
+def test_serving_requests_match_goldens(hvm, workloads, batch_golden):
+    # Requests drawn from a pool of nets arrive as a Poisson process while
+    # others run; each response equals the reference's result for its net.
+    pool = 64
+    nets = workloads.mixed_batch(4096)[:pool]
+    arrivals, tmpl = workloads.serving_requests(200, 5000.0, pool=pool)
+    with hvm.Runtime(device=0) as rt:
+        rt.load_batch([code for code, _ in nets])
+        rt.set_requests(tmpl)
+        st, done, res = rt.run_stream(arrival_s=arrivals, max_inflight=64)
+        gold = batch_golden["nets"]
+        assert st.itrs == sum(gold[t]["itrs"] for t in tmpl)
+        for r, (p, t) in enumerate(zip(res, tmpl)):
+            assert numb_value(int(p)) == int(gold[t]["result"]), (r, t)
+        assert (done >= arrivals).all()
