@@ -167,11 +167,57 @@ typedef struct {
   uint32_t stopped;     /* 1 if the turn was ended by the dry rule */
   uint32_t budget;      /* interactions per thread allowed in the turn */
   uint32_t per_thread;  /* input redexes each thread took at the start */
+  float features[16];   /* scheduler inputs computed when the turn closed */
+  float outputs[3];     /* next turn's budget, stop fraction and static share,
+                           in the policy's output space (hvm_gb300_set_policy) */
 } hvm_gb300_turn;
 
 /* Copies up to `cap` turn records of the last run (needs trace_cap > 0);
  * `*n` receives how many exist. */
 int hvm_gb300_trace(hvm_gb300_runtime* rt, hvm_gb300_turn* out, size_t cap, size_t* n);
+
+/* ---- Turn scheduler -----------------------------------------------------------------
+ *
+ * Replaces the reference's fixed SEED/GROW/WORK turn policy
+ * (src/hvm.cu:1509-1548) for the runtime's later runs. After every turn the
+ * scheduler picks three parameters of the next one, each encoded in [0, 1]:
+ *   o0  turn budget   64 << round(10 o0) rounds per warp (64 .. 65536)
+ *   o1  stop fraction the turn ends once (32 + 192 o1)/256 of the initially
+ *                     busy threads have run dry
+ *   o2  static share  o2 * min(P/N, cap/2) input redexes per thread at turn
+ *                     start when the P pending redexes outnumber the N threads
+ * mode HVM_GB300_POLICY_FIXED   the built-in policy (default);
+ * mode HVM_GB300_POLICY_LEARNED the MLP 16 -> 64 -> 64 -> 3 (ReLU, sigmoid
+ *      outputs) with `weights` packed W1[64][16] b1 W2[64][64] b2 W3[3][64] b3
+ *      (HVM_GB300_POLICY_PARAMS floats), evaluated on the device by the turn's
+ *      last block from the 16 features of hvm_gb300_turn;
+ * mode HVM_GB300_POLICY_CONSTANT `constants[0..2]` while fewer redexes than
+ *      threads are pending, `constants[3..5]` otherwise.
+ * A negative (or non-finite) output keeps the fixed policy's choice. The policy
+ * changes only the order of reduction: normal forms and interaction counts are
+ * the same under every policy. */
+#define HVM_GB300_POLICY_FIXED 0u
+#define HVM_GB300_POLICY_LEARNED 1u
+#define HVM_GB300_POLICY_CONSTANT 2u
+#define HVM_GB300_POLICY_PARAMS 5443
+int hvm_gb300_set_policy(hvm_gb300_runtime* rt, uint32_t mode, const float* weights, size_t n_weights,
+                         const float* constants);
+
+/* Policy training (no reference counterpart). Rows of `x` are feature vectors
+ * (16 floats), rows of `t` target outputs (3 floats), `sw` per-row weights.
+ * The loss is sum_i sw_i * |mlp(x_i) - t_i|^2 / sum_i sw_i.
+ *   hvm_gb300_policy_forward  runs the in-kernel inference routine on each row
+ *   hvm_gb300_policy_grad     the loss and its gradient (HVM_GB300_POLICY_PARAMS)
+ *   hvm_gb300_policy_train    `epochs` full-batch Adam steps (beta 0.9/0.999)
+ *                             from `weights`, which receive the result; `loss`
+ *                             receives the loss before the last step
+ * All run on `device`; return 0, or -1 with `err` set. */
+int hvm_gb300_policy_forward(int device, const float* weights, const float* x, size_t n, float* y, char* err,
+                             size_t err_cap);
+int hvm_gb300_policy_grad(int device, const float* weights, const float* x, const float* t, const float* sw,
+                          size_t n, float* grad, float* loss, char* err, size_t err_cap);
+int hvm_gb300_policy_train(int device, float* weights, const float* x, const float* t, const float* sw, size_t n,
+                           uint32_t epochs, float lr, float* loss, char* err, size_t err_cap);
 
 /* Zeroes the measurement counters of hvm_gb300_stats (kernel_ms, launches,
  * h2d/d2h bytes); they otherwise accumulate over the runtime's life. */

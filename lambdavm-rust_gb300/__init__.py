@@ -56,6 +56,8 @@ class Turn(ctypes.Structure):
         ("stopped", ctypes.c_uint32),
         ("budget", ctypes.c_uint32),
         ("per_thread", ctypes.c_uint32),
+        ("features", ctypes.c_float * 16),
+        ("outputs", ctypes.c_float * 3),
     ]
 
 
@@ -77,6 +79,12 @@ class _Stats(ctypes.Structure):
         ("grid", ctypes.c_uint32),
         ("block", ctypes.c_uint32),
     ]
+
+
+# Turn scheduler modes and the MLP's shape (include/hvm_gb300.h).
+POLICY_FIXED, POLICY_LEARNED, POLICY_CONSTANT = 0, 1, 2
+POLICY_IN, POLICY_HID, POLICY_OUT = 16, 64, 3
+POLICY_PARAMS = POLICY_HID * POLICY_IN + POLICY_HID + POLICY_HID * POLICY_HID + POLICY_HID + POLICY_OUT * POLICY_HID + POLICY_OUT
 
 
 RULE_NAMES = ("LINK", "CALL", "VOID", "ERAS", "ANNI", "COMM", "OPER", "SWIT")
@@ -101,6 +109,10 @@ EXPORTED_SYMBOLS = (
     "hvm_gb300_set_requests",
     "hvm_gb300_batch_result",
     "hvm_gb300_count_live",
+    "hvm_gb300_set_policy",
+    "hvm_gb300_policy_forward",
+    "hvm_gb300_policy_grad",
+    "hvm_gb300_policy_train",
     "hvm_gb300_error",
     "hvm_gb300_destroy",
 )
@@ -145,6 +157,14 @@ def lib() -> ctypes.CDLL:
     L.hvm_gb300_batch_result.argtypes = [ctypes.c_void_p, ctypes.c_uint32, ctypes.c_char_p, ctypes.c_size_t,
                                          ctypes.POINTER(ctypes.c_size_t)]
     L.hvm_gb300_count_live.argtypes = [ctypes.c_void_p, ctypes.POINTER(ctypes.c_uint64)]
+    fp = ctypes.POINTER(ctypes.c_float)
+    L.hvm_gb300_set_policy.argtypes = [ctypes.c_void_p, ctypes.c_uint32, fp, ctypes.c_size_t, fp]
+    L.hvm_gb300_policy_forward.argtypes = [ctypes.c_int, fp, fp, ctypes.c_size_t, fp, ctypes.c_char_p,
+                                           ctypes.c_size_t]
+    L.hvm_gb300_policy_grad.argtypes = [ctypes.c_int, fp, fp, fp, fp, ctypes.c_size_t, fp, fp, ctypes.c_char_p,
+                                        ctypes.c_size_t]
+    L.hvm_gb300_policy_train.argtypes = [ctypes.c_int, fp, fp, fp, fp, ctypes.c_size_t, ctypes.c_uint32,
+                                         ctypes.c_float, fp, ctypes.c_char_p, ctypes.c_size_t]
     L.hvm_gb300_reset_counters.argtypes = [ctypes.c_void_p]
     L.hvm_gb300_reset_counters.restype = None
     L.hvm_gb300_error.argtypes = [ctypes.c_void_p]
@@ -328,7 +348,23 @@ class Runtime:
         self._check(lib().hvm_gb300_trace(self._h, None, 0, ctypes.byref(n)))
         arr = (Turn * max(1, n.value))()
         self._check(lib().hvm_gb300_trace(self._h, arr, n.value, ctypes.byref(n)))
-        return [{k: getattr(arr[i], k) for k, _ in Turn._fields_} for i in range(n.value)]
+        out = []
+        for i in range(n.value):
+            r = {k: getattr(arr[i], k) for k, _ in Turn._fields_}
+            r["features"] = list(r["features"])
+            r["outputs"] = list(r["outputs"])
+            out.append(r)
+        return out
+
+    def set_policy(self, mode: int = POLICY_FIXED, weights=None, constants=None) -> None:
+        """Selects the turn scheduler for later runs: POLICY_FIXED, POLICY_LEARNED
+        with `weights` (POLICY_PARAMS floats), or POLICY_CONSTANT with 6
+        `constants` (budget, stop fraction, static share while fewer redexes
+        than threads are pending, then the same three otherwise; -1 keeps the
+        fixed policy's choice)."""
+        w = _floats(weights) if weights is not None else None
+        c = _floats(constants) if constants is not None else None
+        self._check(lib().hvm_gb300_set_policy(self._h, mode, w, len(w) if w is not None else 0, c))
 
     def close(self) -> None:
         if getattr(self, "_h", None):
@@ -346,6 +382,69 @@ class Runtime:
             self.close()
         except Exception:
             pass
+
+
+def _floats(values):
+    vals = [float(v) for v in values]
+    return (ctypes.c_float * max(1, len(vals)))(*vals) if vals else None
+
+
+def _float_buf(arr, rows: int, cols: int):
+    import numpy as np
+    a = np.ascontiguousarray(np.asarray(arr, dtype=np.float32).reshape(rows, cols))
+    return a, a.ctypes.data_as(ctypes.POINTER(ctypes.c_float))
+
+
+def _err_buf():
+    return ctypes.create_string_buffer(512)
+
+
+def policy_forward(weights, x, device: int = 0):
+    """Outputs of the scheduler MLP for each row of `x` (n x 16), computed by
+    the routine the turn kernel runs."""
+    import numpy as np
+    x = np.asarray(x, dtype=np.float32)
+    n = x.shape[0]
+    w, wp = _float_buf(weights, 1, POLICY_PARAMS)
+    xa, xp = _float_buf(x, n, POLICY_IN)
+    y = np.zeros((n, POLICY_OUT), dtype=np.float32)
+    err = _err_buf()
+    if lib().hvm_gb300_policy_forward(device, wp, xp, n, y.ctypes.data_as(ctypes.POINTER(ctypes.c_float)), err, 512):
+        raise HvmError(err.value.decode())
+    return y
+
+
+def policy_grad(weights, x, t, sw, device: int = 0):
+    """(loss, gradient) of the weighted squared error of the MLP's outputs."""
+    import numpy as np
+    n = np.asarray(x).shape[0]
+    w, wp = _float_buf(weights, 1, POLICY_PARAMS)
+    xa, xp = _float_buf(x, n, POLICY_IN)
+    ta, tp = _float_buf(t, n, POLICY_OUT)
+    sa, sp = _float_buf(sw, n, 1)
+    g = np.zeros(POLICY_PARAMS, dtype=np.float32)
+    loss = ctypes.c_float()
+    err = _err_buf()
+    if lib().hvm_gb300_policy_grad(device, wp, xp, tp, sp, n, g.ctypes.data_as(ctypes.POINTER(ctypes.c_float)),
+                                   ctypes.byref(loss), err, 512):
+        raise HvmError(err.value.decode())
+    return loss.value, g
+
+
+def policy_train(weights, x, t, sw, epochs: int, lr: float = 1e-3, device: int = 0):
+    """Full-batch Adam training on the GPU; returns (new weights, loss)."""
+    import numpy as np
+    n = np.asarray(x).shape[0]
+    w = np.ascontiguousarray(np.asarray(weights, dtype=np.float32).reshape(POLICY_PARAMS).copy())
+    xa, xp = _float_buf(x, n, POLICY_IN)
+    ta, tp = _float_buf(t, n, POLICY_OUT)
+    sa, sp = _float_buf(sw, n, 1)
+    loss = ctypes.c_float()
+    err = _err_buf()
+    if lib().hvm_gb300_policy_train(device, w.ctypes.data_as(ctypes.POINTER(ctypes.c_float)), xp, tp, sp, n,
+                                    epochs, lr, ctypes.byref(loss), err, 512):
+        raise HvmError(err.value.decode())
+    return w, loss.value
 
 
 def run_text(code: str, device: int = 0, **cfg) -> tuple[str, RunStats]:

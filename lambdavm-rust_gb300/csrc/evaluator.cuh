@@ -49,6 +49,8 @@ struct TurnRecord {
   unsigned long long pending;       // redexes in the ring for the next turn
   unsigned int dry, stopped;        // dry threads at close; 1 if ended by the dry rule
   unsigned int budget, per_thread;  // the closed turn's budget and static share
+  float features[16];               // scheduler inputs computed at the close of the turn
+  float outputs[3];                 // the next turn's parameters in output space (see apply_policy)
 };
 
 // Control block of one net. Hot atomics sit on separate 128-byte lines.
@@ -76,8 +78,7 @@ struct alignas(128) Ctl {
   unsigned int static_per_thread;   // ring items each thread takes at turn start
   unsigned int budget;              // interactions per thread per turn
   unsigned int chunk;               // items per dynamic claim
-  unsigned int policy;              // 0 = fixed policy
-  unsigned int pad_c[1];
+  unsigned int pad_c[2];
   unsigned long long hist[8];       // interactions per rule (diagnostic)
   unsigned long long prof[8];       // profile counters (when prof_on): see PROF_*
   unsigned int prof_on;
@@ -87,6 +88,14 @@ struct alignas(128) Ctl {
   // moves to `tail` between turns (the redex ring's discipline).
   unsigned int nf_head, nf_tail, nf_end, vf_head, vf_tail, vf_end;
   long long live_nodes, live_vars;  // words in use, summed at the end of each turn
+  // Scheduler policy (policy.cuh): mode, constant outputs for mode 2 (one
+  // triple while fewer redexes than threads are pending, one otherwise; a
+  // negative entry keeps the fixed policy's choice), MLP weights for mode 1,
+  // and the previous turn's counters for the features.
+  unsigned int policy_mode;
+  float policy_const[6];
+  const float* policy_w;
+  unsigned long long prev_itrs, prev_leak, prev_hist[8], turn_t0;
   unsigned int npool_next;          // next page id of the node pool
   unsigned int vpool_next;          // next page id of the var pool
   TurnRecord* trace;                // per-turn records (null = off)

@@ -22,6 +22,7 @@
 #include <cuda_runtime.h>
 #include <algorithm>
 #include <chrono>
+#include <cmath>
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
@@ -30,6 +31,7 @@
 
 #include "hvm_defs.h"
 #include "evaluator.cuh"
+#include "policy.cuh"
 #include "hvm_gb300.h"
 
 namespace hvm {
@@ -105,6 +107,73 @@ __device__ void fixed_policy(Ctl* c, unsigned long long pending, unsigned long l
   c->static_per_thread = s;
   c->budget = budget;
   c->chunk = chunk;
+}
+
+// The scheduler's 16 inputs, computed by one thread from the control block at
+// the close of a turn (all roughly in [0, 1]).
+__device__ void policy_features(const Dev& d, unsigned long long pending, unsigned long long prev_pending,
+                                float* f) {
+  Ctl* c = d.ctl;
+  const float N = (float)d.nthreads;
+  unsigned long long now;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(now));
+  const float dt_us = c->turn_t0 ? (float)(now - c->turn_t0) * 1e-3f : 0.f;
+  c->turn_t0 = now;
+  const unsigned long long itrs = c->itrs, leak = c->leak;
+  const float it = (float)(itrs - c->prev_itrs), lk = (float)(leak - c->prev_leak);
+  float h[8];
+  for (int i = 0; i < 8; i++) { h[i] = (float)(c->hist[i] - c->prev_hist[i]); c->prev_hist[i] = c->hist[i]; }
+  c->prev_itrs = itrs;
+  c->prev_leak = leak;
+  const float P = (float)pending, Pp = (float)prev_pending;
+  f[0] = log2f(1.f + P) / 24.f;
+  f[1] = log2f(1.f + P / N) / 8.f;
+  f[2] = log2f(1.f + Pp) / 24.f;
+  f[3] = fminf(fmaxf(log2f((1.f + P) / (1.f + Pp)) / 8.f, -1.f), 1.f);
+  f[4] = (float)c->dry / N;
+  f[5] = c->stop ? 1.f : 0.f;
+  f[6] = log2f(1.f + (float)c->budget) / 17.f;
+  f[7] = log2f(1.f + it / N) / 8.f;
+  f[8] = log2f(1.f + dt_us) / 20.f;
+  f[9] = (float)c->live_nodes / (float)(d.node_mask + 1ull);
+  f[10] = (float)c->live_vars / (float)(d.vars_mask + 1ull);
+  f[11] = lk / (1.f + it);
+  f[12] = log2f(1.f + (float)c->turns) / 16.f;
+  f[13] = h[CALL] / (1.f + it);
+  f[14] = h[ANNI] / (1.f + it);
+  f[15] = (h[OPER] + h[SWIT]) / (1.f + it);
+}
+
+// Maps the policy's three outputs in [0, 1] onto the next turn, after the
+// fixed policy has made its choice: o0 the budget (64 << round(10 o0), i.e.
+// 64 .. 65536 rounds), o1 the stop fraction (32 + 192 o1, in 1/256), o2 the
+// share of the input each thread takes statically (o2 * min(P/N, cap/2)) when
+// every thread has work. A negative or non-finite output keeps the fixed
+// choice. `eff` receives the parameters actually chosen, in the same space.
+__device__ void apply_policy(Ctl* c, const float* o, unsigned long long pending, uint32_t nthreads, uint32_t cap,
+                             float* eff) {
+  unsigned long long busy = pending < nthreads ? pending : nthreads;
+  if (o[0] >= 0.f && isfinite(o[0])) c->budget = 64u << (uint32_t)lrintf(fminf(o[0], 1.f) * 10.f);
+  uint32_t frac = c->stop_frac_q8;
+  if (o[1] >= 0.f && isfinite(o[1])) {
+    frac = 32u + (uint32_t)(fminf(o[1], 1.f) * 192.f);
+    unsigned long long keep = (busy * (256 - frac)) >> 8;
+    c->stop_at = (uint32_t)(nthreads - keep);
+  }
+  float share = 1.f;
+  if (pending >= nthreads) {
+    unsigned long long per = pending / nthreads;
+    uint32_t full = (uint32_t)(per < cap / 2 ? per : cap / 2);
+    if (full == 0) full = 1;
+    if (o[2] >= 0.f && isfinite(o[2])) {
+      uint32_t s = (uint32_t)lrintf(fminf(o[2], 1.f) * (float)full);
+      c->static_per_thread = s ? s : 1;
+    }
+    share = (float)c->static_per_thread / (float)full;
+  }
+  eff[0] = log2f((float)(c->budget >> 6)) / 10.f;
+  eff[1] = ((float)frac - 32.f) / 192.f;
+  eff[2] = share;
 }
 
 // MIN_BLOCKS_128 > 0 asks the compiler to fit that many 128-thread blocks per
@@ -272,47 +341,73 @@ __global__ void __launch_bounds__(128, MIN_BLOCKS_128 > 0 ? MIN_BLOCKS_128 : 1) 
   }
 
   // The last block to finish closes the turn and picks the next one.
+  __shared__ unsigned sh_last;
+  __shared__ float feat[POLICY_IN], h1[POLICY_HID], h2[POLICY_HID], outp[POLICY_OUT];
+  __shared__ unsigned long long sh_pending, sh_prev, sh_nb, sh_tail;
   __syncthreads();
   if (threadIdx.x == 0) {
     __threadfence();
     unsigned prev = atomicAdd(&c->blocks_done, 1u);
-    if (prev == gridDim.x - 1) {
+    sh_last = prev == gridDim.x - 1;
+    if (sh_last) {
       __threadfence();
       unsigned long long head = ldcg64(&c->head), tail = ldcg64(&c->tail);
-      unsigned long long nb = head < in_end ? head : in_end;
-      unsigned long long pending = tail - nb;
-      unsigned long long prev_pending = c->pending;
-      if (c->trace && c->turns < c->trace_cap) {
-        unsigned long long now;
-        asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(now));
-        TurnRecord r;
-        r.t_ns = now;
-        r.live_nodes = c->live_nodes;
-        r.itrs = c->itrs;
-        r.pending = pending;
-        r.dry = c->dry;
-        r.stopped = c->stop;
-        r.budget = c->budget;
-        r.per_thread = c->static_per_thread;
-        c->trace[c->turns] = r;
-      }
-      c->base = nb;
-      c->in_end = tail;
-      c->pending = pending;
-      c->turns += 1;
-      c->dry = 0;
-      c->stop = 0;
-      // Free-page rings: the pages returned this turn become takeable.
-      c->nf_head = c->nf_head < c->nf_end ? c->nf_head : c->nf_end;
-      c->nf_end = c->nf_tail;
-      c->vf_head = c->vf_head < c->vf_end ? c->vf_head : c->vf_end;
-      c->vf_end = c->vf_tail;
-      fixed_policy(c, pending, prev_pending, d.nthreads, cap);
-      unsigned long long take = (unsigned long long)c->static_per_thread * d.nthreads;
-      c->head = nb + (take < pending ? take : pending);
-      c->blocks_done = 0;
-      __threadfence();
+      sh_nb = head < in_end ? head : in_end;
+      sh_tail = tail;
+      sh_pending = tail - sh_nb;
+      sh_prev = c->pending;
+      policy_features(d, sh_pending, sh_prev, feat);
     }
+  }
+  __syncthreads();
+  if (!sh_last) return;
+  const uint32_t mode = __ldcg(&c->policy_mode);
+  if (mode == POLICY_LEARNED && c->policy_w) policy_infer_block(c->policy_w, feat, h1, h2, outp);
+  if (threadIdx.x == 0) {
+    const unsigned long long pending = sh_pending, prev_pending = sh_prev, nb = sh_nb;
+    if (mode == POLICY_CONSTANT) {
+      const int k = pending < d.nthreads ? 0 : 3;
+      outp[0] = c->policy_const[k]; outp[1] = c->policy_const[k + 1]; outp[2] = c->policy_const[k + 2];
+    } else if (mode != POLICY_LEARNED || !c->policy_w) {
+      outp[0] = outp[1] = outp[2] = -1.f;
+    }
+    float eff[POLICY_OUT];
+    const unsigned closed_budget = c->budget, closed_share = c->static_per_thread;
+    const unsigned closed_dry = c->dry, closed_stop = c->stop;
+    const unsigned long long closed_turn = c->turns;
+    c->base = nb;
+    c->in_end = sh_tail;
+    c->pending = pending;
+    c->turns += 1;
+    c->dry = 0;
+    c->stop = 0;
+    // Free-page rings: the pages returned this turn become takeable.
+    c->nf_head = c->nf_head < c->nf_end ? c->nf_head : c->nf_end;
+    c->nf_end = c->nf_tail;
+    c->vf_head = c->vf_head < c->vf_end ? c->vf_head : c->vf_end;
+    c->vf_end = c->vf_tail;
+    fixed_policy(c, pending, prev_pending, d.nthreads, cap);
+    apply_policy(c, outp, pending, d.nthreads, cap, eff);
+    if (c->trace && closed_turn < c->trace_cap) {
+      unsigned long long now;
+      asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(now));
+      TurnRecord r;
+      r.t_ns = now;
+      r.live_nodes = c->live_nodes;
+      r.itrs = c->itrs;
+      r.pending = pending;
+      r.dry = closed_dry;
+      r.stopped = closed_stop;
+      r.budget = closed_budget;
+      r.per_thread = closed_share;
+      for (int i = 0; i < POLICY_IN; i++) r.features[i] = feat[i];
+      for (int i = 0; i < POLICY_OUT; i++) r.outputs[i] = eff[i];
+      c->trace[closed_turn] = r;
+    }
+    unsigned long long take = (unsigned long long)c->static_per_thread * d.nthreads;
+    c->head = nb + (take < pending ? take : pending);
+    c->blocks_done = 0;
+    __threadfence();
   }
 }
 
@@ -527,6 +622,10 @@ class Runtime {
   size_t smem = 0;
   uint32_t max_def_nodes = 1, max_def_vars = 1;
   int sms = 0;
+  // Scheduler policy written into the control block at every reset.
+  uint32_t policy_mode = POLICY_FIXED;
+  float policy_const[6] = {-1.f, -1.f, -1.f, -1.f, -1.f, -1.f};
+  float* mem_policy = nullptr;
   double norm_seconds = 0;
   uint64_t norm_calls = 0;
   // Measurement: device time of turn kernels (events around each launch),
@@ -546,10 +645,11 @@ class Runtime {
 
   void release() {
     void* ps[] = {mem_node, mem_vars, mem_ring, mem_cur, mem_scratch, mem_defs, mem_book, g_out, g_kids, g_info, ctl,
-                  mem_trace, mem_roots, mem_free, mem_mains};
+                  mem_trace, mem_roots, mem_free, mem_mains, mem_policy};
     for (void* p : ps) if (p) cudaFree(p);
     mem_node = mem_vars = mem_ring = mem_cur = mem_scratch = mem_defs = mem_book = mem_trace = mem_roots = mem_free =
         mem_mains = nullptr;
+    mem_policy = nullptr;
     g_out = nullptr; g_kids = nullptr; g_info = nullptr; ctl = nullptr;
   }
 
@@ -642,6 +742,7 @@ class Runtime {
     if (cfg.profile) { uint32_t one = 1; CK(cudaMemcpy(&ctl->prof_on, &one, sizeof(one), cudaMemcpyHostToDevice)); }
     uint32_t frac = cfg.stop_frac_q8 ? cfg.stop_frac_q8 : 128;
     CK(cudaMemcpy(&ctl->stop_frac_q8, &frac, sizeof(frac), cudaMemcpyHostToDevice));
+    if (write_policy()) return -1;
     if (cfg.trace_cap) {
       if (!mem_trace) CK(cudaMalloc(&mem_trace, (size_t)cfg.trace_cap * sizeof(TurnRecord)));
       TurnRecord* tp = (TurnRecord*)mem_trace;
@@ -656,6 +757,31 @@ class Runtime {
     norm_seconds = 0;
     norm_calls = 0;
     return 0;
+  }
+
+  int write_policy() {
+    const float* w = policy_mode == POLICY_LEARNED ? mem_policy : nullptr;
+    CK(cudaMemcpy(&ctl->policy_mode, &policy_mode, sizeof(policy_mode), cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(&ctl->policy_const, policy_const, sizeof(policy_const), cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(&ctl->policy_w, &w, sizeof(w), cudaMemcpyHostToDevice));
+    return 0;
+  }
+
+  int set_policy(uint32_t mode, const float* weights, size_t n, const float* constants) {
+    if (mode > POLICY_CONSTANT) return fail("unknown policy mode");
+    if (mode == POLICY_LEARNED) {
+      if (!weights || n != (size_t)POLICY_PARAMS) return fail("learned policy needs HVM_GB300_POLICY_PARAMS weights");
+      for (size_t i = 0; i < n; i++)
+        if (!std::isfinite(weights[i])) return fail("policy weights must be finite");
+      if (!mem_policy) CK(cudaMalloc((void**)&mem_policy, POLICY_PARAMS * sizeof(float)));
+      CK(cudaMemcpy(mem_policy, weights, POLICY_PARAMS * sizeof(float), cudaMemcpyHostToDevice));
+    }
+    if (mode == POLICY_CONSTANT) {
+      if (!constants) return fail("constant policy needs 6 constants");
+      for (int i = 0; i < 6; i++) policy_const[i] = constants[i];
+    }
+    policy_mode = mode;
+    return write_policy();
   }
 
   // Parses the book buffer (src/hvm.c:1408-1453 limits and messages).
@@ -1411,8 +1537,17 @@ extern "C" int hvm_gb300_trace(hvm_gb300_runtime* r, hvm_gb300_turn* out, size_t
     out[i].stopped = tmp[i].stopped;
     out[i].budget = tmp[i].budget;
     out[i].per_thread = tmp[i].per_thread;
+    for (int j = 0; j < 16; j++) out[i].features[j] = tmp[i].features[j];
+    for (int j = 0; j < 3; j++) out[i].outputs[j] = tmp[i].outputs[j];
   }
   return 0;
+}
+
+extern "C" int hvm_gb300_set_policy(hvm_gb300_runtime* r, uint32_t mode, const float* weights, size_t n_weights,
+                                    const float* constants) {
+  if (!r) return -1;
+  r->rt.err.clear();
+  return r->rt.set_policy(mode, weights, n_weights, constants);
 }
 
 extern "C" int hvm_gb300_result(hvm_gb300_runtime* r, char* out, size_t cap, size_t* len) {

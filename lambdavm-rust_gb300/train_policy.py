@@ -1,0 +1,185 @@
+"""Trains the turn scheduler's MLP from evaluator traces (GPU).
+
+The reference schedules turns with a fixed SEED/GROW/WORK policy
+(src/hvm.cu:1509-1548); this runtime's fixed policy is its counterpart and the
+learned policy is trained to imitate the fastest schedule found per net:
+
+1. Every training net runs under the fixed policy and under a grid of constant
+   schedules (per regime: while fewer redexes than threads are pending, and
+   otherwise), with per-turn tracing on. Each run records, at the close of every
+   turn, the 16 scheduler features and the next turn's parameters in the
+   policy's output space (budget, stop fraction, static share).
+2. Per net, the run with the lowest device time wins; its (features, next
+   parameters) pairs join the training set, each net weighted equally.
+3. The MLP is trained on the GPU (hvm_gb300_policy_train: full-batch Adam, one
+   CUDA-graph replay per epoch) and written to a JSON file with the per-net
+   timings of the fixed, best constant and learned schedules.
+
+Normal forms and interaction counts are the same under every schedule; each
+run is checked against the fixed policy's.
+
+    python lambdavm-rust_gb300/train_policy.py --out lambdavm-rust_gb300/policy_weights.json
+"""
+from __future__ import annotations
+
+import argparse
+import importlib
+import itertools
+import json
+import math
+import os
+import sys
+import time
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, os.path.dirname(HERE))
+hvm = importlib.import_module("lambdavm-rust_gb300")
+wl = importlib.import_module("lambdavm-rust_gb300.workloads")
+
+# Constant schedules: (budget, stop fraction, share) per regime; -1 keeps the
+# fixed policy's choice.
+SEED_BUDGET = (-1.0, 0.0, 0.4, 1.0)
+WORK_BUDGET = (-1.0, 0.6)
+WORK_STOP = (0.0, -1.0, 1.0)
+WORK_SHARE = (-1.0, 0.5)
+
+
+def constant_grid() -> list[tuple[float, ...]]:
+    grid = []
+    for sb, wb, ws, wsh in itertools.product(SEED_BUDGET, WORK_BUDGET, WORK_STOP, WORK_SHARE):
+        grid.append((sb, -1.0, -1.0, wb, ws, wsh))
+    return grid
+
+
+def training_nets() -> list[tuple[str, str]]:
+    """Seeded nets of the benchmark families, none equal to a benchmark input."""
+    nets = []
+    for k, (lg, p) in enumerate(itertools.product((12, 14, 16), (1 / 16, 1 / 64, 1 / 256))):
+        seed = 0x5EED0000 + k
+        nets.append((f"skewed_fold_2p{lg}_p{round(1 / p)}", wl.skewed_fold(lg, seed=seed, p=p)))
+    for d in (14, 17):
+        nets.append((f"tree_sum_d{d}", wl.tree_sum(d)))
+    for lg in (10, 12):
+        nets.append((f"bitonic_sort_2p{lg}_s", wl.bitonic_sort(lg, seed=0xB170 + lg)))
+    for n in (3000, 30000):
+        nets.append((f"countdown_{n}", wl.countdown(n)))
+    return nets
+
+
+def timed_run(rt, reps: int) -> tuple[float, object]:
+    """Best device time (ms) over `reps` runs, and the last run's stats."""
+    best, st = math.inf, None
+    for _ in range(reps):
+        rt.reset_counters()
+        st = rt.run()
+        best = min(best, st.kernel_ms)
+    return best, st
+
+
+def collect(nets, reps: int, trace_cap: int, log=print):
+    grid = constant_grid()
+    xs, ts, ws, report = [], [], [], []
+    for name, code in nets:
+        with hvm.Runtime(device=0, trace_cap=trace_cap) as rt:
+            rt.load(code)
+            rt.set_policy(hvm.POLICY_FIXED)
+            fixed_ms, st0 = timed_run(rt, reps)
+            want = (rt.result(), st0.itrs)
+            best = (fixed_ms, None, rt.trace())
+            for const in grid:
+                rt.set_policy(hvm.POLICY_CONSTANT, constants=const)
+                ms, st = timed_run(rt, reps)
+                if (rt.result(), st.itrs) != want:
+                    raise RuntimeError(f"{name}: schedule {const} changed the result")
+                if ms < best[0]:
+                    best = (ms, const, rt.trace())
+            ms, const, trace = best
+            feats = np.array([r["features"] for r in trace], dtype=np.float32)
+            outs = np.array([r["outputs"] for r in trace], dtype=np.float32)
+            # The last record closes the final turn: nothing follows it.
+            feats, outs = feats[:-1], outs[:-1]
+            if len(feats):
+                xs.append(feats)
+                ts.append(np.clip(outs, 0.0, 1.0))
+                ws.append(np.full(len(feats), 1.0 / len(feats), dtype=np.float32))
+            report.append({"net": name, "itrs": want[1], "fixed_ms": round(fixed_ms, 3),
+                           "best_ms": round(ms, 3), "best_schedule": const, "turns": len(trace)})
+            log(f"{name:28s} itrs={want[1]:>11d} fixed={fixed_ms:8.2f} ms best={ms:8.2f} ms {const}")
+    return np.concatenate(xs), np.concatenate(ts), np.concatenate(ws), report
+
+
+def init_weights(seed: int = 1) -> np.ndarray:
+    """He-uniform hidden layers, small output layer, zero biases."""
+    rng = np.random.default_rng(seed)
+    parts = []
+    for fan_in, fan_out, gain in ((16, 64, 2.0), (64, 64, 2.0), (64, 3, 0.1)):
+        lim = math.sqrt(3.0 * gain / fan_in)
+        parts.append(rng.uniform(-lim, lim, size=(fan_out, fan_in)).astype(np.float32).ravel())
+        parts.append(np.zeros(fan_out, dtype=np.float32))
+    w = np.concatenate(parts)
+    assert w.size == hvm.POLICY_PARAMS
+    return w
+
+
+def evaluate(nets, weights, reps: int, log=print) -> list[dict]:
+    rows = []
+    for name, code in nets:
+        with hvm.Runtime(device=0) as rt:
+            rt.load(code)
+            rt.set_policy(hvm.POLICY_FIXED)
+            fixed_ms, st0 = timed_run(rt, reps)
+            want = (rt.result(), st0.itrs)
+            rt.set_policy(hvm.POLICY_LEARNED, weights=weights)
+            ms, st = timed_run(rt, reps)
+            if (rt.result(), st.itrs) != want:
+                raise RuntimeError(f"{name}: learned schedule changed the result")
+        rows.append({"net": name, "fixed_ms": round(fixed_ms, 3), "learned_ms": round(ms, 3),
+                     "speedup": round(fixed_ms / ms, 3)})
+        log(f"{name:28s} fixed={fixed_ms:8.2f} ms learned={ms:8.2f} ms x{fixed_ms / ms:.3f}")
+    return rows
+
+
+def main() -> None:
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--out", default=os.path.join(HERE, "policy_weights.json"))
+    ap.add_argument("--reps", type=int, default=2)
+    ap.add_argument("--epochs", type=int, default=4000)
+    ap.add_argument("--lr", type=float, default=2e-3)
+    ap.add_argument("--trace-cap", type=int, default=8192)
+    ap.add_argument("--seed", type=int, default=1)
+    args = ap.parse_args()
+    t0 = time.time()
+    nets = training_nets()
+    x, t, sw, report = collect(nets, args.reps, args.trace_cap)
+    print(f"collected {len(x)} turns from {len(nets)} nets in {time.time() - t0:.1f} s")
+    w0 = init_weights(args.seed)
+    loss0, _ = hvm.policy_grad(w0, x, t, sw)
+    t1 = time.time()
+    w, loss = hvm.policy_train(w0, x, t, sw, epochs=args.epochs, lr=args.lr)
+    print(f"trained {args.epochs} epochs in {time.time() - t1:.2f} s: loss {loss0:.5f} -> {loss:.5f}")
+    rows = evaluate(nets, w, args.reps)
+    out = {
+        "format": "hvm_gb300 turn-scheduler MLP 16-64-64-3, packed W1 b1 W2 b2 W3 b3 (float32)",
+        "params": [float(v) for v in w],
+        "training": {"nets": report, "turns": int(len(x)), "epochs": args.epochs, "lr": args.lr,
+                     "loss_initial": loss0, "loss_final": loss, "seed": args.seed},
+        "evaluation": rows,
+    }
+    with open(args.out, "w") as f:
+        json.dump(out, f)
+    print(f"wrote {args.out}")
+
+
+def load_weights(path: str | None = None) -> np.ndarray:
+    """The committed policy weights (float32, POLICY_PARAMS)."""
+    with open(path or os.path.join(HERE, "policy_weights.json")) as f:
+        w = np.asarray(json.load(f)["params"], dtype=np.float32)
+    if w.size != hvm.POLICY_PARAMS or not np.all(np.isfinite(w)):
+        raise ValueError("policy weights file is malformed")
+    return w
+
+
+if __name__ == "__main__":
+    main()

@@ -42,3 +42,11 @@ def test_cli_book_matches_library(hvm, tmp_path):
     subprocess.run([hvm.CLI_PATH, "book", str(src), str(out)], check=True)
     import numpy as np
     assert np.array_equal(np.fromfile(out, dtype=np.uint32), hvm.book_from_text(src.read_text()))
+
+
+def test_committed_policy_weights_are_well_formed(hvm):
+    import importlib
+    train = importlib.import_module("lambdavm-rust_gb300.train_policy")
+    w = train.load_weights()
+    assert w.shape == (hvm.POLICY_PARAMS,)
+    assert hvm.POLICY_PARAMS == 5443
