@@ -38,8 +38,16 @@ enum : uint32_t {
 // book[off .. off+rbag_len) (redexes) then book[off+rbag_len ..) (nodes).
 struct DefHdr {
   uint32_t node_len, rbag_len, vars_len, safe;
-  uint32_t root, off, pad0, pad1;
+  uint32_t root, off;
+  uint32_t joined;  // 1: the rbag holds every link of a call, the root's included
+                    // (its caller end written as CALLER_PORT), with vars that
+                    // only wired two links removed; 0: the book's own layout
+  uint32_t pad;
 };
+
+// Stands for the other side of a CALL's redex in a joined def's link list
+// (a REF to a fid no book can have).
+constexpr Port CALLER_PORT = 0xFFFFFFF9u;
 
 // One record per completed turn, written by the turn's last block.
 struct TurnRecord {
@@ -445,6 +453,7 @@ struct Plan {
   uint32_t node_len, rbag_len, vars_len, off;  // CALL: the def
   uint32_t nbase, vbase;  // CALL: first fresh node / var (contiguous runs), or
   bool contig;            //       per-word scratch tables when the def is large
+  bool joined;            // CALL: the def's links include the root link (DefHdr::joined)
   Port root;            // CALL: the def's root
   Numb cv;              // OPER: the result when both sides are numbers
   bool oper_num;        // OPER: B1 is a number
@@ -489,8 +498,8 @@ __device__ __forceinline__ void link_pair(const Dev& d, uint32_t gid, const Plan
     default: {  // CALL
       if (i < p.rbag_len) {
         Pair q = __ldg((const unsigned long long*)&d.book[p.off + i]);
-        x = relocate(d, gid, p, get_fst(q));
-        y = relocate(d, gid, p, get_snd(q));
+        x = get_fst(q) == CALLER_PORT ? p.b : relocate(d, gid, p, get_fst(q));
+        y = get_snd(q) == CALLER_PORT ? p.b : relocate(d, gid, p, get_snd(q));
       } else {
         x = relocate(d, gid, p, p.root);
         y = p.b;
@@ -518,7 +527,7 @@ __device__ __forceinline__ bool plan_redex(const Dev& d, TState& t, Pair r, Plan
       rule = ERAS;  // copy optimisation (src/hvm.c:870-873): still one interaction
     } else {
       p.node_len = h.node_len; p.rbag_len = h.rbag_len; p.vars_len = h.vars_len;
-      p.off = h.off; p.root = h.root;
+      p.off = h.off; p.root = h.root; p.joined = h.joined != 0;
     }
   }
   p.rule = rule;
@@ -683,7 +692,7 @@ __device__ __forceinline__ int lockstep_round(const Dev& d, TState& t, bool has,
           nstore(d, at, new_pair(relocate(d, t.gid, p, get_fst(q)), relocate(d, t.gid, p, get_snd(q))));
         }
         made = p.node_len > 0 || p.vars_len > 0;
-        p.nlinks = p.rbag_len + 1;
+        p.nlinks = p.rbag_len + (p.joined ? 0 : 1);
         break;
       }
     }

@@ -231,6 +231,10 @@ __global__ void __launch_bounds__(128, MIN_BLOCKS_128 > 0 ? MIN_BLOCKS_128 : 1) 
   const bool prof_on = __ldcg(&c->prof_on) != 0;
   for (int i = 0; i < 8; i++) prof.v[i] = 0;
   long long t_loop = clock64();
+  // The turn's input is [base, in_end) and `head` only grows: once a claim
+  // finds it exhausted, the warp stops polling it (an L2 round trip a round).
+  bool ring_dry = false;
+  unsigned stop_flag = 0;  // lane 0: the stop flag as loaded after the previous round
   for (uint32_t round = 0; round < budget; round++) {
     // Intra-warp balancing: each empty lane takes the oldest redex of a lane
     // holding two or more (all in shared memory, no global traffic).
@@ -252,7 +256,7 @@ __global__ void __launch_bounds__(128, MIN_BLOCKS_128 > 0 ? MIN_BLOCKS_128 : 1) 
     }
     // Lanes still empty claim ring input, one atomic for the warp.
     unsigned empty = __ballot_sync(0xFFFFFFFFu, t.len == 0);
-    if (empty) {
+    if (empty && !ring_dry) {
       unsigned long long h = 0;
       if (lane == 0) {
         h = ldcg64(&c->head);
@@ -263,6 +267,7 @@ __global__ void __launch_bounds__(128, MIN_BLOCKS_128 > 0 ? MIN_BLOCKS_128 : 1) 
       if (((empty >> lane) & 1) && h + k < in_end) {
         push(d, t, (Pair)__ldcg((const unsigned long long*)&d.ring[(h + k) & d.ring_mask]));
       }
+      ring_dry = h + __popc(empty) >= in_end;
     }
     if (!__any_sync(0xFFFFFFFFu, t.len > 0)) {
       // The whole warp ran dry: count it; enough dry threads end the turn.
@@ -272,14 +277,15 @@ __global__ void __launch_bounds__(128, MIN_BLOCKS_128 > 0 ? MIN_BLOCKS_128 : 1) 
       }
       break;
     }
-    // The stop flag is loaded before the round and tested after it, so its
-    // latency hides behind the round's own memory traffic.
-    unsigned stop_now = lane == 0 ? *(volatile unsigned*)&c->stop : 0;
     const bool has = t.len > 0;
     const Pair r = has ? pop(t) : 0;
     lockstep_round(d, t, has, r, prof_on ? &prof : nullptr);
     if (__any_sync(0xFFFFFFFFu, t.dead)) break;
-    if (__shfl_sync(0xFFFFFFFFu, stop_now, 0)) break;
+    // The stop flag is tested one round after it was loaded, so its L2
+    // latency hides behind a whole round (a short round would otherwise wait
+    // for it).
+    if (__shfl_sync(0xFFFFFFFFu, stop_flag, 0)) break;
+    if (lane == 0) stop_flag = *(volatile unsigned*)&c->stop;
   }
 
   if (prof_on && lane == 0) {
@@ -597,6 +603,65 @@ struct HostDef {
   std::vector<Pair> rbag, node;
 };
 
+// A CALL wires the def's redexes and then its root to the caller's port
+// (src/hvm.c:865-898), each by the linker. Before upload, every def's links
+// are rewritten as one list -- the redexes, then (root ~ CALLER_PORT) -- and
+// a var whose two occurrences are both link ends (never inside a node) is
+// removed by joining its two links: (P ~ v), (v ~ Q) become (P ~ Q). Such a
+// var is only a wire between two links of the same call, so the device need
+// not allocate, publish and take it (two atomic exchanges and a fence). The
+// remaining vars are renumbered densely. Interactions and normal forms are
+// unchanged: the same redexes are formed, only without the detour.
+static void join_links(const HostDef& h, std::vector<Pair>& links, std::vector<Pair>& nodes, uint32_t& vars_len) {
+  struct L { Port x, y; bool live; };
+  std::vector<L> ls;
+  for (Pair p : h.rbag) ls.push_back({get_fst(p), get_snd(p), true});
+  ls.push_back({h.root, CALLER_PORT, true});
+  std::vector<uint8_t> in_node(h.vars_len, 0);
+  for (Pair p : h.node)
+    for (Port q : {get_fst(p), get_snd(p)})
+      if (get_tag(q) == VAR) in_node[get_val(q)] = 1;
+  auto is_free_var = [&](Port q) { return q != CALLER_PORT && get_tag(q) == VAR && !in_node[get_val(q)]; };
+  for (bool changed = true; changed;) {
+    changed = false;
+    for (size_t j = 0; j < ls.size() && !changed; j++) {
+      if (!ls[j].live) continue;
+      for (int side = 0; side < 2 && !changed; side++) {
+        Port v = side ? ls[j].y : ls[j].x;
+        if (!is_free_var(v)) continue;
+        Port keep = side ? ls[j].x : ls[j].y;
+        if (keep == v) continue;  // v ~ v: a closed loop, left to the linker
+        for (size_t k = 0; k < ls.size(); k++) {
+          if (k == j || !ls[k].live) continue;
+          Port other;
+          if (ls[k].x == v) other = ls[k].y;
+          else if (ls[k].y == v) other = ls[k].x;
+          else continue;
+          ls[j] = {keep, other, true};
+          ls[k].live = false;
+          changed = true;
+          break;
+        }
+      }
+    }
+  }
+  // Dense renumbering of the vars still in use.
+  std::vector<uint32_t> map(h.vars_len, ~0u);
+  uint32_t next = 0;
+  auto renum = [&](Port q) -> Port {
+    if (q == CALLER_PORT || get_tag(q) != VAR) return q;
+    uint32_t& m = map[get_val(q)];
+    if (m == ~0u) m = next++;
+    return new_port(VAR, m);
+  };
+  links.clear();
+  nodes.clear();
+  for (Pair p : h.node) nodes.push_back(new_pair(renum(get_fst(p)), renum(get_snd(p))));
+  for (const L& l : ls)
+    if (l.live) links.push_back(new_pair(renum(l.x), renum(l.y)));
+  vars_len = next;
+}
+
 class Runtime {
  public:
   hvm_gb300_config cfg;
@@ -907,12 +972,15 @@ class Runtime {
     max_def_nodes = 1;
     max_def_vars = 1;
     for (size_t f = 0; f < defs.size(); f++) {
-      HostDef& h = defs[f];
-      hdr[f] = DefHdr{h.node_len, h.rbag_len, h.vars_len, h.safe ? 1u : 0u, h.root, (uint32_t)flat.size(), 0, 0};
-      flat.insert(flat.end(), h.rbag.begin(), h.rbag.end());
-      flat.insert(flat.end(), h.node.begin(), h.node.end());
+      const HostDef& h = defs[f];
+      std::vector<Pair> links, nodes;
+      uint32_t vars_len = 0;
+      join_links(h, links, nodes, vars_len);
+      hdr[f] = DefHdr{h.node_len, (uint32_t)links.size(), vars_len, h.safe ? 1u : 0u, 0, (uint32_t)flat.size(), 1, 0};
+      flat.insert(flat.end(), links.begin(), links.end());
+      flat.insert(flat.end(), nodes.begin(), nodes.end());
       if (h.node_len > max_def_nodes) max_def_nodes = h.node_len;
-      if (h.vars_len > max_def_vars) max_def_vars = h.vars_len;
+      if (vars_len > max_def_vars) max_def_vars = vars_len;
     }
     if (flat.empty()) flat.push_back(0);
     if (mem_defs) cudaFree(mem_defs);
