@@ -70,13 +70,25 @@ def batch_check(res, gold_nets) -> bool:
     return all(numb_u24(p) == int(g["result"]) for p, g in zip(res, gold_nets))
 
 
-def bench_batch(hvm, W, args, plain_sample: int = 128) -> dict:
+def learned_weights():
+    return importlib.import_module("lambdavm-rust_gb300.train_policy").load_weights()
+
+
+def set_policy(hvm, rt, policy: str) -> None:
+    if policy == "learned":
+        rt.set_policy(hvm.POLICY_LEARNED, weights=learned_weights())
+    else:
+        rt.set_policy(hvm.POLICY_FIXED)
+
+
+def bench_batch(hvm, W, args, plain_sample: int = 128, policy: str = "fixed", cfg: dict | None = None) -> dict:
     """Config 4: the 4096-net mixed batch through continuous batching, and the
     plain path (one net per evaluation) on an evenly spaced sample of it."""
     gold = json.load(open(BATCH_GOLDEN))
     nets = W.mixed_batch(gold["count"])
     books = [hvm.book_from_text(code) for code, _ in nets]
-    rt = hvm.Runtime(device=0)
+    rt = hvm.Runtime(device=0, **(cfg or {}))
+    set_policy(hvm, rt, policy)
     rt.load_batch(books)
     for _ in range(max(1, args.warmup // 3)):
         st, done, res = rt.run_stream(max_inflight=BATCH_INFLIGHT, live_frac=BATCH_LIVE_FRAC)
@@ -87,6 +99,13 @@ def bench_batch(hvm, W, args, plain_sample: int = 128) -> dict:
         secs.append(time.perf_counter() - t0)
         ok = ok and st.itrs == gold["total_itrs"] and batch_check(res, gold["nets"])
     batched = gold["total_itrs"] / statistics.median(secs)
+    out = {"nets": gold["count"], "itrs": gold["total_itrs"], "value": batched, "unit": UNIT,
+           "seconds": statistics.median(secs), "p50_done_s": float(sorted(done)[len(done) // 2]),
+           "max_done_s": float(done.max()), "max_inflight": BATCH_INFLIGHT, "live_frac": BATCH_LIVE_FRAC,
+           "parity": bool(ok), "policy": policy, "config": cfg or {}}
+    if not plain_sample:
+        rt.close()
+        return out
     # plain: nets one at a time through the single-net path
     step = max(1, len(books) // plain_sample)
     t0 = time.perf_counter()
@@ -98,12 +117,40 @@ def bench_batch(hvm, W, args, plain_sample: int = 128) -> dict:
         ok = ok and s.itrs == gold["nets"][k]["itrs"]
     plain = p_itrs / (time.perf_counter() - t0)
     rt.close()
-    return {"nets": gold["count"], "itrs": gold["total_itrs"], "value": batched, "unit": UNIT,
-            "seconds": statistics.median(secs), "p50_done_s": float(sorted(done)[len(done) // 2]),
-            "max_done_s": float(done.max()), "max_inflight": BATCH_INFLIGHT, "live_frac": BATCH_LIVE_FRAC,
-            "plain_kernel": {"value": plain, "sample_nets": len(range(0, len(books), step)),
-                             "note": "same nets, one per evaluation (single-net path)"},
-            "batched_over_plain": batched / plain, "parity": bool(ok), "policy": "fixed"}
+    out["plain_kernel"] = {"value": plain, "sample_nets": len(range(0, len(books), step)),
+                           "note": "same nets, one per evaluation (single-net path)"}
+    out["batched_over_plain"] = batched / plain
+    out["parity"] = bool(ok)
+    return out
+
+
+def bench_scheduler(hvm, W, reps: int = 5) -> dict:
+    """Config 3: the skewed fold over 2^18 countdowns under the fixed and the
+    learned turn policy (median wall time of `reps` evaluations each, book
+    resident; every run checked against the reference's interaction count and
+    normal form)."""
+    golden = json.load(open(GOLDEN))["skewed_fold_2p18"]
+    book = hvm.book_from_text(W.skewed_fold(18))
+    out = {"workload": "fold over 2^18 geometric-length countdowns (p = 1/64, cap 2^16), single net",
+           "itrs": golden["itrs"]}
+    for policy in ("fixed", "learned"):
+        with hvm.Runtime(device=0) as rt:
+            set_policy(hvm, rt, policy)
+            rt.load(book)
+            st = rt.run()
+            ok = st.itrs == golden["itrs"] and \
+                hashlib.sha256(hvm.canonical(rt.result()).encode()).hexdigest() == golden["canonical_sha256"]
+            ms = []
+            for _ in range(reps):
+                t0 = time.perf_counter()
+                st = rt.run()
+                ms.append((time.perf_counter() - t0) * 1e3)
+                ok = ok and st.itrs == golden["itrs"]
+            med = statistics.median(ms)
+            out[policy] = {"value": golden["itrs"] / med * 1e3, "unit": UNIT, "ms": med, "turns": st.turns,
+                           "parity": bool(ok)}
+    out["learned_over_fixed"] = out["learned"]["value"] / out["fixed"]["value"]
+    return out
 
 
 def bench_serving(hvm, W, rates=(1e2, 1e3, 1e4, 1e5), seconds: float = 2.0, max_requests: int = 100_000) -> dict:
@@ -425,7 +472,16 @@ def main():
         import torch
         torch.cuda.set_device(local)
         if args.workload == "batch_mixed_4096":
-            b = bench_batch(hvm, W, args)
+            # Autotune on a 512-net sample of the batch, then run the whole batch.
+            at = importlib.import_module("lambdavm-rust_gb300.autotune")
+            gold = json.load(open(BATCH_GOLDEN))
+            sample = [hvm.book_from_text(code) for code, _ in W.mixed_batch(gold["count"])[:512]]
+            space = {"reg_cap_blocks": (0, 8), "graph_turns": (0, 4), "policy": ("fixed", "learned")}
+            best, rows = at.tune_batch(sample, BATCH_INFLIGHT, BATCH_LIVE_FRAC, space=space)
+            policy = best.pop("policy")
+            b = bench_batch(hvm, W, args, policy=policy, cfg=best)
+            b["autotune"] = {"sample_nets": len(sample), "space": space,
+                             "rows": [{**r["candidate"], "seconds": r["seconds"]} for r in rows]}
             line = {"metric": METRIC, "value": b["value"], "unit": UNIT, "n_gpus": 1, "steps": max(1, args.steps // 10),
                     "warmup": max(1, args.warmup // 3), "ms_per_step": b["seconds"] * 1e3, "higher_is_better": True,
                     "scaling": "weak", "vs_baseline": None, "dtype": "u32", "data": "synthetic",
@@ -450,6 +506,8 @@ def main():
         line = bench_gpu(args, hvm, book, golden, desc, ws, rank, local, dist)
         if line is not None and not args.no_batch:
             line["batched"] = bench_batch(hvm, W, args)
+            line["batched_learned"] = bench_batch(hvm, W, args, plain_sample=0, policy="learned")
+            line["scheduler"] = bench_scheduler(hvm, W)
     finally:
         dist.close()
     if line:

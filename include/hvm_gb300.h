@@ -75,6 +75,8 @@ typedef struct {
   uint32_t trace_cap;         /* record up to this many turns (0 = off), see hvm_gb300_trace */
   uint32_t reg_cap_blocks;    /* 0, or 8/12/16: cap registers so that many 128-thread blocks fit per SM */
   uint32_t profile;           /* 1 = collect per-warp round counters into hvm_gb300_stats.prof */
+  uint32_t graph_turns;       /* 0 = one launch per turn; k > 0 = turns run as replays of a CUDA
+                                 graph of k launches (captured once per loaded book/batch) */
 } hvm_gb300_config;
 
 typedef struct {

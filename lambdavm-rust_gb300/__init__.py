@@ -43,6 +43,7 @@ class Config(ctypes.Structure):
         ("trace_cap", ctypes.c_uint32),
         ("reg_cap_blocks", ctypes.c_uint32),
         ("profile", ctypes.c_uint32),
+        ("graph_turns", ctypes.c_uint32),
     ]
 
 

@@ -58,16 +58,63 @@ def _compile(src: str) -> str:
     return obj
 
 
+STANDALONE_ROOT = "runtime.cu"
+STANDALONE_INC = os.path.join(BUILD, "standalone_source.inc")
+RAW_DELIM = "HVMGB300SRC"
+
+
+def standalone_source() -> str:
+    """The evaluator runtime as one CUDA translation unit: runtime.cu with
+    every local `#include "..."` replaced by the file's text (each file once),
+    for `hvm gen-cu` to print around an embedded book."""
+    seen: set[str] = set()
+
+    def expand(name: str) -> str:
+        for d in (CSRC, INCLUDE):
+            path = os.path.join(d, name)
+            if os.path.exists(path):
+                break
+        else:
+            raise FileNotFoundError(name)
+        if path in seen:
+            return ""
+        seen.add(path)
+        out = []
+        for line in open(path).read().splitlines():
+            st = line.strip()
+            if st == "#pragma once":
+                continue
+            if st.startswith('#include "') and st.endswith('"'):
+                out.append(expand(st[len('#include "'):-1]))
+                continue
+            out.append(line)
+        return "\n".join(out)
+
+    src = expand(STANDALONE_ROOT)
+    if ")" + RAW_DELIM + '"' in src:
+        raise RuntimeError("raw-string delimiter occurs in the sources")
+    return src
+
+
+def _write_standalone() -> None:
+    text = 'static const char HVM_STANDALONE_SOURCE[] = R"' + RAW_DELIM + "(" + standalone_source() + ")" + \
+        RAW_DELIM + '";\n'
+    if not os.path.exists(STANDALONE_INC) or open(STANDALONE_INC).read() != text:
+        with open(STANDALONE_INC, "w") as f:
+            f.write(text)
+
+
 def build(verbose: bool = False) -> str:
     """Compiles the library and the CLI if any source changed; returns the library path."""
     os.makedirs(BUILD, exist_ok=True)
+    _write_standalone()
     with ThreadPoolExecutor(max_workers=max(2, len(LIB_SOURCES))) as ex:
         objs = list(ex.map(_compile, LIB_SOURCES))
     if _stale(LIB, objs):
         _run([NVCC, *ARCH, "-shared", "-o", LIB, *objs, "-lcudart"])
     cli_src = os.path.join(CSRC, "hvm_cli.cpp")
-    if os.path.exists(cli_src) and _stale(CLI, [cli_src, LIB] + _headers()):
-        _run([NVCC, *CXXFLAGS, "-o", CLI, cli_src, "-L" + PKG, "-lhvm_gb300",
+    if os.path.exists(cli_src) and _stale(CLI, [cli_src, LIB, STANDALONE_INC] + _headers()):
+        _run([NVCC, *CXXFLAGS, "-I" + BUILD, "-o", CLI, cli_src, "-L" + PKG, "-lhvm_gb300",
               "-Xlinker", "-rpath=$ORIGIN"])
     if verbose:
         print("built", LIB)

@@ -1,8 +1,13 @@
-// hvm_cli.cpp — command-line driver with the reference's `run-cu` surface
-// (src/main.rs:22-65, 93-96): `hvm run-cu FILE` parses the `.hvm` file,
-// serializes the Book and calls the C ABI `hvm_cu(book_buffer)`.
-// `hvm book FILE OUT` writes the serialized book buffer to OUT (the bytes the
-// reference passes across its C ABI), for feeding other runtimes.
+// hvm_cli.cpp — command-line driver with the reference's `run-cu` and
+// `gen-cu` surface (src/main.rs:22-65, 87-96, 128-155):
+//   hvm run-cu FILE    parses the `.hvm` file, serializes the Book and calls
+//                      the C ABI `hvm_cu(book_buffer)`;
+//   hvm gen-cu FILE    prints a standalone CUDA program: this runtime as one
+//                      translation unit, the serialized book as `BOOK_BUF`, and
+//                      a `main` that runs it (compile it with
+//                      `nvcc -gencode arch=compute_103a,code=sm_103a -O3 -std=c++17`);
+//   hvm book FILE OUT  writes the serialized book buffer to OUT (the bytes the
+//                      reference passes across its C ABI).
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
@@ -12,6 +17,7 @@
 #include <vector>
 
 #include "hvm_gb300.h"
+#include "standalone_source.inc"  // HVM_STANDALONE_SOURCE, generated by build.py
 
 static std::string read_file(const char* path) {
   std::ifstream f(path, std::ios::binary);
@@ -42,6 +48,7 @@ static void usage() {
           "HVM2 on GB300\n"
           "usage:\n"
           "  hvm run-cu <file.hvm>       evaluate @main on the GPU\n"
+          "  hvm gen-cu <file.hvm>       print a standalone CUDA program for the file\n"
           "  hvm book <file.hvm> <out>   write the serialized book buffer\n");
   exit(2);
 }
@@ -52,6 +59,18 @@ int main(int argc, char** argv) {
   if (cmd == "run-cu") {
     std::vector<uint32_t> buf = to_buffer(read_file(argv[2]));
     hvm_cu(buf.data());
+    return 0;
+  }
+  if (cmd == "gen-cu") {
+    // Like the reference's gen-cu, the book is embedded as a static buffer and
+    // the program's main evaluates it through hvm_cu.
+    std::vector<uint32_t> buf = to_buffer(read_file(argv[2]));
+    printf("// Generated by `hvm gen-cu %s`: the GB300 evaluator runtime with an embedded book.\n", argv[2]);
+    printf("// Build: nvcc -gencode arch=compute_103a,code=sm_103a -O3 -std=c++17 FILE.cu -o FILE\n\n");
+    fputs(HVM_STANDALONE_SOURCE, stdout);
+    printf("\n\nstatic const uint32_t BOOK_BUF[%zu] = {", buf.size());
+    for (size_t i = 0; i < buf.size(); i++) printf("%s%s%u", i ? "," : "", i % 16 ? "" : "\n  ", buf[i]);
+    printf("\n};\n\nint main() {\n  hvm_cu(BOOK_BUF);\n  return 0;\n}\n");
     return 0;
   }
   if (cmd == "book" && argc == 4) {

@@ -199,7 +199,7 @@ __global__ void __launch_bounds__(128, MIN_BLOCKS_128 > 0 ? MIN_BLOCKS_128 : 1) 
   __syncthreads();
   if (!sh_run) return;
   const unsigned long long base = sh_base, in_end = sh_end;
-  const uint32_t s = sh_s, budget = sh_budget, chunk = sh_chunk, stop_at = sh_stop_at;
+  const uint32_t s = sh_s, budget = sh_budget, stop_at = sh_stop_at;
 
   TState t;
   t.stk = (Pair*)smem_stack + threadIdx.x;
@@ -696,11 +696,18 @@ class Runtime {
   // Measurement: device time of turn kernels (events around each launch),
   // launches of this library's kernels, and bytes copied each way.
   std::vector<cudaEvent_t> events;
+  uint32_t timed_units = 0;             // event pairs recorded by the last launch_turns
+  // CUDA graph of `cfg.graph_turns` turn launches and the Dev it was captured with.
+  cudaGraphExec_t gexec = nullptr;
+  cudaStream_t cap_stream = nullptr;
+  Dev gdev{};
   double kernel_ms = 0;
   uint64_t turn_launches = 0, launches = 0, h2d_bytes = 0, d2h_bytes = 0;
 
   ~Runtime() {
     for (cudaEvent_t e : events) cudaEventDestroy(e);
+    if (gexec) cudaGraphExecDestroy(gexec);
+    if (cap_stream) cudaStreamDestroy(cap_stream);
     release();
   }
 
@@ -1019,6 +1026,61 @@ class Runtime {
     return 0;
   }
 
+  // Captures `cfg.graph_turns` turn launches into a CUDA graph for the
+  // current kernel arguments (the Dev block is passed by value, so a changed
+  // book or batch means a new capture).
+  int ensure_graph() {
+    if (gexec && memcmp(&gdev, &d, sizeof(Dev)) == 0) return 0;
+    if (gexec) { cudaGraphExecDestroy(gexec); gexec = nullptr; }
+    if (!cap_stream) CK(cudaStreamCreateWithFlags(&cap_stream, cudaStreamNonBlocking));
+    CK(cudaStreamBeginCapture(cap_stream, cudaStreamCaptureModeThreadLocal));
+    for (uint32_t i = 0; i < cfg.graph_turns; i++) turn_fn<<<grid, block, smem, cap_stream>>>(d, cap);
+    cudaGraph_t gr = nullptr;
+    CK(cudaStreamEndCapture(cap_stream, &gr));
+    cudaError_t e = cudaGraphInstantiate(&gexec, gr, 0);
+    cudaGraphDestroy(gr);
+    if (e != cudaSuccess) { gexec = nullptr; return fail(std::string("graph instantiation: ") + cudaGetErrorString(e)); }
+    memcpy(&gdev, &d, sizeof(Dev));
+    return 0;
+  }
+
+  // Launches at least n turns on the default stream: single launches, or
+  // replays of the captured graph of `cfg.graph_turns` launches. Each launch
+  // or replay is bracketed by an event pair that collect_times() reads once
+  // the host has synchronised.
+  int launch_turns(uint32_t n) {
+    const uint32_t g = cfg.graph_turns;
+    const uint32_t units = g ? (n + g - 1) / g : n;
+    while (events.size() < 2 * (size_t)units) {
+      cudaEvent_t e;
+      CK(cudaEventCreate(&e));
+      events.push_back(e);
+    }
+    if (g && ensure_graph()) return -1;
+    for (uint32_t i = 0; i < units; i++) {
+      CK(cudaEventRecord(events[2 * i]));
+      if (g) CK(cudaGraphLaunch(gexec, 0));
+      else turn_fn<<<grid, block, smem>>>(d, cap);
+      CK(cudaEventRecord(events[2 * i + 1]));
+    }
+    CK(cudaGetLastError());
+    const uint32_t k = g ? units * g : n;
+    turn_launches += k;
+    launches += k;
+    timed_units = units;
+    return 0;
+  }
+
+  int collect_times() {
+    for (uint32_t i = 0; i < timed_units; i++) {
+      float ms = 0;
+      CK(cudaEventElapsedTime(&ms, events[2 * i], events[2 * i + 1]));
+      kernel_ms += ms;
+    }
+    timed_units = 0;
+    return 0;
+  }
+
   // Runs turns until the ring is empty (src/hvm.cu:1810-1839).
   int normalize() {
     auto t0 = std::chrono::steady_clock::now();
@@ -1027,26 +1089,9 @@ class Runtime {
     unsigned long long last_itrs = ~0ull, last_pending = ~0ull;
     Ctl h;
     for (;;) {
-      while (events.size() < 2 * batch) {
-        cudaEvent_t e;
-        CK(cudaEventCreate(&e));
-        events.push_back(e);
-      }
-      for (uint32_t i = 0; i < batch; i++) {
-        CK(cudaEventRecord(events[2 * i]));
-        turn_fn<<<grid, block, smem>>>(d, cap);
-        CK(cudaEventRecord(events[2 * i + 1]));
-      }
-      CK(cudaGetLastError());
+      if (launch_turns(batch)) return -1;
       turns_run += batch;
-      turn_launches += batch;
-      launches += batch;
-      if (read_ctl(h)) return -1;
-      for (uint32_t i = 0; i < batch; i++) {
-        float ms = 0;
-        CK(cudaEventElapsedTime(&ms, events[2 * i], events[2 * i + 1]));
-        kernel_ms += ms;
-      }
+      if (read_ctl(h) || collect_times()) return -1;
       if (h.status) {
         std::string m = std::string("device error: ") + status_text(h.status) + " (info " + std::to_string(h.err_info) + ")";
         if (h.oom_space)
@@ -1251,12 +1296,8 @@ class Runtime {
         admitted_total += (uint32_t)admit.size();
       }
       // A few turns, then the control block.
-      const uint32_t batch = 4;
-      for (uint32_t i = 0; i < batch; i++) turn_fn<<<grid, block, smem>>>(d, cap);
-      CK(cudaGetLastError());
-      turn_launches += batch;
-      launches += batch;
-      if (read_ctl(h)) return -1;
+      if (launch_turns(4)) return -1;
+      if (read_ctl(h) || collect_times()) return -1;
       if (h.status) return fail(std::string("device error: ") + status_text(h.status));
       // Completions.
       if (!active.empty()) {
@@ -1475,6 +1516,7 @@ extern "C" void hvm_gb300_default_config(hvm_gb300_config* c) {
   c->stack_cap = 8;
   c->reg_cap_blocks = 8;
   c->trace_cap = 0;
+  c->graph_turns = 0;
 }
 
 extern "C" int hvm_gb300_create(const hvm_gb300_config* cfg, hvm_gb300_runtime** out) {

@@ -1,0 +1,60 @@
+"""`hvm gen-cu`: the standalone CUDA program emitter (the reference's
+src/main.rs:128-155 splices its runtime and the serialized book into one
+`.cu` file). The emitted program must compile on its own with nvcc for
+sm_103a and, on a GPU, print what `hvm run-cu` prints for the same file."""
+from __future__ import annotations
+
+import os
+import re
+import shutil
+import subprocess
+
+import pytest
+
+from conftest import parse_output
+
+NVCC = shutil.which("nvcc") or "/usr/local/cuda/bin/nvcc"
+NVCC_FLAGS = ["-gencode", "arch=compute_103a,code=sm_103a", "-O3", "-std=c++17"]
+
+
+def gen_cu(hvm, path) -> str:
+    return subprocess.run([hvm.CLI_PATH, "gen-cu", str(path)], capture_output=True, text=True,
+                          check=True).stdout
+
+
+def compile_cu(src: str, tmp_path, name: str) -> str:
+    cu = tmp_path / f"{name}.cu"
+    cu.write_text(src)
+    exe = str(tmp_path / name)
+    r = subprocess.run([NVCC, *NVCC_FLAGS, str(cu), "-o", exe], capture_output=True, text=True, timeout=600)
+    assert r.returncode == 0, r.stderr[-4000:]
+    return exe
+
+
+def test_gen_cu_embeds_the_book_and_compiles(hvm, tmp_path, ref_programs):
+    prog = next(p for p in ref_programs if p["name"] == "tests/programs/list.hvm")
+    src_file = tmp_path / "list.hvm"
+    src_file.write_text(prog["code"])
+    out = gen_cu(hvm, src_file)
+    # The book buffer is the same words the C ABI receives.
+    m = re.search(r"static const uint32_t BOOK_BUF\[(\d+)\] = \{([^}]*)\};", out)
+    assert m, "no BOOK_BUF in the emitted program"
+    words = [int(x) for x in m.group(2).replace("\n", " ").replace(",", " ").split()]
+    assert words == [int(w) for w in hvm.book_from_text(prog["code"])]
+    assert int(m.group(1)) == len(words)
+    assert "hvm_cu(BOOK_BUF)" in out
+    assert '#include "' not in out  # one translation unit, no local headers needed
+    compile_cu(out, tmp_path, "list")
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("name", ["tests/programs/list.hvm", "tests/programs/numerics/f24.hvm",
+                                  "examples/tuples/tuples.hvm"])
+def test_gen_cu_program_matches_run_cu(hvm, tmp_path, ref_programs, name):
+    prog = next(p for p in ref_programs if p["name"] == name)
+    src_file = tmp_path / "prog.hvm"
+    src_file.write_text(prog["code"])
+    exe = compile_cu(gen_cu(hvm, src_file), tmp_path, "prog")
+    got = parse_output(subprocess.run([exe], capture_output=True, text=True, check=True, timeout=300).stdout)
+    assert got["itrs"] == prog["itrs"]
+    assert hvm.canonical(got["result"]) == hvm.canonical(prog["result"])
