@@ -476,7 +476,7 @@ def main():
             at = importlib.import_module("lambdavm-rust_gb300.autotune")
             gold = json.load(open(BATCH_GOLDEN))
             sample = [hvm.book_from_text(code) for code, _ in W.mixed_batch(gold["count"])[:512]]
-            space = {"reg_cap_blocks": (0, 8), "graph_turns": (0, 4), "policy": ("fixed", "learned")}
+            space = {"reg_cap_blocks": (5, 8), "graph_turns": (0, 4), "policy": ("fixed", "learned")}
             best, rows = at.tune_batch(sample, BATCH_INFLIGHT, BATCH_LIVE_FRAC, space=space)
             policy = best.pop("policy")
             b = bench_batch(hvm, W, args, policy=policy, cfg=best)

@@ -44,6 +44,9 @@ class Config(ctypes.Structure):
         ("reg_cap_blocks", ctypes.c_uint32),
         ("profile", ctypes.c_uint32),
         ("graph_turns", ctypes.c_uint32),
+        ("node_page_log2", ctypes.c_uint32),
+        ("var_page_log2", ctypes.c_uint32),
+        ("max_pages", ctypes.c_uint32),
     ]
 
 

@@ -7,7 +7,7 @@ this module times a workload under each point of a small search space and
 returns the fastest configuration:
 
   reg_cap_blocks  register cap of the turn kernel (0 = none, about 3 blocks of
-                  128 threads per SM; 8 = 64 registers, 8 blocks per SM)
+                  128 threads per SM; 5 or 8 = that many blocks per SM)
   stack_cap       redexes per thread in the shared-memory deque
   graph_turns     0 = one launch per turn; k = CUDA-graph replays of k turns
   policy          the fixed turn policy or the learned one
@@ -32,7 +32,7 @@ sys.path.insert(0, os.path.dirname(os.path.dirname(os.path.abspath(__file__))))
 hvm = importlib.import_module("lambdavm-rust_gb300")
 
 DEFAULT_SPACE = {
-    "reg_cap_blocks": (0, 8),
+    "reg_cap_blocks": (0, 5, 8),
     "stack_cap": (8, 16),
     "graph_turns": (0, 4),
     "policy": ("fixed", "learned"),

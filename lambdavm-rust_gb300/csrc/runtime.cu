@@ -687,6 +687,7 @@ class Runtime {
   size_t smem = 0;
   uint32_t max_def_nodes = 1, max_def_vars = 1;
   int sms = 0;
+  uint32_t max_pages = MAX_PAGES;        // page-list capacity per thread and space
   // Scheduler policy written into the control block at every reset.
   uint32_t policy_mode = POLICY_FIXED;
   float policy_const[6] = {-1.f, -1.f, -1.f, -1.f, -1.f, -1.f};
@@ -740,10 +741,10 @@ class Runtime {
     if (block > 128) return fail("threads_per_block must be <= 128");
     switch (cfg.reg_cap_blocks) {
       case 0: turn_fn = turn_kernel<0>; break;
+      case 5: turn_fn = turn_kernel<5>; break;
+      case 6: turn_fn = turn_kernel<6>; break;
       case 8: turn_fn = turn_kernel<8>; break;
-      case 12: turn_fn = turn_kernel<12>; break;
-      case 16: turn_fn = turn_kernel<16>; break;
-      default: return fail("reg_cap_blocks must be 0, 8, 12 or 16");
+      default: return fail("reg_cap_blocks must be 0, 5, 6 or 8");
     }
     CK(cudaFuncSetAttribute(turn_fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     int per_sm = 0;
@@ -763,11 +764,25 @@ class Runtime {
       while (l >= (int)min_log2 && (words >> l) < 2ull * nthreads) l--;
       return l < (int)min_log2 ? -1 : l;
     };
-    int nl = page_log2_for(n_nodes, 9, 5), vl = page_log2_for(n_vars, 10, 5);
+    if ((cfg.node_page_log2 && (cfg.node_page_log2 < 5 || cfg.node_page_log2 > 12)) ||
+        (cfg.var_page_log2 && (cfg.var_page_log2 < 5 || cfg.var_page_log2 > 12)))
+      return fail("node_page_log2/var_page_log2 must be 0 or in [5, 12]");
+    int nl = page_log2_for(n_nodes, cfg.node_page_log2 ? cfg.node_page_log2 : 9, 5);
+    int vl = page_log2_for(n_vars, cfg.var_page_log2 ? cfg.var_page_log2 : 10, 5);
     if (nl < 0 || vl < 0) return fail("node/var space too small for the thread count");
     d.nspace.page_log2 = (uint32_t)nl;
     d.vspace.page_log2 = (uint32_t)vl;
-    d.nspace.max_pages = d.vspace.max_pages = MAX_PAGES;
+    // Page-list capacity: by default enough for 2^15 node words and 2^16 var
+    // words per thread (64 pages of the default sizes), at least 64 pages.
+    uint32_t mp = cfg.max_pages;
+    if (!mp) {
+      uint32_t a = (1u << 15) >> nl, b = (1u << 16) >> vl;
+      mp = a > b ? a : b;
+      if (mp < MAX_PAGES) mp = MAX_PAGES;
+    }
+    if (mp > 4096) return fail("max_pages must be at most 4096");
+    max_pages = mp;
+    d.nspace.max_pages = d.vspace.max_pages = mp;
     d.npool_end = (uint32_t)(n_nodes >> nl);
     d.vpool_end = (uint32_t)(n_vars >> vl);
     d.node_mask = (uint32_t)(n_nodes - 1);
@@ -777,7 +792,7 @@ class Runtime {
     uint64_t ring_len = 1ull << cfg.ring_log2;
     CK(cudaMalloc(&mem_ring, ring_len * sizeof(Pair)));
     // Page lists + counts + positions + offsets, for both spaces.
-    CK(cudaMalloc(&mem_cur, 2ull * nthreads * (MAX_PAGES + 3) * sizeof(uint32_t)));
+    CK(cudaMalloc(&mem_cur, 2ull * nthreads * (max_pages + 3) * sizeof(uint32_t)));
     CK(cudaMalloc((void**)&ctl, sizeof(Ctl)));
     {
       // One free-page ring per space, as large as the space's page count.
@@ -794,7 +809,7 @@ class Runtime {
     d.ring_mask = ring_len - 1;
     uint32_t* w = (uint32_t*)mem_cur;
     for (PagedSpace* sp : {&d.nspace, &d.vspace}) {
-      sp->lists = w; w += (size_t)nthreads * MAX_PAGES;
+      sp->lists = w; w += (size_t)nthreads * max_pages;
       sp->counts = w; w += nthreads;
       sp->pos = w; w += nthreads;
       sp->off = w; w += nthreads;
@@ -1517,6 +1532,9 @@ extern "C" void hvm_gb300_default_config(hvm_gb300_config* c) {
   c->reg_cap_blocks = 8;
   c->trace_cap = 0;
   c->graph_turns = 0;
+  c->node_page_log2 = 0;
+  c->var_page_log2 = 0;
+  c->max_pages = 0;
 }
 
 extern "C" int hvm_gb300_create(const hvm_gb300_config* cfg, hvm_gb300_runtime** out) {
