@@ -472,12 +472,14 @@ def main():
         import torch
         torch.cuda.set_device(local)
         if args.workload == "batch_mixed_4096":
-            # Autotune on a 512-net sample of the batch, then run the whole batch.
+            # Autotune on the batch itself (one timed run per candidate after a
+            # warm-up run), then measure the whole batch with the winner.
             at = importlib.import_module("lambdavm-rust_gb300.autotune")
             gold = json.load(open(BATCH_GOLDEN))
-            sample = [hvm.book_from_text(code) for code, _ in W.mixed_batch(gold["count"])[:512]]
+            sample = [hvm.book_from_text(code) for code, _ in W.mixed_batch(gold["count"])]
             space = {"reg_cap_blocks": (5, 8), "graph_turns": (0, 4), "policy": ("fixed", "learned")}
             best, rows = at.tune_batch(sample, BATCH_INFLIGHT, BATCH_LIVE_FRAC, space=space)
+            best = dict(best)
             policy = best.pop("policy")
             b = bench_batch(hvm, W, args, policy=policy, cfg=best)
             b["autotune"] = {"sample_nets": len(sample), "space": space,

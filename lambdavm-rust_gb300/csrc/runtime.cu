@@ -20,6 +20,9 @@
 //     single-word reads, and the final tree is serialised by one gather
 //     kernel instead of a device printf (src/hvm.cu:2290-2297).
 #include <cuda_runtime.h>
+#include <dlfcn.h>
+#include <errno.h>
+#include <time.h>
 #include <algorithm>
 #include <chrono>
 #include <cmath>
@@ -38,6 +41,14 @@ namespace hvm {
 
 // Capacity of each thread's page list (pages of one space a thread may own).
 constexpr uint32_t MAX_PAGES = 64;
+constexpr uint32_t HOST_NODE_WORDS = 1u << 17;  // node words the host may write IO results into
+// IO encodings (src/run.c:32-60).
+constexpr uint32_t IO_MAGIC_0 = 0xD0CA11, IO_MAGIC_1 = 0xFF1FF1;
+constexpr uint32_t IO_CALL_TAG = 1;
+constexpr uint32_t RESULT_OK_TAG = 0, RESULT_ERR_TAG = 1;
+constexpr uint32_t IO_ERR_TYPE_TAG = 0, IO_ERR_NAME_TAG = 1, IO_ERR_INNER_TAG = 2;
+constexpr uint32_t LIST_NIL_TAG = 0, LIST_CONS_TAG = 1;
+constexpr uint32_t HOST_VAR_WORDS = 1u << 16;   // var words of the same
 // Batches: nets per batch (each takes one ROOT var at the top of the var
 // space) and definitions over all nets (REF vals have 28 bits).
 constexpr uint32_t MAX_BATCH = 1u << 20;
@@ -434,11 +445,11 @@ __global__ void reset_alloc_kernel(Dev d) {
   }
 }
 
-// Starts a normalisation from `redex` (src/hvm.cu:1488-1497): sets ROOT to
-// NONE and makes `redex` the only input of the next turn.
-__global__ void boot_kernel(Dev d, Pair redex, uint32_t cap) {
+// Starts a normalisation from `redex` (src/hvm.cu:1488-1497): sets the root
+// var (ROOT, or net k's ROOT var in a batch) to NONE and makes `redex` the
+// only input of the next turn.
+__global__ void boot_kernel(Dev d, Pair redex, Port root, uint32_t cap) {
   Ctl* c = d.ctl;
-  const Port root = get_snd(redex);  // ROOT, or net k's ROOT var in a batch
   if (get_tag(root) == VAR) d.vars[get_val(root) & d.vars_mask] = NONE;
   unsigned long long at = c->tail;
   d.ring[at & d.ring_mask] = redex;
@@ -687,6 +698,8 @@ class Runtime {
   size_t smem = 0;
   uint32_t max_def_nodes = 1, max_def_vars = 1;
   int sms = 0;
+  // Host injection region per space (0 = nodes, 1 = vars): [lo, hi) words, next candidate.
+  uint32_t host_lo[2] = {0, 0}, host_hi[2] = {0, 0}, host_next[2] = {0, 0};
   uint32_t max_pages = MAX_PAGES;        // page-list capacity per thread and space
   // Scheduler policy written into the control block at every reset.
   uint32_t policy_mode = POLICY_FIXED;
@@ -824,6 +837,22 @@ class Runtime {
     CK(cudaMemset(mem_vars, 0, (1ull << cfg.vars_log2) * sizeof(Port)));
     // The top `nroots` var words are ROOT vars: no page that holds one is handed out.
     d.vpool_end = (uint32_t)(((1ull << cfg.vars_log2) - nroots) >> d.vspace.page_log2);
+    // The last pages below each pool's end are the host's: IO results are
+    // written there (host_take), never by the device allocator.
+    {
+      const uint32_t hn = std::max(1u, HOST_NODE_WORDS >> d.nspace.page_log2);
+      const uint32_t hv = std::max(1u, HOST_VAR_WORDS >> d.vspace.page_log2);
+      const uint32_t nfull = (uint32_t)((1ull << cfg.node_log2) >> d.nspace.page_log2);
+      if (nfull <= d.nthreads + hn || d.vpool_end <= d.nthreads + hv) return fail("node/var space too small for the thread count");
+      d.npool_end = nfull - hn;
+      d.vpool_end -= hv;
+      host_lo[0] = d.npool_end << d.nspace.page_log2;
+      host_hi[0] = (uint32_t)std::min<uint64_t>((uint64_t)(d.npool_end + hn) << d.nspace.page_log2, d.node_mask);
+      host_lo[1] = d.vpool_end << d.vspace.page_log2;
+      host_hi[1] = (d.vpool_end + hv) << d.vspace.page_log2;
+      host_next[0] = host_lo[0];
+      host_next[1] = host_lo[1];
+    }
     if (d.vpool_end < d.nthreads) return fail("var space too small for this batch");
     CK(cudaMemset(ctl, 0, sizeof(Ctl)));
     if (cfg.profile) { uint32_t one = 1; CK(cudaMemcpy(&ctl->prof_on, &one, sizeof(one), cudaMemcpyHostToDevice)); }
@@ -1034,8 +1063,17 @@ class Runtime {
     return 0;
   }
 
+  // Pushes `redex` and resets `root` (the reference's boot_redex,
+  // src/hvm.c:1480-1486, which always resets ROOT).
+  int boot_root(Pair redex, Port root) {
+    boot_kernel<<<1, 1>>>(d, redex, root, cap);
+    CK(cudaGetLastError());
+    launches++;
+    return 0;
+  }
+
   int boot(Pair redex) {
-    boot_kernel<<<1, 1>>>(d, redex, cap);
+    boot_kernel<<<1, 1>>>(d, redex, get_snd(redex), cap);
     CK(cudaGetLastError());
     launches++;
     return 0;
@@ -1385,6 +1423,281 @@ class Runtime {
   }
 
   // boot @main ~ ROOT, then the IO loop without IO builtins (src/run.cu:857-925).
+  // ---- IO (src/run.c:32-810) ---------------------------------------------
+  //
+  // The program's ROOT is read back as a lambda-encoded IO constructor; an
+  // IO_CALL names a host function, its argument and a continuation. The host
+  // reads the argument back, runs the function, writes its result into the
+  // net (the host injection region, one copy per structure) and boots
+  // `(result, ROOT) ~ continuation`, until an IO_DONE (or anything else).
+
+  // A run of n free words of one space in the host region (0 = nodes,
+  // 1 = vars): candidates are read back once and must all be 0 (free).
+  int host_take(int sp, uint32_t n, uint32_t& base) {
+    const uint32_t span = host_hi[sp] - host_lo[sp];
+    if (n == 0 || n > span) return fail("IO result larger than the host injection region");
+    std::vector<uint64_t> w(n);
+    for (uint32_t moved = 0; moved <= 2 * span;) {
+      uint32_t at = host_next[sp];
+      if (at + n > host_hi[sp]) { moved += host_hi[sp] - at; host_next[sp] = host_lo[sp]; continue; }
+      if (sp == 0) CK(cudaMemcpy(w.data(), d.node + at, n * sizeof(Pair), cudaMemcpyDeviceToHost));
+      else {
+        std::vector<uint32_t> v(n);
+        CK(cudaMemcpy(v.data(), d.vars + at, n * sizeof(Port), cudaMemcpyDeviceToHost));
+        for (uint32_t i = 0; i < n; i++) w[i] = v[i];
+      }
+      d2h_bytes += (uint64_t)n * (sp == 0 ? sizeof(Pair) : sizeof(Port));
+      uint32_t last = n;
+      for (uint32_t i = 0; i < n; i++) if (w[i]) last = i;
+      if (last == n) { base = at; host_next[sp] = at + n; return 0; }
+      host_next[sp] = at + last + 1;
+      moved += last + 1;
+    }
+    return fail("IO host injection region is full");
+  }
+
+  // Builds a small net on the host: nodes and vars numbered locally, written
+  // into the host region in one copy each by commit(). A port is either one
+  // of the net's own ports (external) or a local node / local var.
+  struct LPort {
+    Port p;
+    uint8_t kind;  // 0 external, 1 local node (CON), 2 local var
+  };
+  struct Inject {
+    std::vector<std::pair<LPort, LPort>> nodes;
+    uint32_t nvars = 0;
+    LPort var() { return LPort{new_port(VAR, nvars++), 2}; }
+    LPort node(LPort a, LPort b) {
+      nodes.push_back({a, b});
+      return LPort{new_port(CON, (uint32_t)nodes.size() - 1), 1};
+    }
+  };
+  static LPort ext(Port p) { return LPort{p, 0}; }
+
+  // Places an Inject in the host region and returns where `p` landed.
+  int commit(Inject& in, LPort p, Port& out) {
+    uint32_t nb = 0, vb = 0;
+    if (!in.nodes.empty() && host_take(0, (uint32_t)in.nodes.size(), nb)) return -1;
+    if (in.nvars && host_take(1, in.nvars, vb)) return -1;
+    auto rel = [&](LPort q) -> Port {
+      if (q.kind == 1) return new_port(get_tag(q.p), nb + get_val(q.p));
+      if (q.kind == 2) return new_port(VAR, vb + get_val(q.p));
+      return q.p;
+    };
+    std::vector<Pair> ns(in.nodes.size());
+    for (size_t i = 0; i < ns.size(); i++) ns[i] = new_pair(rel(in.nodes[i].first), rel(in.nodes[i].second));
+    if (!ns.empty()) CK(cudaMemcpy(d.node + nb, ns.data(), ns.size() * sizeof(Pair), cudaMemcpyHostToDevice));
+    if (in.nvars) {
+      std::vector<Port> vs(in.nvars, NONE);
+      CK(cudaMemcpy(d.vars + vb, vs.data(), vs.size() * sizeof(Port), cudaMemcpyHostToDevice));
+    }
+    h2d_bytes += ns.size() * sizeof(Pair) + (uint64_t)in.nvars * sizeof(Port);
+    out = rel(p);
+    return 0;
+  }
+
+  // Lambda-encoded constructor lam t ((((t TAG) a0) a1) ...) (src/run.c:184-374):
+  // application nodes (arg, result) from the tag outwards, the innermost
+  // result and the lambda's body sharing one var.
+  static LPort ctr_in(Inject& in, uint32_t tag, const LPort* args, uint32_t n) {
+    LPort r = in.var();
+    LPort chain = r;
+    for (uint32_t i = n; i-- > 0;) chain = in.node(args[i], chain);
+    LPort first = in.node(ext(new_port(NUM, new_u24(tag))), chain);
+    return in.node(first, r);
+  }
+
+  int inject_bytes(const std::string& b, Port& out) {
+    Inject in;
+    LPort list = ctr_in(in, LIST_NIL_TAG, nullptr, 0);
+    for (size_t i = b.size(); i-- > 0;) {
+      LPort args[2] = {ext(new_port(NUM, new_u24((uint32_t)(uint8_t)b[i]))), list};
+      list = ctr_in(in, LIST_CONS_TAG, args, 2);
+    }
+    return commit(in, list, out);
+  }
+  int inject_ctr(uint32_t tag, Port a, Port& out) {
+    Inject in;
+    LPort arg = ext(a);
+    return commit(in, ctr_in(in, tag, &arg, 1), out);
+  }
+  int inject_ok(Port v, Port& out) { return inject_ctr(RESULT_OK_TAG, v, out); }
+  int inject_io_err(uint32_t err_tag, Port val, Port& out) {
+    Inject in;
+    LPort v = ext(val);
+    LPort e = err_tag <= IO_ERR_NAME_TAG ? ctr_in(in, err_tag, nullptr, 0) : ctr_in(in, err_tag, &v, 1);
+    return commit(in, ctr_in(in, RESULT_ERR_TAG, &e, 1), out);
+  }
+  int inject_io_err_num(int32_t code, Port& out) { return inject_io_err(IO_ERR_INNER_TAG, new_port(NUM, new_i24(code)), out); }
+  int inject_io_err_str(const std::string& msg, Port& out) {
+    Port b;
+    if (inject_bytes(msg, b)) return -1;
+    return inject_io_err(IO_ERR_INNER_TAG, b, out);
+  }
+
+  // Readback of a right-nested tuple of at most `size` elements (src/run.c:99-117).
+  int read_tup(Port p, uint32_t size, std::vector<Port>& elems) {
+    elems.clear();
+    while (get_tag(p) == CON && elems.size() + 1 < size) {
+      Pair nd = node_load(get_val(p));
+      Port e;
+      if (expand(get_fst(nd), &e)) return -1;
+      elems.push_back(e);
+      if (expand(get_snd(nd), &p)) return -1;
+    }
+    elems.push_back(p);
+    return 0;
+  }
+
+  // Readback of a lambda-encoded list of u24 (src/run.c:119-182): each
+  // element is normalised in turn, the tail booted against ROOT.
+  int read_bytes(Port p, std::string& out) {
+    out.clear();
+    for (;;) {
+      if (normalize()) return -1;
+      Ctr c;
+      if (read_ctr(peek(p), c)) return -1;
+      if (c.tag == LIST_CONS_TAG && c.nargs == 2 && get_tag(c.args[0]) == NUM) {
+        out.push_back((char)get_u24(get_val(c.args[0])));
+        if (boot_root(new_pair(c.args[1], ROOT), ROOT)) return -1;
+        p = ROOT;
+        continue;
+      }
+      return 0;
+    }
+  }
+
+  FILE* io_file(Port p) {
+    if (get_tag(p) != NUM) {
+      fprintf(stderr, "non-num where file descriptor was expected: %i\n", get_tag(p));
+      return nullptr;
+    }
+    uint32_t fd = get_u24(get_val(p));
+    if (fd == 0) return stdin;
+    if (fd == 1) return stdout;
+    if (fd == 2) return stderr;
+    return fd < 256 ? io_files()[fd] : nullptr;
+  }
+  static FILE** io_files() { static FILE* files[256]; return files; }
+  static void** io_dylibs() { static void* libs[256]; return libs; }
+
+  // One IO function call (src/run.c:430-770); `ret` receives its result.
+  int io_call(const std::string& name, Port argm, Port& ret) {
+    std::vector<Port> tup;
+    if (name == "READ") {
+      if (read_tup(argm, 2, tup)) return -1;
+      if (tup.size() != 2) return inject_io_err(IO_ERR_TYPE_TAG, 0, ret);
+      FILE* fp = io_file(tup[0]);
+      uint32_t want = get_u24(get_val(tup[1]));
+      if (!fp) return inject_io_err_num(EBADF, ret);
+      std::string buf(want, '\0');
+      size_t got = fread(&buf[0], 1, want, fp);
+      if (got != want && ferror(fp)) return inject_io_err_num(ferror(fp), ret);
+      buf.resize(got);
+      Port b;
+      if (inject_bytes(buf, b)) return -1;
+      return inject_ok(b, ret);
+    }
+    if (name == "OPEN") {
+      if (read_tup(argm, 2, tup)) return -1;
+      if (tup.size() != 2) return inject_io_err(IO_ERR_TYPE_TAG, 0, ret);
+      std::string path, mode;
+      if (read_bytes(tup[0], path) || read_bytes(tup[1], mode)) return -1;
+      for (uint32_t fd = 3; fd < 256; fd++) {
+        if (io_files()[fd] == nullptr) {
+          io_files()[fd] = fopen(path.c_str(), mode.c_str());
+          if (!io_files()[fd]) return inject_io_err_num(errno, ret);
+          return inject_ok(new_port(NUM, new_u24(fd)), ret);
+        }
+      }
+      return inject_io_err_num(EMFILE, ret);
+    }
+    if (name == "CLOSE") {
+      FILE* fp = io_file(argm);
+      if (!fp) return inject_io_err_num(EBADF, ret);
+      if (fclose(fp) != 0) return inject_io_err_num(ferror(fp), ret);
+      io_files()[get_u24(get_val(argm))] = nullptr;
+      return inject_ok(new_port(ERA, 0), ret);
+    }
+    if (name == "WRITE") {
+      if (read_tup(argm, 2, tup)) return -1;
+      if (tup.size() != 2) return inject_io_err(IO_ERR_TYPE_TAG, 0, ret);
+      FILE* fp = io_file(tup[0]);
+      std::string bytes;
+      if (read_bytes(tup[1], bytes)) return -1;
+      if (!fp) return inject_io_err_num(EBADF, ret);
+      if (fwrite(bytes.data(), 1, bytes.size(), fp) != bytes.size()) return inject_io_err_num(ferror(fp), ret);
+      return inject_ok(new_port(ERA, 0), ret);
+    }
+    if (name == "FLUSH") {
+      FILE* fp = io_file(argm);
+      if (!fp) return inject_io_err_num(EBADF, ret);
+      if (fflush(fp) != 0) return inject_io_err_num(ferror(fp), ret);
+      return inject_ok(new_port(ERA, 0), ret);
+    }
+    if (name == "SEEK") {
+      if (read_tup(argm, 3, tup)) return -1;
+      if (tup.size() != 3) return inject_io_err(IO_ERR_TYPE_TAG, 0, ret);
+      FILE* fp = io_file(tup[0]);
+      int32_t off = get_i24(get_val(tup[1]));
+      uint32_t whence = (uint32_t)get_i24(get_val(tup[2]));
+      if (!fp) return inject_io_err_num(EBADF, ret);
+      int cw = whence == 0 ? SEEK_SET : whence == 1 ? SEEK_CUR : whence == 2 ? SEEK_END : -1;
+      if (cw < 0) return inject_io_err(IO_ERR_TYPE_TAG, 0, ret);
+      if (fseek(fp, off, cw) != 0) return inject_io_err_num(ferror(fp), ret);
+      return inject_ok(new_port(ERA, 0), ret);
+    }
+    if (name == "GET_TIME") {
+      const uint64_t ns = (uint64_t)std::chrono::duration_cast<std::chrono::nanoseconds>(
+                              std::chrono::system_clock::now().time_since_epoch()).count();
+      Inject in;
+      LPort t = in.node(ext(new_port(NUM, new_u24((uint32_t)(ns >> 24) & 0xFFFFFFF))),
+                        ext(new_port(NUM, new_u24((uint32_t)(ns & 0xFFFFFFF)))));
+      Port tp;
+      if (commit(in, t, tp)) return -1;
+      return inject_ok(tp, ret);
+    }
+    if (name == "SLEEP") {
+      if (read_tup(argm, 2, tup)) return -1;
+      if (tup.size() != 2) return inject_io_err(IO_ERR_TYPE_TAG, 0, ret);
+      uint64_t ns = ((uint64_t)get_u24(get_val(tup[0])) << 24) | get_u24(get_val(tup[1]));
+      struct timespec ts;
+      ts.tv_sec = (time_t)(ns / 1000000000ull);
+      ts.tv_nsec = (long)(ns % 1000000000ull);
+      nanosleep(&ts, nullptr);
+      return inject_ok(new_port(ERA, 0), ret);
+    }
+    if (name == "DL_OPEN") {
+      if (read_tup(argm, 2, tup)) return -1;
+      std::string path;
+      if (read_bytes(tup[0], path)) return -1;
+      const int flags = get_u24(get_val(tup.size() > 1 ? tup[1] : 0)) ? RTLD_LAZY : RTLD_NOW;
+      for (uint32_t h = 0; h < 256; h++) {
+        if (io_dylibs()[h] == nullptr) {
+          io_dylibs()[h] = dlopen(path.c_str(), flags);
+          if (!io_dylibs()[h]) { const char* e = dlerror(); return inject_io_err_str(e ? e : "dlopen failed", ret); }
+          return inject_ok(new_port(NUM, new_u24(h)), ret);
+        }
+      }
+      return inject_io_err_str("too many open dylibs", ret);
+    }
+    if (name == "DL_CLOSE") {
+      if (get_tag(argm) != NUM || get_u24(get_val(argm)) >= 256 || !io_dylibs()[get_u24(get_val(argm))])
+        return inject_io_err(IO_ERR_TYPE_TAG, 0, ret);
+      void*& h = io_dylibs()[get_u24(get_val(argm))];
+      if (dlclose(h) != 0) { const char* e = dlerror(); return inject_io_err_str(e ? e : "dlclose failed", ret); }
+      h = nullptr;
+      return inject_ok(new_port(ERA, 0), ret);
+    }
+    if (name == "DL_CALL") {
+      // The reference hands the library its own CPU net structures
+      // (src/run.c:716-739); a device-resident net has no such ABI.
+      return inject_io_err_str("DL_CALL is not available with the GPU runtime", ret);
+    }
+    return inject_io_err(IO_ERR_NAME_TAG, 0, ret);
+  }
+
+  // The IO loop around normalisation (src/run.c:778-810).
   int run_main() {
     if (defs.empty()) return fail("no book loaded");
     if (reset_net()) return -1;
@@ -1396,9 +1709,22 @@ class Runtime {
       if (read_ctr(peek(ROOT), c)) return -1;
       if (c.nargs < 1 || get_tag(c.args[0]) != CON) break;
       Pair magic = node_load(get_val(c.args[0]));
-      if (get_val(get_fst(magic)) != new_u24(0xD0CA11) || get_val(get_snd(magic)) != new_u24(0xFF1FF1)) break;
-      if (c.tag == 1) fprintf(stderr, "IO calls are not supported by this runtime\n");
-      break;
+      if (get_val(get_fst(magic)) != new_u24(IO_MAGIC_0) || get_val(get_snd(magic)) != new_u24(IO_MAGIC_1)) break;
+      if (c.tag != IO_CALL_TAG) break;  // IO_DONE
+      if (c.nargs != 4) {
+        fprintf(stderr, "invalid IO_CALL: args_len = %u\n", c.nargs);
+        break;
+      }
+      const Port argm = c.args[2], cont = c.args[3];
+      std::string name;
+      if (read_bytes(c.args[1], name)) return -1;
+      Port ret;
+      if (io_call(name, argm, ret)) return -1;
+      Inject in;
+      LPort loc = in.node(ext(ret), ext(ROOT));
+      Port lp;
+      if (commit(in, loc, lp)) return -1;
+      if (boot_root(new_pair(lp, cont), ROOT)) return -1;
     }
     return 0;
   }
@@ -1858,7 +2184,7 @@ static int normalize(Ctx& x) {
 }
 
 static int boot(Ctx& x, Pair redex) {
-  boot_kernel<<<1, 1>>>(x.d, redex, CAP);
+  boot_kernel<<<1, 1>>>(x.d, redex, get_snd(redex), CAP);
   return cuda_ok(x, cudaGetLastError());
 }
 

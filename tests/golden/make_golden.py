@@ -13,6 +13,12 @@ reference sources exist; the fixtures travel, the reference does not).
   batch_mixed_4096.json    per net of the 4096-net mixed batch
                            (workloads.mixed_batch): its family and size, the
                            reference C runtime's interaction count and result.
+  io_programs.json         the reference's IO programs (tests/programs/io,
+                           examples/demo_io) run by the reference C runtime
+                           in a scratch directory holding the files they
+                           open, with the test harness's stdin
+                           (tests/run.rs:79-96): printed lines, `Result:`,
+                           `- ITRS:`, and the snapshot's text.
   configs.json             the same two fields for the seeded benchmark
                            workloads (lambdavm-rust_gb300/workloads.py), with
                            large results stored as a SHA-256 of their
@@ -20,7 +26,7 @@ reference sources exist; the fixtures travel, the reference does not).
                            evaluation counted by the oracle (-w), the
                            roofline numerator.
 
-Usage: python tests/golden/make_golden.py [--reference /root/reference]
+Usage: python tests/golden/make_golden.py [--reference /root/reference] [--only-io | --only-batch]
 """
 from __future__ import annotations
 
@@ -73,6 +79,46 @@ def run_ref(code: str) -> dict:
     return {"result": res.group(1), "itrs": int(itrs.group(1))}
 
 
+# Files the IO programs open, relative to their working directory: the first
+# 47 bytes of LICENSE are what tests/programs/io/basic.hvm prints.
+IO_FILES = {"LICENSE": " " * 33 + "Apache License\n", "README.md": "# readme\n"}
+IO_STDIN = "io from the tests\n"
+
+
+def run_ref_io(code: str) -> dict:
+    buf = H.book_from_text(code)
+    with tempfile.TemporaryDirectory() as cwd:
+        for name, text in IO_FILES.items():
+            with open(os.path.join(cwd, name), "w") as f:
+                f.write(text)
+        path = os.path.join(cwd, "book.bin")
+        buf.tofile(path)
+        r = subprocess.run([REF_BIN, path], capture_output=True, text=True, timeout=600, cwd=cwd, input=IO_STDIN)
+    res = re.search(r"^Result: (.*)$", r.stdout, re.M)
+    itrs = re.search(r"^- ITRS: (\d+)$", r.stdout, re.M)
+    if r.returncode != 0 or not res or not itrs:
+        raise RuntimeError(f"reference run failed: rc={r.returncode}\n{r.stdout[-2000:]}\n{r.stderr[-2000:]}")
+    printed = r.stdout[:res.start()]
+    return {"printed": printed, "result": res.group(1), "itrs": int(itrs.group(1))}
+
+
+def make_io(ref: str) -> None:
+    out = []
+    files = sorted(glob.glob(os.path.join(ref, "tests", "programs", "io", "*.hvm"))
+                   + glob.glob(os.path.join(ref, "examples", "demo_io", "*.hvm")))
+    for path in files:
+        rel = os.path.relpath(path, ref)
+        code = open(path).read()
+        key = rel.replace("tests/programs/", "").replace("examples/", "").replace("/", "__")
+        snap = os.path.join(ref, "tests", "snapshots", f"run__io_file@{key}.snap")
+        snapshot = open(snap).read().split("---\n", 2)[-1] if os.path.exists(snap) else None
+        entry = {"name": rel, "code": code, "snapshot": snapshot, **run_ref_io(code)}
+        out.append(entry)
+        print(rel, entry["itrs"], repr(entry["printed"][:60]))
+    with open(os.path.join(HERE, "io_programs.json"), "w") as f:
+        json.dump({"files": IO_FILES, "stdin": IO_STDIN, "programs": out}, f, indent=1)
+
+
 def _batch_entry(item):
     idx, code, info = item
     r = run_ref(code)
@@ -105,9 +151,14 @@ def main() -> None:
     ap.add_argument("--reference", default="/root/reference")
     ap.add_argument("--skip-configs", action="store_true")
     ap.add_argument("--only-batch", action="store_true")
+    ap.add_argument("--only-io", action="store_true")
     args = ap.parse_args()
     if args.only_batch:
         make_batch()
+        return
+    if args.only_io:
+        subprocess.run(["make", "-C", os.path.join(ROOT, "oracle"), "ref", f"REF_SRC={args.reference}/src"], check=True)
+        make_io(args.reference)
         return
     subprocess.run(["make", "-C", os.path.join(ROOT, "oracle"), "ref", f"REF_SRC={args.reference}/src"], check=True)
     subprocess.run(["make", "-C", os.path.join(ROOT, "oracle")], check=True)

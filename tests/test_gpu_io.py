@@ -1,0 +1,36 @@
+"""IO programs (the reference's tests/programs/io and examples/demo_io): the
+evaluator's IO loop reads each IO_CALL back from the device net, runs the host
+function (OPEN, READ, WRITE, CLOSE, ...) and writes its result into the net.
+Printed output, the normal form and the interaction count must equal the
+reference C runtime's on the same files and stdin (tests/golden/io_programs.json,
+made by make_golden.py --only-io; the reference harness is tests/run.rs:67-96)."""
+from __future__ import annotations
+
+import json
+import os
+import subprocess
+
+import pytest
+
+from conftest import GOLDEN, parse_output
+
+pytestmark = pytest.mark.gpu
+
+with open(os.path.join(GOLDEN, "io_programs.json")) as _f:
+    IO = json.load(_f)
+
+
+@pytest.mark.parametrize("prog", IO["programs"], ids=[p["name"] for p in IO["programs"]])
+def test_io_program_matches_reference(hvm, tmp_path, prog):
+    for name, text in IO["files"].items():
+        (tmp_path / name).write_text(text)
+    src = tmp_path / "prog.hvm"
+    src.write_text(prog["code"])
+    r = subprocess.run([hvm.CLI_PATH, "run-cu", str(src)], capture_output=True, text=True, cwd=tmp_path,
+                       input=IO["stdin"], timeout=300)
+    assert r.returncode == 0, r.stderr
+    got = parse_output(r.stdout)
+    printed = r.stdout[:r.stdout.index("Result: ")]
+    assert printed == prog["printed"]
+    assert got["itrs"] == prog["itrs"]
+    assert hvm.canonical(got["result"]) == hvm.canonical(prog["result"])
