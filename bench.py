@@ -430,6 +430,20 @@ def bench_gpu(args, hvm, book, golden, desc, ws, rank, local, dist):
         "interactions_per_launch": itrs_per_launch,
         "avg_launch_ms": counters.kernel_ms / max(1, turns_effective),
     }
+    # Second roofline: the model's atomic operations (node takes + var
+    # exchanges, counted by the oracle) against the measured atomicExch
+    # throughput at random addresses of a 64 MB region (L2-resident) and of
+    # a 2 GB one (the var space's size).
+    roofline_atomic = None
+    if golden.get("algorithmic_atomics"):
+        api = golden["algorithmic_atomics"] / golden["itrs"]
+        peak_l2 = hvm.atomic_peak(1 << 24, local) / 1e9
+        peak_far = hvm.atomic_peak(1 << 29, local) / 1e9
+        ach = api * itrs_total / kernel_s / 1e9 if kernel_s > 0 else None
+        roofline_atomic = {"bound": "l2_atomics", "achieved": ach, "peak": peak_l2, "unit": "Gatomic/s",
+                           "frac": ach / peak_l2 if ach else None, "peak_2gb_region": peak_far,
+                           "frac_of_2gb_region": ach / peak_far if ach else None,
+                           "atomics_per_interaction": api, "peak_source": "measured by hvm_gb300_atomic_peak"}
     # CPU baseline: the oracle port on this host's cores, one full evaluation.
     threads = os.cpu_count() or 1
     c_itrs, c_secs, _ = run_oracle(book, threads)
@@ -446,6 +460,7 @@ def bench_gpu(args, hvm, book, golden, desc, ws, rank, local, dist):
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
         "gpu_launches": launches,
         "roofline": roofline,
+        "roofline_atomic": roofline_atomic,
         "cpu_baseline": cpu,
         "clocks": clocks,
     }

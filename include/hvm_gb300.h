@@ -224,6 +224,13 @@ int hvm_gb300_policy_grad(int device, const float* weights, const float* x, cons
 int hvm_gb300_policy_train(int device, float* weights, const float* x, const float* t, const float* sw, size_t n,
                            uint32_t epochs, float lr, float* loss, char* err, size_t err_cap);
 
+/* Measures the device's atomic-exchange throughput (no reference counterpart;
+ * the denominator of the evaluator's atomic roofline): a full grid issues
+ * independent 32-bit atomicExch at pseudo-random addresses of a region of
+ * `region_words` (a power of two) words; `*exch_per_s` receives operations per
+ * second of device time. Allocates and frees the region. */
+int hvm_gb300_atomic_peak(int device, uint64_t region_words, double* exch_per_s, char* err, size_t err_cap);
+
 /* Zeroes the measurement counters of hvm_gb300_stats (kernel_ms, launches,
  * h2d/d2h bytes); they otherwise accumulate over the runtime's life. */
 void hvm_gb300_reset_counters(hvm_gb300_runtime* rt);

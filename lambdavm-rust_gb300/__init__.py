@@ -117,6 +117,7 @@ EXPORTED_SYMBOLS = (
     "hvm_gb300_policy_forward",
     "hvm_gb300_policy_grad",
     "hvm_gb300_policy_train",
+    "hvm_gb300_atomic_peak",
     "hvm_gb300_error",
     "hvm_gb300_destroy",
 )
@@ -169,6 +170,8 @@ def lib() -> ctypes.CDLL:
                                         ctypes.c_size_t]
     L.hvm_gb300_policy_train.argtypes = [ctypes.c_int, fp, fp, fp, fp, ctypes.c_size_t, ctypes.c_uint32,
                                          ctypes.c_float, fp, ctypes.c_char_p, ctypes.c_size_t]
+    L.hvm_gb300_atomic_peak.argtypes = [ctypes.c_int, ctypes.c_uint64, ctypes.POINTER(ctypes.c_double),
+                                        ctypes.c_char_p, ctypes.c_size_t]
     L.hvm_gb300_reset_counters.argtypes = [ctypes.c_void_p]
     L.hvm_gb300_reset_counters.restype = None
     L.hvm_gb300_error.argtypes = [ctypes.c_void_p]
@@ -449,6 +452,16 @@ def policy_train(weights, x, t, sw, epochs: int, lr: float = 1e-3, device: int =
                                     epochs, lr, ctypes.byref(loss), err, 512):
         raise HvmError(err.value.decode())
     return w, loss.value
+
+
+def atomic_peak(region_words: int = 1 << 24, device: int = 0) -> float:
+    """Measured 32-bit atomicExch operations per second at random addresses
+    of a region of `region_words` words (the atomic roofline's denominator)."""
+    v = ctypes.c_double()
+    err = _err_buf()
+    if lib().hvm_gb300_atomic_peak(device, region_words, ctypes.byref(v), err, 512):
+        raise HvmError(err.value.decode())
+    return v.value
 
 
 def run_text(code: str, device: int = 0, **cfg) -> tuple[str, RunStats]:

@@ -26,7 +26,7 @@ NVCC = os.environ.get("NVCC", "nvcc")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 CXXFLAGS = ["-O3", "-std=c++17", "-I" + INCLUDE, "-I" + CSRC]
 
-LIB_SOURCES = ["frontend.cpp", "runtime.cu", "mlp.cu"]
+LIB_SOURCES = ["frontend.cpp", "runtime.cu", "mlp.cu", "peaks.cu"]
 
 
 def _run(cmd: list[str]) -> None:

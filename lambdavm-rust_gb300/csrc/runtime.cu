@@ -71,17 +71,6 @@ static const char* status_text(uint32_t s) {
 
 __device__ __forceinline__ unsigned long long ldcg64(const unsigned long long* p) { return __ldcg(p); }
 
-__device__ __forceinline__ bool claim(const Dev& d, TState& t, unsigned long long in_end, uint32_t chunk) {
-  if (ldcg64(&d.ctl->head) >= in_end) return false;
-  unsigned long long h = atomicAdd(&d.ctl->head, (unsigned long long)chunk);
-  if (h >= in_end) return false;
-  unsigned long long e = h + chunk < in_end ? h + chunk : in_end;
-  for (unsigned long long i = h; i < e; i++) {
-    push(d, t, (Pair)__ldcg((const unsigned long long*)&d.ring[i & d.ring_mask]));
-  }
-  return true;
-}
-
 __device__ __forceinline__ unsigned long long warp_sum(unsigned long long v) {
   for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xFFFFFFFFu, v, o);
   return v;

@@ -253,7 +253,9 @@ static Worker** g_workers;
 static int g_count_bytes;
 static int g_precise;  /* -n: also print the normalisation time in ns */
 static u64 g_bytes;
+static u64 g_atomics;  /* node takes and var exchanges: the atomic operations of the model */
 #define COUNT(n) do { if (g_count_bytes) g_bytes += (n); } while (0)
+#define COUNT_ATOMIC() do { if (g_count_bytes) g_atomics++; } while (0)
 static u32 g_nthreads;
 static u64 g_node_slice, g_vars_slice;
 
@@ -301,10 +303,10 @@ static u32 grab_vars(Worker* w, u32 want) {
 
 static inline Pair node_get(u32 i) { return atomic_load_explicit(&g_net->node[i], memory_order_relaxed); }
 static inline void node_put(u32 i, Pair p) { COUNT(8); atomic_store_explicit(&g_net->node[i], p, memory_order_relaxed); }
-static inline Pair node_swap(u32 i, Pair p) { COUNT(16); return atomic_exchange_explicit(&g_net->node[i], p, memory_order_relaxed); }
+static inline Pair node_swap(u32 i, Pair p) { COUNT(16); COUNT_ATOMIC(); return atomic_exchange_explicit(&g_net->node[i], p, memory_order_relaxed); }
 static inline Port var_get(u32 i) { return atomic_load_explicit(&g_net->vars[i], memory_order_relaxed); }
 static inline void var_put(u32 i, Port p) { COUNT(4); atomic_store_explicit(&g_net->vars[i], p, memory_order_relaxed); }
-static inline Port var_swap(u32 i, Port p) { COUNT(8); return atomic_exchange_explicit(&g_net->vars[i], p, memory_order_relaxed); }
+static inline Port var_swap(u32 i, Port p) { COUNT(8); COUNT_ATOMIC(); return atomic_exchange_explicit(&g_net->vars[i], p, memory_order_relaxed); }
 
 /* Maps a def-local port to the freshly allocated slots (src/hvm.c:346-362). */
 static inline Port relocate(Worker* w, Port p) {
@@ -708,6 +710,6 @@ int main(int argc, char** argv) {
   printf("- TIME: %.2fs\n", secs);
   printf("- MIPS: %.2f\n", (double)itrs / secs / 1000000.0);
   if (g_precise) printf("- NORM_NS: %" PRIu64 "\n", t_norm - t0);
-  if (counted) printf("- BYTES: %" PRIu64 "\n", g_bytes);
+  if (counted) printf("- BYTES: %" PRIu64 "\n- ATOMICS: %" PRIu64 "\n", g_bytes, g_atomics);
   return 0;
 }

@@ -50,8 +50,9 @@ REF_BIN = os.path.join(ROOT, "oracle", "_ref", "hvm_ref")
 PORT_BIN = os.path.join(ROOT, "oracle", "_build", "hvm_oracle")
 
 
-def algorithmic_bytes(code: str) -> int:
-    """Word-touch bytes of the whole evaluation, counted by the oracle (-w)."""
+def algorithmic_counts(code: str) -> tuple[int, int]:
+    """Word-touch bytes and atomic operations (node takes + var exchanges) of
+    the whole evaluation, counted by the oracle (-w)."""
     buf = H.book_from_text(code)
     with tempfile.NamedTemporaryFile(suffix=".bin", delete=False) as f:
         buf.tofile(f.name)
@@ -60,7 +61,36 @@ def algorithmic_bytes(code: str) -> int:
         r = subprocess.run([PORT_BIN, "-w", path], capture_output=True, text=True, timeout=3600, check=True)
     finally:
         os.unlink(path)
-    return int(re.search(r"^- BYTES: (\d+)$", r.stdout, re.M).group(1))
+    return (int(re.search(r"^- BYTES: (\d+)$", r.stdout, re.M).group(1)),
+            int(re.search(r"^- ATOMICS: (\d+)$", r.stdout, re.M).group(1)))
+
+
+CONFIG_CASES = {
+    "tree_sum_d12": lambda: W.tree_sum(12),
+    "tree_sum_d20": lambda: W.tree_sum(20),
+    "bitonic_sort_2p8": lambda: W.bitonic_sort(8),
+    "bitonic_sort_2p12": lambda: W.bitonic_sort(12),
+    "bitonic_sort_2p16": lambda: W.bitonic_sort(16),
+    "skewed_fold_2p10": lambda: W.skewed_fold(10),
+    "skewed_fold_2p18": lambda: W.skewed_fold(18),
+    "countdown_100000": lambda: W.countdown(100000),
+}
+
+
+def config_code(name: str) -> str:
+    return CONFIG_CASES[name]()
+
+
+def refresh_counts() -> None:
+    """Recounts the algorithmic bytes and atomics of every entry of
+    configs.json (the reference's results in it are left as they are)."""
+    path = os.path.join(HERE, "configs.json")
+    cfg = json.load(open(path))
+    for name, entry in cfg.items():
+        entry["algorithmic_bytes"], entry["algorithmic_atomics"] = algorithmic_counts(config_code(name))
+        print(name, entry["algorithmic_bytes"], entry["algorithmic_atomics"])
+    with open(path, "w") as f:
+        json.dump(cfg, f, indent=1)
 
 
 def run_ref(code: str) -> dict:
@@ -152,7 +182,12 @@ def main() -> None:
     ap.add_argument("--skip-configs", action="store_true")
     ap.add_argument("--only-batch", action="store_true")
     ap.add_argument("--only-io", action="store_true")
+    ap.add_argument("--only-counts", action="store_true")
     args = ap.parse_args()
+    if args.only_counts:
+        subprocess.run(["make", "-C", os.path.join(ROOT, "oracle")], check=True)
+        refresh_counts()
+        return
     if args.only_batch:
         make_batch()
         return
@@ -185,22 +220,14 @@ def main() -> None:
 
     if args.skip_configs:
         return
-    cases = {
-        "tree_sum_d12": W.tree_sum(12),
-        "tree_sum_d20": W.tree_sum(20),
-        "bitonic_sort_2p8": W.bitonic_sort(8),
-        "bitonic_sort_2p12": W.bitonic_sort(12),
-        "bitonic_sort_2p16": W.bitonic_sort(16),
-        "skewed_fold_2p10": W.skewed_fold(10),
-        "skewed_fold_2p18": W.skewed_fold(18),
-        "countdown_100000": W.countdown(100000),
-    }
     out = {}
-    for name, code in cases.items():
+    for name in CONFIG_CASES:
+        code = config_code(name)
         r = run_ref(code)
         canon = H.canonical(r["result"])
+        nbytes, natomics = algorithmic_counts(code)
         entry = {"itrs": r["itrs"], "canonical_sha256": hashlib.sha256(canon.encode()).hexdigest(),
-                 "algorithmic_bytes": algorithmic_bytes(code)}
+                 "algorithmic_bytes": nbytes, "algorithmic_atomics": natomics}
         if len(r["result"]) <= 4096:
             entry["result"] = r["result"]
         out[name] = entry

@@ -113,3 +113,12 @@ def test_errors_are_reported_not_hung(hvm, workloads, ref_programs):
         r.load(workloads.countdown(100000))
         with pytest.raises(hvm.HvmError, match="turn budget"):
             r.run()
+
+
+def test_atomic_peak_probe(hvm):
+    # The atomic roofline's denominator: positive and of the right order for
+    # an L2 (between 1e8 and 1e13 random 32-bit exchanges per second).
+    v = hvm.atomic_peak(1 << 20)
+    assert 1e8 < v < 1e13
+    with pytest.raises(hvm.HvmError):
+        hvm.atomic_peak(1000)  # not a power of two
