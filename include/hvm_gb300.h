@@ -80,6 +80,8 @@ typedef struct {
   uint32_t node_page_log2;    /* allocator page of 2^k node words (0 = 9; 5..12) */
   uint32_t var_page_log2;     /* allocator page of 2^k var words (0 = 10; 5..12) */
   uint32_t max_pages;         /* pages a thread may own per space (0 = 2^15 node / 2^16 var words' worth) */
+  uint32_t steal_min;         /* a lane gives its oldest redex to an empty lane of its warp once it holds
+                                 this many (0 = 2) */
 } hvm_gb300_config;
 
 typedef struct {

@@ -47,6 +47,7 @@ class Config(ctypes.Structure):
         ("node_page_log2", ctypes.c_uint32),
         ("var_page_log2", ctypes.c_uint32),
         ("max_pages", ctypes.c_uint32),
+        ("steal_min", ctypes.c_uint32),
     ]
 
 

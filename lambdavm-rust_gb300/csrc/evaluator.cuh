@@ -141,6 +141,7 @@ struct Dev {
   uint32_t* vloc;             // CALL scratch: [max_def_vars][nthreads]
   uint32_t nthreads;
   uint32_t ndefs;
+  uint32_t steal_min;         // a lane gives a redex to an empty lane of its warp once it holds this many
   const DefHdr* defs;
   const Pair* book;
   Ctl* ctl;

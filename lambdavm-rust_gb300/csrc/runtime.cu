@@ -239,7 +239,7 @@ __global__ void __launch_bounds__(128, MIN_BLOCKS_128 > 0 ? MIN_BLOCKS_128 : 1) 
     // Intra-warp balancing: each empty lane takes the oldest redex of a lane
     // holding two or more (all in shared memory, no global traffic).
     unsigned want = __ballot_sync(0xFFFFFFFFu, t.len == 0);
-    unsigned give = __ballot_sync(0xFFFFFFFFu, t.len >= 2);
+    unsigned give = __ballot_sync(0xFFFFFFFFu, t.len >= d.steal_min);
     if (want && give) {
       // A giving lane whose fresh words are not yet fenced publishes them
       // before another lane can take a redex that points at them.
@@ -758,6 +758,8 @@ class Runtime {
 
     uint64_t n_nodes = 1ull << cfg.node_log2, n_vars = 1ull << cfg.vars_log2;
     d.nthreads = nthreads;
+    if (cfg.steal_min == 1 || cfg.steal_min > cap) return fail("steal_min must be 0 or in [2, stack_cap]");
+    d.steal_min = cfg.steal_min ? cfg.steal_min : 2;
     // Pages: a power of two of words, at most 512 node / 1024 var words, and
     // small enough that every thread starts with one page and at least as
     // many pages again remain in the pool.
@@ -845,7 +847,7 @@ class Runtime {
     if (d.vpool_end < d.nthreads) return fail("var space too small for this batch");
     CK(cudaMemset(ctl, 0, sizeof(Ctl)));
     if (cfg.profile) { uint32_t one = 1; CK(cudaMemcpy(&ctl->prof_on, &one, sizeof(one), cudaMemcpyHostToDevice)); }
-    uint32_t frac = cfg.stop_frac_q8 ? cfg.stop_frac_q8 : 128;
+    uint32_t frac = cfg.stop_frac_q8 ? cfg.stop_frac_q8 : 32;
     CK(cudaMemcpy(&ctl->stop_frac_q8, &frac, sizeof(frac), cudaMemcpyHostToDevice));
     if (write_policy()) return -1;
     if (cfg.trace_cap) {
@@ -1842,7 +1844,7 @@ extern "C" void hvm_gb300_default_config(hvm_gb300_config* c) {
   c->vars_log2 = 29;
   c->ring_log2 = 26;
   c->max_turns = 0;
-  c->stop_frac_q8 = 128;
+  c->stop_frac_q8 = 32;
   c->stack_cap = 8;
   c->reg_cap_blocks = 8;
   c->trace_cap = 0;
@@ -1850,6 +1852,7 @@ extern "C" void hvm_gb300_default_config(hvm_gb300_config* c) {
   c->node_page_log2 = 0;
   c->var_page_log2 = 0;
   c->max_pages = 0;
+  c->steal_min = 0;
 }
 
 extern "C" int hvm_gb300_create(const hvm_gb300_config* cfg, hvm_gb300_runtime** out) {
@@ -2314,6 +2317,7 @@ extern "C" int hvm_gb300_run_noalloc(const uint32_t* book, size_t words, uint32_
   d.nloc = nullptr;  // every def fits one chunk: the scratch tables are never used
   d.vloc = nullptr;
   d.nthreads = NTHREADS;
+  d.steal_min = 2;
   d.ndefs = book[0];
   d.defs = (const DefHdr*)(A + OFF_DEFS);
   d.book = (const Pair*)(A + OFF_BOOK);

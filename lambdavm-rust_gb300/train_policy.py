@@ -42,7 +42,7 @@ wl = importlib.import_module("lambdavm-rust_gb300.workloads")
 # fixed policy's choice.
 SEED_BUDGET = (-1.0, 0.0, 0.4, 1.0)
 WORK_BUDGET = (-1.0, 0.6)
-WORK_STOP = (0.0, -1.0, 1.0)
+WORK_STOP = (-1.0, 0.25, 0.5)
 WORK_SHARE = (-1.0, 0.5)
 
 
