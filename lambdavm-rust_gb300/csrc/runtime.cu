@@ -686,6 +686,9 @@ class Runtime {
   void (*turn_fn)(Dev, uint32_t) = nullptr;
   size_t smem = 0;
   uint32_t max_def_nodes = 1, max_def_vars = 1;
+  size_t defs_bytes = 0, book_bytes = 0, scratch_bytes = 0;  // capacities of mem_defs / mem_book / mem_scratch
+  std::string result_cache;            // the last run's `Result:` text (hvm_gb300_result)
+  bool result_valid = false;
   int sms = 0;
   // Host injection region per space (0 = nodes, 1 = vars): [lo, hi) words, next candidate.
   uint32_t host_lo[2] = {0, 0}, host_hi[2] = {0, 0}, host_next[2] = {0, 0};
@@ -725,6 +728,7 @@ class Runtime {
     mem_node = mem_vars = mem_ring = mem_cur = mem_scratch = mem_defs = mem_book = mem_trace = mem_roots = mem_free =
         mem_mains = nullptr;
     mem_policy = nullptr;
+    defs_bytes = book_bytes = scratch_bytes = 0;
     g_out = nullptr; g_kids = nullptr; g_info = nullptr; ctl = nullptr;
   }
 
@@ -824,6 +828,7 @@ class Runtime {
 
   // Clears the whole net (node/var words, ring, cursors, counters).
   int reset_net() {
+    result_valid = false;
     CK(cudaMemset(mem_node, 0, (1ull << cfg.node_log2) * sizeof(Pair)));
     CK(cudaMemset(mem_vars, 0, (1ull << cfg.vars_log2) * sizeof(Port)));
     // The top `nroots` var words are ROOT vars: no page that holds one is handed out.
@@ -1025,20 +1030,28 @@ class Runtime {
       if (vars_len > max_def_vars) max_def_vars = vars_len;
     }
     if (flat.empty()) flat.push_back(0);
-    if (mem_defs) cudaFree(mem_defs);
-    if (mem_book) cudaFree(mem_book);
-    if (mem_scratch) cudaFree(mem_scratch);
-    mem_defs = mem_book = mem_scratch = nullptr;
-    CK(cudaMalloc(&mem_defs, hdr.size() * sizeof(DefHdr)));
-    CK(cudaMalloc(&mem_book, flat.size() * sizeof(Pair)));
-    CK(cudaMemcpy(mem_defs, hdr.data(), hdr.size() * sizeof(DefHdr), cudaMemcpyHostToDevice));
-    CK(cudaMemcpy(mem_book, flat.data(), flat.size() * sizeof(Pair), cudaMemcpyHostToDevice));
-    h2d_bytes += hdr.size() * sizeof(DefHdr) + flat.size() * sizeof(Pair);
+    // Device buffers are kept between loads and grown only when a book needs
+    // more (cudaFree synchronises the device; a reload should not).
+    auto ensure = [&](void*& p, size_t& have, size_t need) -> int {
+      if (p && have >= need) return 0;
+      if (p) cudaFree(p);
+      p = nullptr;
+      have = 0;
+      CK(cudaMalloc(&p, need));
+      have = need;
+      return 0;
+    };
     // Relocation tables: for defs larger than a chunk, and as the fallback
     // when a CALL finds no contiguous run; so at least CHUNK words each.
     if (max_def_nodes < CHUNK) max_def_nodes = CHUNK;
     if (max_def_vars < CHUNK) max_def_vars = CHUNK;
-    CK(cudaMalloc(&mem_scratch, (size_t)(max_def_nodes + max_def_vars) * d.nthreads * sizeof(uint32_t)));
+    if (ensure(mem_defs, defs_bytes, hdr.size() * sizeof(DefHdr)) ||
+        ensure(mem_book, book_bytes, flat.size() * sizeof(Pair)) ||
+        ensure(mem_scratch, scratch_bytes, (size_t)(max_def_nodes + max_def_vars) * d.nthreads * sizeof(uint32_t)))
+      return -1;
+    CK(cudaMemcpy(mem_defs, hdr.data(), hdr.size() * sizeof(DefHdr), cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(mem_book, flat.data(), flat.size() * sizeof(Pair), cudaMemcpyHostToDevice));
+    h2d_bytes += hdr.size() * sizeof(DefHdr) + flat.size() * sizeof(Pair);
     d.tables = 1;
     d.defs = (const DefHdr*)mem_defs;
     d.book = (const Pair*)mem_book;
@@ -1127,6 +1140,7 @@ class Runtime {
 
   // Runs turns until the ring is empty (src/hvm.cu:1810-1839).
   int normalize() {
+    result_valid = false;  // the net changes
     auto t0 = std::chrono::steady_clock::now();
     uint32_t batch = 4;
     uint64_t turns_run = 0, stalled_turns = 0;
@@ -1998,8 +2012,12 @@ extern "C" int hvm_gb300_set_policy(hvm_gb300_runtime* r, uint32_t mode, const f
 
 extern "C" int hvm_gb300_result(hvm_gb300_runtime* r, char* out, size_t cap, size_t* len) {
   if (!r) return -1;
-  std::string s;
-  if (r->rt.result_text(s)) return -1;
+  hvm::Runtime& rt = r->rt;
+  if (!rt.result_valid) {  // computed once per run: a size query and the copy share it
+    if (rt.result_text(rt.result_cache)) return -1;
+    rt.result_valid = true;
+  }
+  const std::string& s = rt.result_cache;
   if (len) *len = s.size();
   if (out) {
     if (cap <= s.size()) { r->rt.fail("result buffer too small"); return -2; }
