@@ -298,7 +298,7 @@ __device__ __forceinline__ uint32_t runs_of(uint32_t m, uint32_t n) {
 // 0 when the page list is full and the pool is empty. Taken words are
 // written at once (vars as NONE, nodes as MARK) so no later scan can see them
 // free before their owner fills them.
-template <bool VARS>
+template <bool VARS, bool MARK = true>
 __device__ __forceinline__ uint32_t alloc_run(const Dev& d, TState& t, Alloc& a, uint32_t n, uint32_t soft_limit = 0) {
   const PagedSpace& sp = VARS ? d.vspace : d.nspace;
   const uint32_t page_words = 1u << sp.page_log2;
@@ -311,7 +311,8 @@ __device__ __forceinline__ uint32_t alloc_run(const Dev& d, TState& t, Alloc& a,
       a.mask &= ~((n == 32 ? ~0u : (1u << n) - 1) << b);
       uint32_t at = a.chunk + b;
       for (uint32_t i = 0; i < n; i++) {
-        if (VARS) vstore(d, at + i, NONE); else nstore(d, at + i, NODE_MARK);
+        if (VARS) vstore(d, at + i, NONE);
+        else if (MARK) nstore(d, at + i, NODE_MARK);
       }
       if (VARS) t.live_vars += n; else t.live_nodes += n;
       return at;
@@ -663,7 +664,9 @@ __device__ __forceinline__ int lockstep_round(const Dev& d, TState& t, bool has,
           // one and relocated through the per-thread tables.
           const uint32_t soft = d.tables ? SOFT_RUN_CHUNKS : 0;
           p.vbase = p.vars_len ? alloc_run<true>(d, t, t.va, p.vars_len, soft) : 0;
-          p.nbase = (p.node_len && (p.vbase || !p.vars_len)) ? alloc_run<false>(d, t, t.na, p.node_len, soft) : 0;
+          // The node run is the interaction's last node allocation and is
+          // filled right below, so its words need no mark.
+          p.nbase = (p.node_len && (p.vbase || !p.vars_len)) ? alloc_run<false, false>(d, t, t.na, p.node_len, soft) : 0;
           if ((p.vars_len && !p.vbase) || (p.node_len && !p.nbase)) {
             if (!d.tables) { rc = IR_FATAL; break; }
             if (p.vbase) {  // give back
