@@ -4,7 +4,8 @@ The reference schedules turns with a fixed SEED/GROW/WORK policy
 (src/hvm.cu:1509-1548); this runtime's fixed policy is its counterpart and the
 learned policy is trained to imitate the fastest schedule found per net:
 
-1. Every training net runs under the fixed policy and under a grid of constant
+1. Every training net (and, with --streams, two continuously batched slices
+   of the 4096-net mixed pool) runs under the fixed policy and under a grid of constant
    schedules (per regime: while fewer redexes than threads are pending, and
    otherwise), with per-turn tracing on. Each run records, at the close of every
    turn, the 16 scheduler features and the next turn's parameters in the
@@ -53,6 +54,13 @@ def constant_grid() -> list[tuple[float, ...]]:
     return grid
 
 
+def training_streams(n: int = 768) -> list[tuple[str, list[str]]]:
+    """Continuously batched streams: two slices of the 4096-net mixed pool
+    (the batch benchmark runs the whole pool)."""
+    pool = wl.mixed_batch(4096)
+    return [(f"stream_{n}_a", [c for c, _ in pool[:n]]), (f"stream_{n}_b", [c for c, _ in pool[2048:2048 + n]])]
+
+
 def training_nets() -> list[tuple[str, str]]:
     """Seeded nets of the benchmark families, none equal to a benchmark input."""
     nets = []
@@ -68,14 +76,38 @@ def training_nets() -> list[tuple[str, str]]:
     return nets
 
 
-def timed_run(rt, reps: int) -> tuple[float, object]:
-    """Best device time (ms) over `reps` runs, and the last run's stats."""
+# Continuous-batching settings of the batch benchmark.
+STREAM_INFLIGHT, STREAM_LIVE_FRAC = 512, 0.25
+
+
+def timed_run(rt, reps: int, stream: bool = False) -> tuple[float, object]:
+    """Best time (ms) over `reps` runs, and the last run's stats: device time
+    for a single net, wall time for a stream (admission is part of it)."""
     best, st = math.inf, None
     for _ in range(reps):
         rt.reset_counters()
-        st = rt.run()
-        best = min(best, st.kernel_ms)
+        if stream:
+            t0 = time.perf_counter()
+            st, _, res = rt.run_stream(max_inflight=STREAM_INFLIGHT, live_frac=STREAM_LIVE_FRAC)
+            best = min(best, (time.perf_counter() - t0) * 1e3)
+            st.results = tuple(int(p) for p in res)
+        else:
+            st = rt.run()
+            best = min(best, st.kernel_ms)
     return best, st
+
+
+def _load(rt, item) -> bool:
+    """Loads a single net (text) or a stream (list of texts); True for a stream."""
+    if isinstance(item, list):
+        rt.load_batch([hvm.book_from_text(c) for c in item])
+        return True
+    rt.load(item)
+    return False
+
+
+def _outcome(rt, st, stream: bool):
+    return (st.results, st.itrs) if stream else (rt.result(), st.itrs)
 
 
 def collect(nets, reps: int, trace_cap: int, log=print):
@@ -83,15 +115,15 @@ def collect(nets, reps: int, trace_cap: int, log=print):
     xs, ts, ws, report = [], [], [], []
     for name, code in nets:
         with hvm.Runtime(device=0, trace_cap=trace_cap) as rt:
-            rt.load(code)
+            stream = _load(rt, code)
             rt.set_policy(hvm.POLICY_FIXED)
-            fixed_ms, st0 = timed_run(rt, reps)
-            want = (rt.result(), st0.itrs)
+            fixed_ms, st0 = timed_run(rt, reps, stream)
+            want = _outcome(rt, st0, stream)
             best = (fixed_ms, None, rt.trace())
             for const in grid:
                 rt.set_policy(hvm.POLICY_CONSTANT, constants=const)
-                ms, st = timed_run(rt, reps)
-                if (rt.result(), st.itrs) != want:
+                ms, st = timed_run(rt, reps, stream)
+                if _outcome(rt, st, stream) != want:
                     raise RuntimeError(f"{name}: schedule {const} changed the result")
                 if ms < best[0]:
                     best = (ms, const, rt.trace())
@@ -127,13 +159,13 @@ def evaluate(nets, weights, reps: int, log=print) -> list[dict]:
     rows = []
     for name, code in nets:
         with hvm.Runtime(device=0) as rt:
-            rt.load(code)
+            stream = _load(rt, code)
             rt.set_policy(hvm.POLICY_FIXED)
-            fixed_ms, st0 = timed_run(rt, reps)
-            want = (rt.result(), st0.itrs)
+            fixed_ms, st0 = timed_run(rt, reps, stream)
+            want = _outcome(rt, st0, stream)
             rt.set_policy(hvm.POLICY_LEARNED, weights=weights)
-            ms, st = timed_run(rt, reps)
-            if (rt.result(), st.itrs) != want:
+            ms, st = timed_run(rt, reps, stream)
+            if _outcome(rt, st, stream) != want:
                 raise RuntimeError(f"{name}: learned schedule changed the result")
         rows.append({"net": name, "fixed_ms": round(fixed_ms, 3), "learned_ms": round(ms, 3),
                      "speedup": round(fixed_ms / ms, 3)})
@@ -149,9 +181,11 @@ def main() -> None:
     ap.add_argument("--lr", type=float, default=2e-3)
     ap.add_argument("--trace-cap", type=int, default=8192)
     ap.add_argument("--seed", type=int, default=1)
+    ap.add_argument("--streams", type=int, default=0,
+                    help="also train on two continuously batched streams of this many nets each")
     args = ap.parse_args()
     t0 = time.time()
-    nets = training_nets()
+    nets = training_nets() + (training_streams(args.streams) if args.streams else [])
     x, t, sw, report = collect(nets, args.reps, args.trace_cap)
     print(f"collected {len(x)} turns from {len(nets)} nets in {time.time() - t0:.1f} s")
     w0 = init_weights(args.seed)
