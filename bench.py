@@ -82,7 +82,7 @@ def set_policy(hvm, rt, policy: str) -> None:
 
 
 def bench_batch(hvm, W, args, plain_sample: int = 128, policy: str = "fixed", cfg: dict | None = None) -> dict:
-    """Config 4: the 4096-net mixed batch through continuous batching, and the
+    """The 4096-net mixed batch through continuous batching, and the
     plain path (one net per evaluation) on an evenly spaced sample of it."""
     gold = json.load(open(BATCH_GOLDEN))
     nets = W.mixed_batch(gold["count"])
@@ -125,7 +125,7 @@ def bench_batch(hvm, W, args, plain_sample: int = 128, policy: str = "fixed", cf
 
 
 def bench_scheduler(hvm, W, reps: int = 5) -> dict:
-    """Config 3: the skewed fold over 2^18 countdowns under the fixed and the
+    """The skewed fold over 2^18 countdowns under the fixed and the
     learned turn policy (median wall time of `reps` evaluations each, book
     resident; every run checked against the reference's interaction count and
     normal form)."""
@@ -154,7 +154,7 @@ def bench_scheduler(hvm, W, reps: int = 5) -> dict:
 
 
 def bench_serving(hvm, W, rates=(1e2, 1e3, 1e4, 1e5), seconds: float = 2.0, max_requests: int = 100_000) -> dict:
-    """Config 5: Poisson arrivals at each rate for about `seconds` of arrivals
+    """Serving: Poisson arrivals at each rate for about `seconds` of arrivals
     (at most `max_requests`), nets drawn from the 4096-net pool; latency =
     completion - arrival on the host clock; every response checked against
     the reference's result for its net."""

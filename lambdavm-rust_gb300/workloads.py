@@ -8,7 +8,7 @@ nodes split into REF'd sub-definitions of at most 31 CON nodes each (the
 reference CUDA loader rejects definitions with more than 64 nodes,
 src/hvm.cu:1922-1930).
 
-Configurations:
+Workloads:
   tree_sum(20)       sum(d) = d==0 ? 1 : sum(d-1)+sum(d-1)       -> 1048576
   bitonic_sort(16)   sort of 2^16 PCG32 u24 keys, returns the sorted tree
   skewed_fold(18)    2^18 countdown loops of Geometric(1/64) length capped
@@ -231,7 +231,7 @@ def poisson_arrivals(count: int, rate: float, seed: int = 0x5E21E) -> list[float
 
 def serving_requests(count: int, rate: float, pool: int = 4096, seed: int = 0x5E21E) -> tuple[list[float], list[int]]:
     """`count` requests arriving as a Poisson process of `rate`/s, each a net
-    drawn uniformly from the first `pool` nets of mixed_batch (the config-4
-    families). Returns (arrival times, template index per request)."""
+    drawn uniformly from the first `pool` nets of mixed_batch (the mixed
+    batch's families). Returns (arrival times, template index per request)."""
     rng = PCG32(seed ^ 0xA5A5A5A5, PCG_DEFAULT_SEQ)
     return poisson_arrivals(count, rate, seed), [rng.next() % pool for _ in range(count)]
