@@ -50,3 +50,27 @@ def test_committed_policy_weights_are_well_formed(hvm):
     w = train.load_weights()
     assert w.shape == (hvm.POLICY_PARAMS,)
     assert hvm.POLICY_PARAMS == 5443
+
+
+def test_ctypes_mirrors_match_the_header(hvm, tmp_path):
+    # The Python structs must have the C header's layout: compare sizes
+    # (and the offset of the last field) with a probe compiled against it.
+    import ctypes
+    import os
+    import shutil
+    import subprocess
+    cc = shutil.which("gcc") or shutil.which("cc")
+    if cc is None:
+        import pytest
+        pytest.skip("no C compiler")
+    inc = os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))), "include")
+    src = tmp_path / "probe.c"
+    src.write_text('#include <stdio.h>\n#include <stddef.h>\n#include "hvm_gb300.h"\n'
+                   'int main(void) { printf("%zu %zu %zu %zu %zu\\n", sizeof(hvm_gb300_config),'
+                   ' offsetof(hvm_gb300_config, turn_budget_cap), sizeof(hvm_gb300_stats),'
+                   ' sizeof(hvm_gb300_turn), offsetof(hvm_gb300_turn, outputs)); return 0; }\n')
+    exe = tmp_path / "probe"
+    subprocess.run([cc, "-I", inc, str(src), "-o", str(exe)], check=True)
+    got = [int(x) for x in subprocess.run([str(exe)], capture_output=True, text=True, check=True).stdout.split()]
+    assert got == [ctypes.sizeof(hvm.Config), hvm.Config.turn_budget_cap.offset, ctypes.sizeof(hvm._Stats),
+                   ctypes.sizeof(hvm.Turn), hvm.Turn.outputs.offset]
