@@ -82,6 +82,8 @@ typedef struct {
   uint32_t max_pages;         /* pages a thread may own per space (0 = 2^15 node / 2^16 var words' worth) */
   uint32_t steal_min;         /* a lane gives its oldest redex to an empty lane of its warp once it holds
                                  this many (0 = 2) */
+  uint32_t turn_budget_cap;   /* 0, or the most rounds a turn may run (default 1024): bounds how long a
+                                 stream waits between admissions and completion checks (serving latency) */
 } hvm_gb300_config;
 
 typedef struct {

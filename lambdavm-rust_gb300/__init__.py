@@ -48,6 +48,7 @@ class Config(ctypes.Structure):
         ("var_page_log2", ctypes.c_uint32),
         ("max_pages", ctypes.c_uint32),
         ("steal_min", ctypes.c_uint32),
+        ("turn_budget_cap", ctypes.c_uint32),
     ]
 
 

@@ -86,7 +86,9 @@ struct alignas(128) Ctl {
   unsigned int static_per_thread;   // ring items each thread takes at turn start
   unsigned int budget;              // interactions per thread per turn
   unsigned int chunk;               // items per dynamic claim
-  unsigned int pad_c[2];
+  unsigned int budget_cap;          // 0, or the most rounds a turn may run (bounds how long the
+                                    // host waits between admissions and completion checks)
+  unsigned int pad_c[1];
   unsigned long long hist[8];       // interactions per rule (diagnostic)
   unsigned long long prof[8];       // profile counters (when prof_on): see PROF_*
   unsigned int prof_on;

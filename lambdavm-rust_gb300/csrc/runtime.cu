@@ -105,7 +105,7 @@ __device__ void fixed_policy(Ctl* c, unsigned long long pending, unsigned long l
   unsigned long long keep = (busy * (256 - c->stop_frac_q8)) >> 8;  // busy threads that keep the turn going
   c->stop_at = (uint32_t)(nthreads - keep);
   c->static_per_thread = s;
-  c->budget = budget;
+  c->budget = c->budget_cap && budget > c->budget_cap ? c->budget_cap : budget;
   c->chunk = chunk;
 }
 
@@ -153,7 +153,10 @@ __device__ void policy_features(const Dev& d, unsigned long long pending, unsign
 __device__ void apply_policy(Ctl* c, const float* o, unsigned long long pending, uint32_t nthreads, uint32_t cap,
                              float* eff) {
   unsigned long long busy = pending < nthreads ? pending : nthreads;
-  if (o[0] >= 0.f && isfinite(o[0])) c->budget = 64u << (uint32_t)lrintf(fminf(o[0], 1.f) * 10.f);
+  if (o[0] >= 0.f && isfinite(o[0])) {
+    const uint32_t b = 64u << (uint32_t)lrintf(fminf(o[0], 1.f) * 10.f);
+    c->budget = c->budget_cap && b > c->budget_cap ? c->budget_cap : b;
+  }
   uint32_t frac = c->stop_frac_q8;
   if (o[1] >= 0.f && isfinite(o[1])) {
     frac = 32u + (uint32_t)(fminf(o[1], 1.f) * 192.f);
@@ -876,6 +879,8 @@ class Runtime {
     CK(cudaMemcpy(&ctl->policy_mode, &policy_mode, sizeof(policy_mode), cudaMemcpyHostToDevice));
     CK(cudaMemcpy(&ctl->policy_const, policy_const, sizeof(policy_const), cudaMemcpyHostToDevice));
     CK(cudaMemcpy(&ctl->policy_w, &w, sizeof(w), cudaMemcpyHostToDevice));
+    const uint32_t bc = cfg.turn_budget_cap;
+    CK(cudaMemcpy(&ctl->budget_cap, &bc, sizeof(bc), cudaMemcpyHostToDevice));
     return 0;
   }
 
@@ -1867,6 +1872,7 @@ extern "C" void hvm_gb300_default_config(hvm_gb300_config* c) {
   c->var_page_log2 = 0;
   c->max_pages = 0;
   c->steal_min = 0;
+  c->turn_budget_cap = 1024;
 }
 
 extern "C" int hvm_gb300_create(const hvm_gb300_config* cfg, hvm_gb300_runtime** out) {
