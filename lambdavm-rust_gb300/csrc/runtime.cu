@@ -1331,6 +1331,7 @@ class Runtime {
       for (uint32_t k = 0; k < nroots; k++) weight[k] = book_words(k);
     }
     std::vector<uint32_t> admit;
+    uint32_t stream_cap = cfg.turn_budget_cap;  // the cap written at reset
     Ctl h;
     memset(&h, 0, sizeof(h));
     auto t0 = std::chrono::steady_clock::now();
@@ -1357,6 +1358,17 @@ class Runtime {
         launches++;
         for (uint32_t net : admit) active.push_back(net);
         admitted_total += (uint32_t)admit.size();
+      }
+      // Turns are capped (cfg.turn_budget_cap) only while no admitted-ready
+      // request waits: a short turn then bounds the latency of arrivals and
+      // completions; with a backlog, longer turns keep the host out of the way.
+      {
+        const uint32_t want_cap = ready_head < ready.size() ? 0u : cfg.turn_budget_cap;
+        if (want_cap != stream_cap) {
+          CK(cudaMemcpy(&ctl->budget_cap, &want_cap, sizeof(want_cap), cudaMemcpyHostToDevice));
+          h2d_bytes += sizeof(want_cap);
+          stream_cap = want_cap;
+        }
       }
       // A few turns, then the control block.
       if (launch_turns(4)) return -1;
