@@ -41,14 +41,14 @@ namespace hvm {
 
 // Capacity of each thread's page list (pages of one space a thread may own).
 constexpr uint32_t MAX_PAGES = 64;
-constexpr uint32_t HOST_NODE_WORDS = 1u << 17;  // node words the host may write IO results into
+constexpr uint32_t HOST_NODE_WORDS = 1u << 21;  // node words the host may write IO results into (at most 1/64 of the space)
 // IO encodings (src/run.c:32-60).
 constexpr uint32_t IO_MAGIC_0 = 0xD0CA11, IO_MAGIC_1 = 0xFF1FF1;
 constexpr uint32_t IO_CALL_TAG = 1;
 constexpr uint32_t RESULT_OK_TAG = 0, RESULT_ERR_TAG = 1;
 constexpr uint32_t IO_ERR_TYPE_TAG = 0, IO_ERR_NAME_TAG = 1, IO_ERR_INNER_TAG = 2;
 constexpr uint32_t LIST_NIL_TAG = 0, LIST_CONS_TAG = 1;
-constexpr uint32_t HOST_VAR_WORDS = 1u << 16;   // var words of the same
+constexpr uint32_t HOST_VAR_WORDS = 1u << 20;   // var words of the same
 // Batches: nets per batch (each takes one ROOT var at the top of the var
 // space) and definitions over all nets (REF vals have 28 bits).
 constexpr uint32_t MAX_BATCH = 1u << 20;
@@ -839,8 +839,10 @@ class Runtime {
     // The last pages below each pool's end are the host's: IO results are
     // written there (host_take), never by the device allocator.
     {
-      const uint32_t hn = std::max(1u, HOST_NODE_WORDS >> d.nspace.page_log2);
-      const uint32_t hv = std::max(1u, HOST_VAR_WORDS >> d.vspace.page_log2);
+      const uint64_t hn_words = std::min<uint64_t>(HOST_NODE_WORDS, (1ull << cfg.node_log2) / 64);
+      const uint64_t hv_words = std::min<uint64_t>(HOST_VAR_WORDS, (1ull << cfg.vars_log2) / 64);
+      const uint32_t hn = std::max<uint32_t>(1u, (uint32_t)(hn_words >> d.nspace.page_log2));
+      const uint32_t hv = std::max<uint32_t>(1u, (uint32_t)(hv_words >> d.vspace.page_log2));
       const uint32_t nfull = (uint32_t)((1ull << cfg.node_log2) >> d.nspace.page_log2);
       if (nfull <= d.nthreads + hn || d.vpool_end <= d.nthreads + hv) return fail("node/var space too small for the thread count");
       d.npool_end = nfull - hn;
