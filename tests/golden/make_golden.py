@@ -111,7 +111,10 @@ def run_ref(code: str) -> dict:
 
 # Files the IO programs open, relative to their working directory: the first
 # 47 bytes of LICENSE are what tests/programs/io/basic.hvm prints.
-IO_FILES = {"LICENSE": " " * 33 + "Apache License\n", "README.md": "# readme\n"}
+IO_FILES = {"LICENSE": " " * 33 + "Apache License\n" + "".join(f"fixture line {i:05d}\n" for i in range(1500)),
+            "README.md": "# readme\n"}
+# A larger read: tests/programs/io/basic.hvm with its READ of 47 bytes made 20000.
+BIG_READ = ("@call ~ (d ((e 47) f))", "@call ~ (d ((e 20000) f))")
 IO_STDIN = "io from the tests\n"
 
 
@@ -145,6 +148,11 @@ def make_io(ref: str) -> None:
         entry = {"name": rel, "code": code, "snapshot": snapshot, **run_ref_io(code)}
         out.append(entry)
         print(rel, entry["itrs"], repr(entry["printed"][:60]))
+        if rel.endswith("io/basic.hvm") and BIG_READ[0] in code:
+            big = code.replace(BIG_READ[0], BIG_READ[1])
+            entry = {"name": rel + " (READ 20000)", "code": big, "snapshot": None, **run_ref_io(big)}
+            out.append(entry)
+            print(entry["name"], entry["itrs"], len(entry["printed"]))
     with open(os.path.join(HERE, "io_programs.json"), "w") as f:
         json.dump({"files": IO_FILES, "stdin": IO_STDIN, "programs": out}, f, indent=1)
 
