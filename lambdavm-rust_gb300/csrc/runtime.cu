@@ -49,6 +49,7 @@ constexpr uint32_t RESULT_OK_TAG = 0, RESULT_ERR_TAG = 1;
 constexpr uint32_t IO_ERR_TYPE_TAG = 0, IO_ERR_NAME_TAG = 1, IO_ERR_INNER_TAG = 2;
 constexpr uint32_t LIST_NIL_TAG = 0, LIST_CONS_TAG = 1;
 constexpr uint32_t HOST_VAR_WORDS = 1u << 20;   // var words of the same
+constexpr uint32_t LIST_READ_MAX = 1u << 20;    // list elements one device readback pass returns
 // Batches: nets per batch (each takes one ROOT var at the top of the var
 // space) and definitions over all nets (REF vals have 28 bits).
 constexpr uint32_t MAX_BATCH = 1u << 20;
@@ -594,6 +595,55 @@ __global__ void gather_kernel(Dev d, Port root, Port* out, uint32_t* kids, uint3
   if (threadIdx.x == 0) { info[0] = next < cap ? next : cap; info[1] = overflow; }
 }
 
+// Reads a lambda-encoded list of u24 (lam t (((t CONS) head) tail) ... lam t
+// (t NIL)) straight from the net, as the host readback would, as long as no
+// REF must be expanded (expansion normalises, which only the host loop
+// does). info = {elements read, 1 if the host must continue, the port of the
+// element where it stopped}. One thread: the list is a chain.
+__global__ void read_list_kernel(Dev d, Port p, uint32_t max, uint32_t* out, uint32_t* info) {
+  if (blockIdx.x != 0 || threadIdx.x != 0) return;
+  auto peekp = [&](Port q) -> Port {
+    for (uint32_t g = 0; g < (1u << 20) && get_tag(q) == VAR; g++) {
+      Port v = __ldcg(&d.vars[get_val(q) & d.vars_mask]);
+      if (v == NONE || v == 0) break;
+      q = v;
+    }
+    return q;
+  };
+  auto node = [&](Port q) -> Pair { return (Pair)__ldcg((const unsigned long long*)&d.node[get_val(q)]); };
+  uint32_t k = 0, host = 0;
+  while (k < max) {
+    const Port lam = peekp(p);
+    if (get_tag(lam) == REF) { host = 1; break; }
+    if (get_tag(lam) != CON) break;
+    const Pair ln = node(lam);
+    const Port app = peekp(get_fst(ln));
+    if (get_tag(app) == REF) { host = 1; break; }
+    if (get_tag(app) != CON) break;
+    const Pair an = node(app);
+    const Port tag = peekp(get_fst(an));
+    if (get_tag(tag) == REF) { host = 1; break; }
+    if (get_tag(tag) != NUM || get_u24(get_val(tag)) != 1) break;  // not a CONS
+    const Port a1 = peekp(get_snd(an));
+    if (get_tag(a1) == REF) { host = 1; break; }
+    if (get_tag(a1) != CON) break;
+    const Pair n1 = node(a1);
+    const Port head = peekp(get_fst(n1)), a2 = peekp(get_snd(n1));
+    if (get_tag(head) == REF || get_tag(a2) == REF) { host = 1; break; }
+    if (get_tag(a2) != CON) break;
+    const Pair n2 = node(a2);
+    const Port tail = peekp(get_fst(n2)), a3 = peekp(get_snd(n2));
+    if (get_tag(tail) == REF || get_tag(a3) == REF) { host = 1; break; }
+    if (get_tag(a3) == CON || get_tag(head) != NUM) break;  // not exactly two arguments, or not a number
+    out[k++] = get_u24(get_val(head));
+    p = tail;
+  }
+  if (k == max) host = 1;
+  info[0] = k;
+  info[1] = host;
+  info[2] = p;
+}
+
 // ---- host runtime ----------------------------------------------------------------
 
 #define CK(x) do { cudaError_t e_ = (x); if (e_ != cudaSuccess) { return fail(std::string(#x) + ": " + cudaGetErrorString(e_)); } } while (0)
@@ -695,6 +745,7 @@ class Runtime {
   int sms = 0;
   // Host injection region per space (0 = nodes, 1 = vars): [lo, hi) words, next candidate.
   uint32_t host_lo[2] = {0, 0}, host_hi[2] = {0, 0}, host_next[2] = {0, 0};
+  uint32_t* list_buf = nullptr;          // device list readback: LIST_READ_MAX values + info
   uint32_t max_pages = MAX_PAGES;        // page-list capacity per thread and space
   // Scheduler policy written into the control block at every reset.
   uint32_t policy_mode = POLICY_FIXED;
@@ -726,11 +777,12 @@ class Runtime {
 
   void release() {
     void* ps[] = {mem_node, mem_vars, mem_ring, mem_cur, mem_scratch, mem_defs, mem_book, g_out, g_kids, g_info, ctl,
-                  mem_trace, mem_roots, mem_free, mem_mains, mem_policy};
+                  mem_trace, mem_roots, mem_free, mem_mains, mem_policy, list_buf};
     for (void* p : ps) if (p) cudaFree(p);
     mem_node = mem_vars = mem_ring = mem_cur = mem_scratch = mem_defs = mem_book = mem_trace = mem_roots = mem_free =
         mem_mains = nullptr;
     mem_policy = nullptr;
+    list_buf = nullptr;
     defs_bytes = book_bytes = scratch_bytes = 0;
     g_out = nullptr; g_kids = nullptr; g_info = nullptr; ctl = nullptr;
   }
@@ -1577,6 +1629,23 @@ class Runtime {
   // element is normalised in turn, the tail booted against ROOT.
   int read_bytes(Port p, std::string& out) {
     out.clear();
+    // Most lists are already in normal form: read them on the device in one
+    // pass; the host loop below takes over where a REF must be expanded.
+    if (normalize()) return -1;
+    if (!list_buf) CK(cudaMalloc((void**)&list_buf, (LIST_READ_MAX + 4) * sizeof(uint32_t)));
+    read_list_kernel<<<1, 1>>>(d, p, LIST_READ_MAX, list_buf, list_buf + LIST_READ_MAX);
+    CK(cudaGetLastError());
+    launches++;
+    uint32_t info[3];
+    CK(cudaMemcpy(info, list_buf + LIST_READ_MAX, sizeof(info), cudaMemcpyDeviceToHost));
+    if (info[0]) {
+      std::vector<uint32_t> v(info[0]);
+      CK(cudaMemcpy(v.data(), list_buf, v.size() * sizeof(uint32_t), cudaMemcpyDeviceToHost));
+      for (uint32_t x : v) out.push_back((char)x);
+    }
+    d2h_bytes += sizeof(info) + (uint64_t)info[0] * sizeof(uint32_t);
+    if (!info[1]) return 0;
+    p = info[2];
     for (;;) {
       if (normalize()) return -1;
       Ctr c;
