@@ -189,14 +189,13 @@ __global__ void __launch_bounds__(128, MIN_BLOCKS_128 > 0 ? MIN_BLOCKS_128 : 1) 
   // Turn parameters are read once per block so every thread of the block
   // takes the same early-exit decision.
   __shared__ unsigned long long sh_base, sh_end;
-  __shared__ unsigned sh_run, sh_s, sh_budget, sh_chunk, sh_stop_at, blk_dry;
+  __shared__ unsigned sh_run, sh_s, sh_budget, sh_stop_at, blk_dry;
   if (threadIdx.x == 0) {
     sh_base = ldcg64(&c->base);
     sh_end = ldcg64(&c->in_end);
     sh_run = sh_base != sh_end && __ldcg(&c->status) == 0;  // else: normal form reached, or failed
     sh_s = __ldcg(&c->static_per_thread);
     sh_budget = __ldcg(&c->budget);
-    sh_chunk = __ldcg(&c->chunk);
     sh_stop_at = __ldcg(&c->stop_at);
     blk_dry = 0;
   }
