@@ -84,6 +84,11 @@ typedef struct {
                                  this many (0 = 2) */
   uint32_t turn_budget_cap;   /* 0, or the most rounds a turn may run (default 1024): bounds how long a
                                  stream waits between admissions and completion checks (serving latency) */
+  uint32_t narrow_below;      /* 0 = off; else (default 1024) turns that start with fewer pending redexes
+                                 than this run the `narrow_reg_cap` kernel variant on its own grid, the
+                                 others the `reg_cap_blocks` one; the host switches between its polls */
+  uint32_t narrow_reg_cap;    /* 0 (default: no register cap, no spills), or 5/6/8: the register cap of
+                                 that narrow variant */
 } hvm_gb300_config;
 
 typedef struct {

@@ -49,6 +49,8 @@ class Config(ctypes.Structure):
         ("max_pages", ctypes.c_uint32),
         ("steal_min", ctypes.c_uint32),
         ("turn_budget_cap", ctypes.c_uint32),
+        ("narrow_below", ctypes.c_uint32),
+        ("narrow_reg_cap", ctypes.c_uint32),
     ]
 
 

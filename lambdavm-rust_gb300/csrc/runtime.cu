@@ -458,6 +458,30 @@ __global__ void boot_kernel(Dev d, Pair redex, Port root, uint32_t cap) {
   __threadfence();
 }
 
+// Re-plans the next turn for a grid of d.nthreads threads after the host
+// switched kernel variants between two turns: the static share, the claim
+// head and the stop threshold depend on the thread count (as fixed_policy
+// sets them); the round budget is kept.
+__global__ void retarget_kernel(Dev d, uint32_t cap) {
+  Ctl* c = d.ctl;
+  const unsigned long long pending = c->in_end - c->base;
+  const uint32_t n = d.nthreads;
+  uint32_t s = 1;
+  if (pending >= n) {
+    unsigned long long per = pending / n;
+    s = (uint32_t)(per < cap / 2 ? per : cap / 2);
+    if (s == 0) s = 1;
+  }
+  unsigned long long busy = pending < n ? pending : n;
+  unsigned long long keep = (busy * (256 - c->stop_frac_q8)) >> 8;
+  c->stop_at = (uint32_t)(n - keep);
+  c->static_per_thread = s;
+  c->chunk = pending < n ? 1 : (cap / 4 > 1 ? cap / 4 : 1);
+  unsigned long long take = (unsigned long long)s * n;
+  c->head = c->base + (take < pending ? take : pending);
+  __threadfence();
+}
+
 // Starts a batch: net k's redex `@main_k ~ ROOT_k` with ROOT_k = ROOT_VAR - k.
 __global__ void boot_batch_kernel(Dev d, const uint32_t* mains, uint32_t n, uint32_t cap) {
   Ctl* c = d.ctl;
@@ -736,6 +760,16 @@ class Runtime {
   uint32_t gather_cap = 0;
   uint32_t grid = 0, block = 0, cap = 0;
   void (*turn_fn)(Dev, uint32_t) = nullptr;
+  // Turn kernel variants: 0 = `reg_cap_blocks`, 1 = `narrow_reg_cap` (used
+  // while few redexes are pending, when `narrow_below` is set). Per-thread
+  // allocator state and CALL scratch are sized for the larger grid.
+  struct Variant {
+    void (*fn)(Dev, uint32_t) = nullptr;
+    uint32_t grid = 0, nthreads = 0;
+  };
+  Variant variants[2];
+  int cur_variant = 0;
+  uint32_t nthreads_max = 0;
   size_t smem = 0;
   uint32_t max_def_nodes = 1, max_def_vars = 1;
   size_t defs_bytes = 0, book_bytes = 0, scratch_bytes = 0;  // capacities of mem_defs / mem_book / mem_scratch
@@ -799,20 +833,33 @@ class Runtime {
       return fail("node_log2/vars_log2 must be in [10, 29]");
     smem = (size_t)block * cap * sizeof(Pair);
     if (block > 128) return fail("threads_per_block must be <= 128");
-    switch (cfg.reg_cap_blocks) {
-      case 0: turn_fn = turn_kernel<0>; break;
-      case 5: turn_fn = turn_kernel<5>; break;
-      case 6: turn_fn = turn_kernel<6>; break;
-      case 8: turn_fn = turn_kernel<8>; break;
-      default: return fail("reg_cap_blocks must be 0, 5, 6 or 8");
-    }
-    CK(cudaFuncSetAttribute(turn_fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    int per_sm = 0;
-    CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, turn_fn, (int)block, smem));
-    if (per_sm <= 0) return fail("turn kernel does not fit on an SM with this block size / stack capacity");
-    if (cfg.blocks_per_sm && (int)cfg.blocks_per_sm < per_sm) per_sm = (int)cfg.blocks_per_sm;
-    grid = (uint32_t)(per_sm * sms);
-    uint32_t nthreads = grid * block;
+    // The turn kernel variant (register cap) and its grid; with `narrow_below`,
+    // a second variant runs the turns that start with fewer pending redexes.
+    auto make_variant = [&](uint32_t reg_cap, Variant& v) -> int {
+      switch (reg_cap) {
+        case 0: v.fn = turn_kernel<0>; break;
+        case 5: v.fn = turn_kernel<5>; break;
+        case 6: v.fn = turn_kernel<6>; break;
+        case 8: v.fn = turn_kernel<8>; break;
+        default: return fail("reg_cap_blocks / narrow_reg_cap must be 0, 5, 6 or 8");
+      }
+      CK(cudaFuncSetAttribute(v.fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+      int per_sm = 0;
+      CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, v.fn, (int)block, smem));
+      if (per_sm <= 0) return fail("turn kernel does not fit on an SM with this block size / stack capacity");
+      if (cfg.blocks_per_sm && (int)cfg.blocks_per_sm < per_sm) per_sm = (int)cfg.blocks_per_sm;
+      v.grid = (uint32_t)(per_sm * sms);
+      v.nthreads = v.grid * block;
+      return 0;
+    };
+    if (make_variant(cfg.reg_cap_blocks, variants[0])) return -1;
+    variants[1] = variants[0];
+    if (cfg.narrow_below && make_variant(cfg.narrow_reg_cap, variants[1])) return -1;
+    cur_variant = 0;
+    turn_fn = variants[0].fn;
+    grid = variants[0].grid;
+    uint32_t nthreads = variants[0].nthreads;
+    nthreads_max = std::max(variants[0].nthreads, variants[1].nthreads);
 
     uint64_t n_nodes = 1ull << cfg.node_log2, n_vars = 1ull << cfg.vars_log2;
     d.nthreads = nthreads;
@@ -823,7 +870,7 @@ class Runtime {
     // many pages again remain in the pool.
     auto page_log2_for = [&](uint64_t words, uint32_t max_log2, uint32_t min_log2) -> int {
       int l = (int)max_log2;
-      while (l >= (int)min_log2 && (words >> l) < 2ull * nthreads) l--;
+      while (l >= (int)min_log2 && (words >> l) < 2ull * nthreads_max) l--;
       return l < (int)min_log2 ? -1 : l;
     };
     if ((cfg.node_page_log2 && (cfg.node_page_log2 < 5 || cfg.node_page_log2 > 12)) ||
@@ -854,7 +901,7 @@ class Runtime {
     uint64_t ring_len = 1ull << cfg.ring_log2;
     CK(cudaMalloc(&mem_ring, ring_len * sizeof(Pair)));
     // Page lists + counts + positions + offsets, for both spaces.
-    CK(cudaMalloc(&mem_cur, 2ull * nthreads * (max_pages + 3) * sizeof(uint32_t)));
+    CK(cudaMalloc(&mem_cur, 2ull * nthreads_max * (max_pages + 3) * sizeof(uint32_t)));
     CK(cudaMalloc((void**)&ctl, sizeof(Ctl)));
     {
       // One free-page ring per space, as large as the space's page count.
@@ -871,10 +918,10 @@ class Runtime {
     d.ring_mask = ring_len - 1;
     uint32_t* w = (uint32_t*)mem_cur;
     for (PagedSpace* sp : {&d.nspace, &d.vspace}) {
-      sp->lists = w; w += (size_t)nthreads * max_pages;
-      sp->counts = w; w += nthreads;
-      sp->pos = w; w += nthreads;
-      sp->off = w; w += nthreads;
+      sp->lists = w; w += (size_t)nthreads_max * max_pages;
+      sp->counts = w; w += nthreads_max;
+      sp->pos = w; w += nthreads_max;
+      sp->off = w; w += nthreads_max;
     }
     d.ctl = ctl;
     return reset_net();
@@ -895,7 +942,7 @@ class Runtime {
       const uint32_t hn = std::max<uint32_t>(1u, (uint32_t)(hn_words >> d.nspace.page_log2));
       const uint32_t hv = std::max<uint32_t>(1u, (uint32_t)(hv_words >> d.vspace.page_log2));
       const uint32_t nfull = (uint32_t)((1ull << cfg.node_log2) >> d.nspace.page_log2);
-      if (nfull <= d.nthreads + hn || d.vpool_end <= d.nthreads + hv) return fail("node/var space too small for the thread count");
+      if (nfull <= nthreads_max + hn || d.vpool_end <= nthreads_max + hv) return fail("node/var space too small for the thread count");
       d.npool_end = nfull - hn;
       d.vpool_end -= hv;
       host_lo[0] = d.npool_end << d.nspace.page_log2;
@@ -905,7 +952,7 @@ class Runtime {
       host_next[0] = host_lo[0];
       host_next[1] = host_lo[1];
     }
-    if (d.vpool_end < d.nthreads) return fail("var space too small for this batch");
+    if (d.vpool_end < nthreads_max) return fail("var space too small for this batch");
     CK(cudaMemset(ctl, 0, sizeof(Ctl)));
     if (cfg.profile) { uint32_t one = 1; CK(cudaMemcpy(&ctl->prof_on, &one, sizeof(one), cudaMemcpyHostToDevice)); }
     uint32_t frac = cfg.stop_frac_q8 ? cfg.stop_frac_q8 : 32;
@@ -919,7 +966,12 @@ class Runtime {
       CK(cudaMemcpy(&ctl->trace_cap, &cap_, sizeof(cap_), cudaMemcpyHostToDevice));
     }
     // Thread g starts with page g of each space; the pools start after them.
-    reset_alloc_kernel<<<(d.nthreads + 255) / 256, 256>>>(d);
+    // Every thread of the larger variant's grid gets its pages.
+    {
+      Dev all = d;
+      all.nthreads = nthreads_max;
+      reset_alloc_kernel<<<(nthreads_max + 255) / 256, 256>>>(all);
+    }
     CK(cudaGetLastError());
     launches++;
     norm_seconds = 0;
@@ -1105,7 +1157,7 @@ class Runtime {
     if (max_def_vars < CHUNK) max_def_vars = CHUNK;
     if (ensure(mem_defs, defs_bytes, hdr.size() * sizeof(DefHdr)) ||
         ensure(mem_book, book_bytes, flat.size() * sizeof(Pair)) ||
-        ensure(mem_scratch, scratch_bytes, (size_t)(max_def_nodes + max_def_vars) * d.nthreads * sizeof(uint32_t)))
+        ensure(mem_scratch, scratch_bytes, (size_t)(max_def_nodes + max_def_vars) * nthreads_max * sizeof(uint32_t)))
       return -1;
     CK(cudaMemcpy(mem_defs, hdr.data(), hdr.size() * sizeof(DefHdr), cudaMemcpyHostToDevice));
     CK(cudaMemcpy(mem_book, flat.data(), flat.size() * sizeof(Pair), cudaMemcpyHostToDevice));
@@ -1115,8 +1167,29 @@ class Runtime {
     d.book = (const Pair*)mem_book;
     d.ndefs = (uint32_t)defs.size();
     d.nloc = (uint32_t*)mem_scratch;
-    d.vloc = d.nloc + (size_t)max_def_nodes * d.nthreads;
+    d.vloc = d.nloc + (size_t)max_def_nodes * nthreads_max;
     return 0;
+  }
+
+  // Makes variant v the one that runs the next turns (between turns, with
+  // the device idle) and re-plans the pending turn for its grid.
+  int use_variant(int v) {
+    if (v == cur_variant) return 0;
+    cur_variant = v;
+    turn_fn = variants[v].fn;
+    grid = variants[v].grid;
+    d.nthreads = variants[v].nthreads;
+    retarget_kernel<<<1, 1>>>(d, cap);
+    CK(cudaGetLastError());
+    launches++;
+    return 0;
+  }
+
+  // After a poll: the narrow variant while fewer than `narrow_below`
+  // redexes are pending, else the configured one.
+  int pick_variant(const Ctl& h) {
+    if (!cfg.narrow_below || h.base == h.in_end) return 0;
+    return use_variant(h.in_end - h.base < cfg.narrow_below ? 1 : 0);
   }
 
   int read_ctl(Ctl& h) {
@@ -1228,6 +1301,7 @@ class Runtime {
       }
       last_itrs = h.itrs;
       last_pending = h.pending;
+      if (pick_variant(h)) return -1;
       if (batch < 64) batch *= 2;
     }
     norm_seconds += std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
@@ -1427,6 +1501,7 @@ class Runtime {
       if (launch_turns(4)) return -1;
       if (read_ctl(h) || collect_times()) return -1;
       if (h.status) return fail(std::string("device error: ") + status_text(h.status));
+      if (pick_variant(h)) return -1;
       // Completions.
       if (!active.empty()) {
         CK(cudaMemcpy(dlive, active.data(), active.size() * sizeof(uint32_t), cudaMemcpyHostToDevice));
@@ -1955,6 +2030,8 @@ extern "C" void hvm_gb300_default_config(hvm_gb300_config* c) {
   c->max_pages = 0;
   c->steal_min = 0;
   c->turn_budget_cap = 1024;
+  c->narrow_below = 1024;
+  c->narrow_reg_cap = 0;
 }
 
 extern "C" int hvm_gb300_create(const hvm_gb300_config* cfg, hvm_gb300_runtime** out) {
