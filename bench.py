@@ -54,6 +54,8 @@ WORKLOADS = {
     "batch_mixed_4096": (None, None, "4096 independent nets (1/3 tree sums d 8..18, 1/3 bitonic sorts of 2^6..2^12 "
                                      "keys then summed, 1/3 countdowns 10..1e5), continuous batching"),
     "serving": (None, None, "Poisson arrivals of nets drawn from the 4096-net mixed pool, continuous batching"),
+    "compiled_calls": (None, None, "standalone `hvm gen-cu --compiled` programs against `hvm gen-cu` ones "
+                                   "(bitonic 2^16, tree sum d=20, skewed fold 2^18, countdown 1e5)"),
 }
 
 # Continuous-batching settings for the mixed batch (admission cap and live-memory
@@ -151,6 +153,59 @@ def bench_scheduler(hvm, W, reps: int = 5) -> dict:
                            "parity": bool(ok)}
     out["learned_over_fixed"] = out["learned"]["value"] / out["fixed"]["value"]
     return out
+
+
+def bench_compiled_calls(hvm, W, reps: int = 3) -> dict:
+    """Compiled calls against the table-driven CALL: for each workload the
+    standalone programs of `hvm gen-cu --compiled` and `hvm gen-cu`, built
+    with nvcc for sm_103a, each run `reps` times as its own process with
+    kernels loaded eagerly (so the printed MIPS covers the evaluation only:
+    boot, turns and readback). Every run is checked against the reference's
+    interaction count and normal form."""
+    from concurrent.futures import ThreadPoolExecutor
+    nvcc = os.path.join(os.environ.get("CUDA_HOME", "/usr/local/cuda"), "bin", "nvcc")
+    golden = json.load(open(GOLDEN))
+    cases = [("bitonic_sort_2p16", W.bitonic_sort(16)), ("tree_sum_d20", W.tree_sum(20)),
+             ("skewed_fold_2p18", W.skewed_fold(18)), ("countdown_100000", W.countdown(100000))]
+    tmp = tempfile.mkdtemp(prefix="hvm_cc_")
+    jobs = []
+    for name, code in cases:
+        src = os.path.join(tmp, name + ".hvm")
+        open(src, "w").write(code)
+        for arm in ("interpreted", "compiled"):
+            cmd = [hvm.CLI_PATH, "gen-cu"] + (["--compiled"] if arm == "compiled" else []) + [src]
+            cu = os.path.join(tmp, f"{name}_{arm}.cu")
+            open(cu, "w").write(subprocess.run(cmd, capture_output=True, text=True, check=True).stdout)
+            jobs.append((name, arm, cu, cu[:-3]))
+
+    def build(job):
+        _, _, cu, exe = job
+        subprocess.run([nvcc, "-gencode", "arch=compute_103a,code=sm_103a", "-O3", "-std=c++17", cu, "-o", exe],
+                       check=True, capture_output=True, timeout=900)
+
+    t0 = time.perf_counter()
+    with ThreadPoolExecutor(max_workers=8) as ex:
+        list(ex.map(build, jobs))
+    build_s = time.perf_counter() - t0
+    env = dict(os.environ, CUDA_MODULE_LOADING="EAGER")
+    out = {}
+    for name, arm, _, exe in jobs:
+        g = golden[name]
+        mips, ok = [], True
+        for _ in range(reps):
+            txt = subprocess.run([exe], capture_output=True, text=True, check=True, env=env, timeout=600).stdout
+            res = re.search(r"^Result: (.*)$", txt, re.M).group(1)
+            itrs = int(re.search(r"^- ITRS: (\d+)$", txt, re.M).group(1))
+            mips.append(float(re.search(r"^- MIPS: ([0-9.]+)$", txt, re.M).group(1)))
+            ok = ok and itrs == g["itrs"] and \
+                hashlib.sha256(hvm.canonical(res).encode()).hexdigest() == g["canonical_sha256"]
+        row = out.setdefault(name, {"itrs": g["itrs"]})
+        row[arm + "_itrs_per_s"] = statistics.median(mips) * 1e6
+        row[arm + "_parity"] = bool(ok)
+    for row in out.values():
+        row["compiled_over_interpreted"] = row["compiled_itrs_per_s"] / row["interpreted_itrs_per_s"]
+    return {"workloads": out, "reps": reps, "nvcc_build_s": build_s,
+            "note": "median of reps; each run is one process (runtime creation excluded from its timing)"}
 
 
 def bench_serving(hvm, W, rates=(1e2, 1e3, 1e4, 1e5), seconds: float = 2.0, max_requests: int = 100_000) -> dict:
@@ -479,6 +534,19 @@ def main():
     hvm = ensure_built()
     W = importlib.import_module("lambdavm-rust_gb300.workloads")
     key, make, desc = WORKLOADS[args.workload]
+    if args.workload == "compiled_calls":
+        if args.impl == "reference" or rank != 0:
+            if rank == 0:
+                print(json.dumps({"impl": "reference", "unavailable": "the CPU arm runs the single-net workloads"}))
+            return
+        cc = bench_compiled_calls(hvm, W)
+        b = cc["workloads"]["bitonic_sort_2p16"]
+        line = {"metric": METRIC, "value": b["compiled_itrs_per_s"], "unit": UNIT, "n_gpus": 1, "steps": cc["reps"],
+                "warmup": 0, "ms_per_step": b["itrs"] / b["compiled_itrs_per_s"] * 1e3, "higher_is_better": True,
+                "scaling": "weak", "vs_baseline": None, "dtype": "u32", "data": "synthetic",
+                "config": {"workload": desc, **cc}}
+        print(json.dumps(line), flush=True)
+        return
     if args.workload in ("batch_mixed_4096", "serving"):
         if args.impl == "reference" or rank != 0:
             if rank == 0:

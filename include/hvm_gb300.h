@@ -53,6 +53,16 @@ int hvm_gb300_book_from_text(const char* text, uint32_t* out, size_t out_cap_wor
 int hvm_gb300_canonical_tree(const char* text, char* out, size_t out_cap, size_t* out_len,
                              char* err, size_t err_cap);
 
+/* CUDA source of the compiled calls for a serialized book (the reference's
+ * cmp::compile_book for its CUDA target, src/cmp.rs:10-119, which its gen-cu
+ * leaves disabled at src/main.rs:140-146): per def, its node stores and links
+ * as straight-line code. `hvm gen-cu --compiled` appends it to the standalone
+ * program, which then defines HVM_COMPILED_CALLS. No GPU is used. Returns 0,
+ * 1 on a bad book, 3 if `out` is too small; `out == NULL` queries the length
+ * (without the terminating NUL). */
+int hvm_gb300_compile_calls(const uint32_t* book, size_t words, char* out, size_t out_cap, size_t* out_len,
+                            char* err, size_t err_cap);
+
 /* ---- Handle API ----------------------------------------------------------------
  *
  * Re-entrant form of `hvm_cu` for callers that run many nets, read results

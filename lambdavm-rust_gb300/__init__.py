@@ -102,6 +102,7 @@ EXPORTED_SYMBOLS = (
     "hvm_cu",
     "hvm_gb300_book_from_text",
     "hvm_gb300_canonical_tree",
+    "hvm_gb300_compile_calls",
     "hvm_gb300_default_config",
     "hvm_gb300_create",
     "hvm_gb300_load_book",
@@ -143,6 +144,8 @@ def lib() -> ctypes.CDLL:
                                            ctypes.POINTER(ctypes.c_size_t), ctypes.c_char_p, ctypes.c_size_t]
     L.hvm_gb300_canonical_tree.argtypes = [ctypes.c_char_p, ctypes.c_char_p, ctypes.c_size_t,
                                            ctypes.POINTER(ctypes.c_size_t), ctypes.c_char_p, ctypes.c_size_t]
+    L.hvm_gb300_compile_calls.argtypes = [u32p, ctypes.c_size_t, ctypes.c_char_p, ctypes.c_size_t,
+                                          ctypes.POINTER(ctypes.c_size_t), ctypes.c_char_p, ctypes.c_size_t]
     L.hvm_gb300_default_config.argtypes = [ctypes.POINTER(Config)]
     L.hvm_gb300_default_config.restype = None
     L.hvm_gb300_create.argtypes = [ctypes.POINTER(Config), ctypes.POINTER(ctypes.c_void_p)]
@@ -216,6 +219,22 @@ def canonical(tree_text: str) -> str:
     out = ctypes.create_string_buffer(n.value + 1)
     rc = L.hvm_gb300_canonical_tree(data, out, n.value + 1, ctypes.byref(n), err, len(err))
     if rc:
+        raise HvmError(err.value.decode())
+    return out.value.decode()
+
+
+def compile_calls(book) -> str:
+    """CUDA source of the compiled calls for a book (text or serialized
+    words): what `hvm gen-cu --compiled` appends to the standalone program."""
+    L = lib()
+    words = book_from_text(book) if isinstance(book, str) else np.ascontiguousarray(book, dtype=np.uint32)
+    ptr = words.ctypes.data_as(ctypes.POINTER(ctypes.c_uint32))
+    n = ctypes.c_size_t()
+    err = ctypes.create_string_buffer(4096)
+    if L.hvm_gb300_compile_calls(ptr, words.size, None, 0, ctypes.byref(n), err, len(err)):
+        raise HvmError(err.value.decode())
+    out = ctypes.create_string_buffer(n.value + 1)
+    if L.hvm_gb300_compile_calls(ptr, words.size, out, n.value + 1, ctypes.byref(n), err, len(err)):
         raise HvmError(err.value.decode())
     return out.value.decode()
 

@@ -147,6 +147,9 @@ struct Dev {
   const DefHdr* defs;
   const Pair* book;
   Ctl* ctl;
+#ifdef HVM_COMPILED_CALLS
+  uint32_t compiled;          // 1 when the loaded book is the one compiled into this program
+#endif
 };
 
 // ---- memory access -----------------------------------------------------------
@@ -462,8 +465,26 @@ struct Plan {
   Numb cv;              // OPER: the result when both sides are numbers
   bool oper_num;        // OPER: B1 is a number
   bool counted;         // counts as an interaction (every rule but LINK)
+#ifdef HVM_COMPILED_CALLS
+  uint32_t fid;         // CALL: the def
+#endif
 };
 constexpr uint32_t IDLE_RULE = 8;
+
+#ifdef HVM_COMPILED_CALLS
+// Compiled calls (the reference's compile_book for its CUDA target,
+// src/cmp.rs:10-119, which src/main.rs:140-146 leaves disabled): a program
+// emitted by `hvm gen-cu --compiled` defines these from its book, as
+// straight-line code per def, with the def's words as immediates instead of
+// loads from the def tables. Both are used for contiguous runs only, and
+// both return false for a def that was not compiled (it then runs from the
+// tables); the interactions are the same either way.
+// Writes def fid's nodes at nb, nb+1, ... (their vars at vb, vb+1, ...).
+__device__ __forceinline__ bool compiled_call_nodes(const Dev& d, uint32_t fid, uint32_t nb, uint32_t vb);
+// The i-th link of def fid (its redexes, then its root ~ `caller`).
+__device__ __forceinline__ bool compiled_call_link(uint32_t fid, uint32_t i, uint32_t nb, uint32_t vb, Port caller,
+                                                   Port& x, Port& y);
+#endif
 
 // Maps a def-local port to the fresh words of this CALL (adjust_port,
 // src/hvm.c:346-362): base + index for contiguous runs, else the scratch tables.
@@ -500,6 +521,9 @@ __device__ __forceinline__ void link_pair(const Dev& d, uint32_t gid, const Plan
       break;
     case SWIT: x = new_port(CON, p.n0); y = get_fst(p.B); break;
     default: {  // CALL
+#ifdef HVM_COMPILED_CALLS
+      if (d.compiled && p.contig && compiled_call_link(p.fid, i, p.nbase, p.vbase, p.b, x, y)) break;
+#endif
       if (i < p.rbag_len) {
         Pair q = __ldg((const unsigned long long*)&d.book[p.off + i]);
         x = get_fst(q) == CALLER_PORT ? p.b : relocate(d, gid, p, get_fst(q));
@@ -532,6 +556,9 @@ __device__ __forceinline__ bool plan_redex(const Dev& d, TState& t, Pair r, Plan
     } else {
       p.node_len = h.node_len; p.rbag_len = h.rbag_len; p.vars_len = h.vars_len;
       p.off = h.off; p.root = h.root; p.joined = h.joined != 0;
+#ifdef HVM_COMPILED_CALLS
+      p.fid = fid;
+#endif
     }
   }
   p.rule = rule;
@@ -692,6 +719,9 @@ __device__ __forceinline__ int lockstep_round(const Dev& d, TState& t, bool has,
           if (rc != IR_DONE) break;
         }
         const Pair* nodes = d.book + p.off + p.rbag_len;
+#ifdef HVM_COMPILED_CALLS
+        if (!(d.compiled && p.contig && compiled_call_nodes(d, p.fid, p.nbase, p.vbase)))
+#endif
         for (uint32_t i = 0; i < p.node_len; i++) {
           Pair q = __ldg((const unsigned long long*)&nodes[i]);
           uint32_t at = p.contig ? p.nbase + i : d.nloc[(size_t)i * d.nthreads + t.gid];

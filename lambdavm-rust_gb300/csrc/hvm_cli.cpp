@@ -2,10 +2,14 @@
 // `gen-cu` surface (src/main.rs:22-65, 87-96, 128-155):
 //   hvm run-cu FILE    parses the `.hvm` file, serializes the Book and calls
 //                      the C ABI `hvm_cu(book_buffer)`;
-//   hvm gen-cu FILE    prints a standalone CUDA program: this runtime as one
+//   hvm gen-cu [--compiled] FILE
+//                      prints a standalone CUDA program: this runtime as one
 //                      translation unit, the serialized book as `BOOK_BUF`, and
 //                      a `main` that runs it (compile it with
 //                      `nvcc -gencode arch=compute_103a,code=sm_103a -O3 -std=c++17`);
+//                      with --compiled, the book's defs are also compiled into
+//                      straight-line CALL code (the reference's compile_book for
+//                      its CUDA target, src/cmp.rs:10-119);
 //   hvm book FILE OUT  writes the serialized book buffer to OUT (the bytes the
 //                      reference passes across its C ABI).
 #include <cstdio>
@@ -48,7 +52,8 @@ static void usage() {
           "HVM2 on GB300\n"
           "usage:\n"
           "  hvm run-cu <file.hvm>       evaluate @main on the GPU\n"
-          "  hvm gen-cu <file.hvm>       print a standalone CUDA program for the file\n"
+          "  hvm gen-cu [--compiled] <file.hvm>\n"
+          "                              print a standalone CUDA program for the file\n"
           "  hvm book <file.hvm> <out>   write the serialized book buffer\n");
   exit(2);
 }
@@ -64,10 +69,28 @@ int main(int argc, char** argv) {
   if (cmd == "gen-cu") {
     // Like the reference's gen-cu, the book is embedded as a static buffer and
     // the program's main evaluates it through hvm_cu.
-    std::vector<uint32_t> buf = to_buffer(read_file(argv[2]));
-    printf("// Generated by `hvm gen-cu %s`: the GB300 evaluator runtime with an embedded book.\n", argv[2]);
+    const bool compiled = std::string(argv[2]) == "--compiled";
+    if (compiled && argc < 4) usage();
+    const char* path = compiled ? argv[3] : argv[2];
+    std::vector<uint32_t> buf = to_buffer(read_file(path));
+    std::string calls;
+    if (compiled) {
+      size_t n = 0;
+      char err[1024];
+      if (hvm_gb300_compile_calls(buf.data(), buf.size(), nullptr, 0, &n, err, sizeof err) != 0) {
+        fprintf(stderr, "%s\n", err);
+        exit(101);
+      }
+      calls.resize(n + 1);
+      hvm_gb300_compile_calls(buf.data(), buf.size(), &calls[0], calls.size(), &n, err, sizeof err);
+      calls.resize(n);
+    }
+    printf("// Generated by `hvm gen-cu %s%s`: the GB300 evaluator runtime with an embedded book.\n",
+           compiled ? "--compiled " : "", path);
     printf("// Build: nvcc -gencode arch=compute_103a,code=sm_103a -O3 -std=c++17 FILE.cu -o FILE\n\n");
+    if (compiled) printf("#define HVM_COMPILED_CALLS 1\n\n");
     fputs(HVM_STANDALONE_SOURCE, stdout);
+    fputs(calls.c_str(), stdout);
     printf("\n\nstatic const uint32_t BOOK_BUF[%zu] = {", buf.size());
     for (size_t i = 0; i < buf.size(); i++) printf("%s%s%u", i ? "," : "", i % 16 ? "" : "\n  ", buf[i]);
     printf("\n};\n\nint main() {\n  hvm_cu(BOOK_BUF);\n  return 0;\n}\n");

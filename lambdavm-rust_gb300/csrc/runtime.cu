@@ -738,6 +738,178 @@ static void join_links(const HostDef& h, std::vector<Pair>& links, std::vector<P
   vars_len = next;
 }
 
+// The device's def tables for a book: per def a header, then its links (the
+// redexes and the root link, joined) and its nodes, all defs in one array.
+static void def_tables(const std::vector<HostDef>& defs, std::vector<DefHdr>& hdr, std::vector<Pair>& flat,
+                       uint32_t& max_nodes, uint32_t& max_vars) {
+  hdr.assign(defs.size(), DefHdr{});
+  flat.clear();
+  max_nodes = 1;
+  max_vars = 1;
+  for (size_t f = 0; f < defs.size(); f++) {
+    const HostDef& h = defs[f];
+    std::vector<Pair> links, nodes;
+    uint32_t vars_len = 0;
+    join_links(h, links, nodes, vars_len);
+    hdr[f] = DefHdr{h.node_len, (uint32_t)links.size(), vars_len, h.safe ? 1u : 0u, 0, (uint32_t)flat.size(), 1, 0};
+    flat.insert(flat.end(), links.begin(), links.end());
+    flat.insert(flat.end(), nodes.begin(), nodes.end());
+    if (h.node_len > max_nodes) max_nodes = h.node_len;
+    if (vars_len > max_vars) max_vars = vars_len;
+  }
+  if (flat.empty()) flat.push_back(0);
+}
+
+// FNV-1a over the def tables: identifies the book a compiled program was
+// emitted for.
+static uint64_t tables_hash(const std::vector<DefHdr>& hdr, const std::vector<Pair>& flat) {
+  uint64_t x = 0xCBF29CE484222325ull;
+  auto mix = [&](const void* p, size_t n) {
+    const unsigned char* b = (const unsigned char*)p;
+    for (size_t i = 0; i < n; i++) { x ^= b[i]; x *= 0x100000001B3ull; }
+  };
+  mix(hdr.data(), hdr.size() * sizeof(DefHdr));
+  mix(flat.data(), flat.size() * sizeof(Pair));
+  return x;
+}
+
+#ifdef HVM_COMPILED_CALLS
+uint64_t compiled_book_hash();  // emitted with the compiled calls
+#endif
+
+// Limits of the compiled calls: the code is inlined at the CALL sites of
+// every turn kernel variant, so only the defs that run repeatedly are
+// compiled, up to these totals.
+constexpr size_t COMPILED_MAX_DEFS = 256;
+constexpr size_t COMPILED_MAX_WORDS = 8192;  // node words + links
+
+// The defs that lie on a cycle of the book's REF graph (recursive functions)
+// and the defs these call: the ones a run calls over and over. A book's data
+// defs (called once each, from @main) are not among them.
+static std::vector<bool> recursive_defs(const std::vector<HostDef>& defs) {
+  const size_t n = defs.size();
+  std::vector<std::vector<uint32_t>> out(n);
+  for (size_t f = 0; f < n; f++) {
+    auto add = [&](Port q) {
+      if (get_tag(q) == REF && (get_val(q) & 0xFFFFFFFu) < n) out[f].push_back(get_val(q) & 0xFFFFFFFu);
+    };
+    add(defs[f].root);
+    for (Pair p : defs[f].rbag) { add(get_fst(p)); add(get_snd(p)); }
+    for (Pair p : defs[f].node) { add(get_fst(p)); add(get_snd(p)); }
+  }
+  // Tarjan's strongly connected components, with an explicit stack.
+  std::vector<int> index(n, -1), low(n, 0);
+  std::vector<bool> on(n, false), rec(n, false);
+  std::vector<uint32_t> stack;
+  std::vector<std::pair<uint32_t, size_t>> work;  // (def, next edge)
+  int next = 0;
+  for (uint32_t s = 0; s < n; s++) {
+    if (index[s] >= 0) continue;
+    work.push_back({s, 0});
+    while (!work.empty()) {
+      const uint32_t v = work.back().first;
+      size_t& k = work.back().second;
+      if (k == 0 && index[v] < 0) { index[v] = low[v] = next++; stack.push_back(v); on[v] = true; }
+      if (k < out[v].size()) {
+        const uint32_t w = out[v][k++];
+        if (index[w] < 0) work.push_back({w, 0});
+        else if (on[w]) low[v] = std::min(low[v], index[w]);
+        continue;
+      }
+      if (low[v] == index[v]) {
+        std::vector<uint32_t> comp;
+        uint32_t w;
+        do { w = stack.back(); stack.pop_back(); on[w] = false; comp.push_back(w); } while (w != v);
+        const bool self = std::find(out[v].begin(), out[v].end(), v) != out[v].end();
+        if (comp.size() > 1 || self)
+          for (uint32_t c : comp) rec[c] = true;
+      }
+      work.pop_back();
+      if (!work.empty()) low[work.back().first] = std::min(low[work.back().first], low[v]);
+    }
+  }
+  // With everything a recursive def calls (its non-recursive helpers).
+  std::vector<uint32_t> todo;
+  for (uint32_t f = 0; f < n; f++) if (rec[f]) todo.push_back(f);
+  while (!todo.empty()) {
+    const uint32_t v = todo.back();
+    todo.pop_back();
+    for (uint32_t w : out[v]) if (!rec[w]) { rec[w] = true; todo.push_back(w); }
+  }
+  return rec;
+}
+
+// CUDA source of the compiled calls for a book (see compiled_call_nodes in
+// the evaluator): per recursive def, its node stores and its links with the
+// fresh node / var bases added to the def-local indices.
+static std::string compiled_calls_source(const std::vector<HostDef>& defs) {
+  std::vector<DefHdr> hdr;
+  std::vector<Pair> flat;
+  uint32_t mn = 0, mv = 0;
+  def_tables(defs, hdr, flat, mn, mv);
+  std::vector<bool> pick = recursive_defs(defs);
+  size_t ndefs = 0, words = 0;
+  for (size_t f = 0; f < defs.size(); f++) {
+    if (!pick[f]) continue;
+    const size_t w = hdr[f].node_len + hdr[f].rbag_len;
+    if (ndefs + 1 > COMPILED_MAX_DEFS || words + w > COMPILED_MAX_WORDS) { pick[f] = false; continue; }
+    ndefs++;
+    words += w;
+  }
+  static const char* tags[8] = {"VAR", "REF", "ERA", "NUM", "CON", "DUP", "OPR", "SWI"};
+  auto port = [&](Port q) -> std::string {
+    char b[64];
+    if (q == CALLER_PORT) return "caller";
+    const Tag t = get_tag(q);
+    if (t >= CON) snprintf(b, sizeof b, "new_port(%s, nb + %uu)", tags[t], get_val(q));
+    else if (t == VAR) snprintf(b, sizeof b, "new_port(VAR, vb + %uu)", get_val(q));
+    else snprintf(b, sizeof b, "0x%08xu", q);
+    return b;
+  };
+  std::string o;
+  char line[96];
+  o += "\n// ---- compiled calls (hvm gen-cu --compiled) ----\n";
+  o += "namespace hvm {\n";
+  snprintf(line, sizeof line, "// %zu of %zu defs compiled (the recursive ones and their callees)\n", ndefs, defs.size());
+  o += line;
+  o += "__device__ __forceinline__ bool compiled_call_nodes(const Dev& d, uint32_t fid, uint32_t nb, uint32_t vb) {\n";
+  o += "  (void)d; (void)nb; (void)vb;\n";
+  o += "  switch (fid) {\n";
+  for (size_t f = 0; f < defs.size(); f++) {
+    if (!pick[f]) continue;
+    snprintf(line, sizeof line, "    case %zuu:  // %s\n", f, defs[f].name.c_str());
+    o += line;
+    const Pair* nodes = flat.data() + hdr[f].off + hdr[f].rbag_len;
+    for (uint32_t i = 0; i < hdr[f].node_len; i++) {
+      snprintf(line, sizeof line, "      nstore(d, nb + %uu, new_pair(", i);
+      o += line + port(get_fst(nodes[i])) + ", " + port(get_snd(nodes[i])) + "));\n";
+    }
+    o += "      return true;\n";
+  }
+  o += "    default: return false;\n  }\n}\n\n";
+  o += "__device__ __forceinline__ bool compiled_call_link(uint32_t fid, uint32_t i, uint32_t nb, uint32_t vb, Port caller,\n";
+  o += "                                                   Port& x, Port& y) {\n";
+  o += "  (void)i; (void)nb; (void)vb; (void)caller; (void)x; (void)y;\n";
+  o += "  switch (fid) {\n";
+  for (size_t f = 0; f < defs.size(); f++) {
+    if (!pick[f]) continue;
+    snprintf(line, sizeof line, "    case %zuu:  // %s\n      switch (i) {\n", f, defs[f].name.c_str());
+    o += line;
+    const Pair* links = flat.data() + hdr[f].off;
+    for (uint32_t i = 0; i < hdr[f].rbag_len; i++) {
+      snprintf(line, sizeof line, "        case %uu: x = ", i);
+      o += line + port(get_fst(links[i])) + "; y = " + port(get_snd(links[i])) + "; return true;\n";
+    }
+    o += "        default: return false;\n      }\n";
+  }
+  o += "    default: return false;\n  }\n}\n\n";
+  snprintf(line, sizeof line, "uint64_t compiled_book_hash() { return 0x%016llxull; }\n",
+           (unsigned long long)tables_hash(hdr, flat));
+  o += line;
+  o += "}  // namespace hvm\n";
+  return o;
+}
+
 class Runtime {
  public:
   hvm_gb300_config cfg;
@@ -1124,22 +1296,15 @@ class Runtime {
   }
 
   int upload_book() {
-    std::vector<DefHdr> hdr(defs.size());
+    std::vector<DefHdr> hdr;
     std::vector<Pair> flat;
-    max_def_nodes = 1;
-    max_def_vars = 1;
-    for (size_t f = 0; f < defs.size(); f++) {
-      const HostDef& h = defs[f];
-      std::vector<Pair> links, nodes;
-      uint32_t vars_len = 0;
-      join_links(h, links, nodes, vars_len);
-      hdr[f] = DefHdr{h.node_len, (uint32_t)links.size(), vars_len, h.safe ? 1u : 0u, 0, (uint32_t)flat.size(), 1, 0};
-      flat.insert(flat.end(), links.begin(), links.end());
-      flat.insert(flat.end(), nodes.begin(), nodes.end());
-      if (h.node_len > max_def_nodes) max_def_nodes = h.node_len;
-      if (vars_len > max_def_vars) max_def_vars = vars_len;
-    }
-    if (flat.empty()) flat.push_back(0);
+    def_tables(defs, hdr, flat, max_def_nodes, max_def_vars);
+#ifdef HVM_COMPILED_CALLS
+    // A program with compiled calls evaluates the book it was emitted for.
+    if (tables_hash(hdr, flat) != compiled_book_hash())
+      return fail("this program's compiled calls were emitted for another book");
+    d.compiled = 1;
+#endif
     // Device buffers are kept between loads and grown only when a book needs
     // more (cudaFree synchronises the device; a reload should not).
     auto ensure = [&](void*& p, size_t& have, size_t need) -> int {
@@ -2010,6 +2175,25 @@ class Runtime {
 struct hvm_gb300_runtime {
   hvm::Runtime rt;
 };
+
+extern "C" int hvm_gb300_compile_calls(const uint32_t* book, size_t words, char* out, size_t out_cap,
+                                       size_t* out_len, char* err, size_t err_cap) {
+  auto put_err = [&](const std::string& m) {
+    if (err && err_cap) {
+      size_t k = std::min(m.size(), err_cap - 1);
+      memcpy(err, m.data(), k);
+      err[k] = 0;
+    }
+  };
+  hvm::Runtime parser;  // parse_book only: no device state is created
+  std::vector<hvm::HostDef> defs;
+  if (parser.parse_book(book, words, defs)) { put_err(parser.err); return 1; }
+  const std::string src = hvm::compiled_calls_source(defs);
+  if (out_len) *out_len = src.size();
+  if (out && out_cap > src.size()) { memcpy(out, src.data(), src.size()); out[src.size()] = 0; }
+  else if (out) { put_err("output buffer too small"); return 3; }
+  return 0;
+}
 
 extern "C" void hvm_gb300_default_config(hvm_gb300_config* c) {
   memset(c, 0, sizeof(*c));

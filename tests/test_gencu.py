@@ -9,6 +9,7 @@ import re
 import shutil
 import subprocess
 
+import numpy as np
 import pytest
 
 from conftest import parse_output
@@ -17,9 +18,9 @@ NVCC = shutil.which("nvcc") or "/usr/local/cuda/bin/nvcc"
 NVCC_FLAGS = ["-gencode", "arch=compute_103a,code=sm_103a", "-O3", "-std=c++17"]
 
 
-def gen_cu(hvm, path) -> str:
-    return subprocess.run([hvm.CLI_PATH, "gen-cu", str(path)], capture_output=True, text=True,
-                          check=True).stdout
+def gen_cu(hvm, path, compiled: bool = False) -> str:
+    cmd = [hvm.CLI_PATH, "gen-cu"] + (["--compiled"] if compiled else []) + [str(path)]
+    return subprocess.run(cmd, capture_output=True, text=True, check=True).stdout
 
 
 def compile_cu(src: str, tmp_path, name: str) -> str:
@@ -47,14 +48,40 @@ def test_gen_cu_embeds_the_book_and_compiles(hvm, tmp_path, ref_programs):
     compile_cu(out, tmp_path, "list")
 
 
+def test_compiled_calls_source(hvm, workloads):
+    # One straight-line case per def with nodes / links, the def words as
+    # immediates relative to the fresh bases, and the book's hash.
+    code = workloads.bitonic_sort(8)
+    src = hvm.compile_calls(code)
+    assert src == hvm.compile_calls(hvm.book_from_text(code))  # text or serialized words
+    ndefs = int(hvm.book_from_text(code)[0])
+    cases = re.findall(r"^    case (\d+)u:", src, re.M)
+    assert 0 < len(cases) <= 2 * ndefs and all(int(c) < ndefs for c in cases)
+    assert "compiled_call_nodes" in src and "compiled_call_link" in src
+    assert re.search(r"nstore\(d, nb \+ 0u, new_pair\(", src)
+    assert re.search(r"uint64_t compiled_book_hash\(\) \{ return 0x[0-9a-f]{16}ull; \}", src)
+    with pytest.raises(hvm.HvmError):
+        hvm.compile_calls(np.zeros(1, dtype=np.uint32))  # an empty book
+
+
+def test_gen_cu_compiled_compiles(hvm, tmp_path, workloads):
+    src_file = tmp_path / "bitonic.hvm"
+    src_file.write_text(workloads.bitonic_sort(8))
+    out = gen_cu(hvm, src_file, compiled=True)
+    assert out.index("#define HVM_COMPILED_CALLS") < out.index("namespace hvm")
+    assert out.index("compiled_book_hash() {") < out.index("static const uint32_t BOOK_BUF")
+    compile_cu(out, tmp_path, "bitonic_compiled")
+
+
 @pytest.mark.gpu
+@pytest.mark.parametrize("compiled", [False, True])
 @pytest.mark.parametrize("name", ["tests/programs/list.hvm", "tests/programs/numerics/f24.hvm",
-                                  "examples/tuples/tuples.hvm"])
-def test_gen_cu_program_matches_run_cu(hvm, tmp_path, ref_programs, name):
+                                  "examples/tuples/tuples.hvm", "examples/sort_bitonic/main.hvm"])
+def test_gen_cu_program_matches_run_cu(hvm, tmp_path, ref_programs, name, compiled):
     prog = next(p for p in ref_programs if p["name"] == name)
     src_file = tmp_path / "prog.hvm"
     src_file.write_text(prog["code"])
-    exe = compile_cu(gen_cu(hvm, src_file), tmp_path, "prog")
+    exe = compile_cu(gen_cu(hvm, src_file, compiled), tmp_path, "prog")
     got = parse_output(subprocess.run([exe], capture_output=True, text=True, check=True, timeout=300).stdout)
     assert got["itrs"] == prog["itrs"]
     assert hvm.canonical(got["result"]) == hvm.canonical(prog["result"])
