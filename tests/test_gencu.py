@@ -64,6 +64,46 @@ def test_compiled_calls_source(hvm, workloads):
         hvm.compile_calls(np.zeros(1, dtype=np.uint32))  # an empty book
 
 
+def _hot_defs(code: str) -> set[str]:
+    # Defs on a cycle of the REF graph, and every def those reach.
+    body: dict[str, str] = {}
+    name = None
+    for line in code.splitlines():
+        m = re.match(r"^@([\w.\-/]+)\s*=(.*)$", line)
+        if m:
+            name = m.group(1)
+            body[name] = m.group(2)
+        elif name is not None:
+            body[name] += " " + line
+    refs = {n: set(re.findall(r"@([\w.\-/]+)", b)) & body.keys() for n, b in body.items()}
+
+    def reach(src: str) -> set[str]:
+        seen, todo = set(), [src]
+        while todo:
+            for w in refs[todo.pop()]:
+                if w not in seen:
+                    seen.add(w)
+                    todo.append(w)
+        return seen
+
+    cyclic = {n for n in body if n in reach(n)}
+    hot = set(cyclic)
+    for n in cyclic:
+        hot |= reach(n)
+    return hot
+
+
+@pytest.mark.parametrize("make", [lambda W: W.bitonic_sort(8), lambda W: W.tree_sum(12),
+                                  lambda W: W.skewed_fold(10), lambda W: W.countdown(1000)],
+                         ids=["bitonic_2p8", "tree_sum_d12", "skewed_fold_2p10", "countdown_1000"])
+def test_compiled_calls_pick_the_recursive_defs(hvm, workloads, make):
+    code = make(workloads)
+    src = hvm.compile_calls(code)
+    got = set(re.findall(r"^    case \d+u:  // (\S+)$", src, re.M))
+    assert got == _hot_defs(code)
+    assert "main" not in got
+
+
 def test_gen_cu_compiled_compiles(hvm, tmp_path, workloads):
     src_file = tmp_path / "bitonic.hvm"
     src_file.write_text(workloads.bitonic_sort(8))
