@@ -63,6 +63,23 @@ def test_live_oracle_seeded_nets(hvm, rt, workloads, oracle):
         assert hvm.canonical(res) == hvm.canonical(want["result"])
 
 
+@pytest.mark.parametrize("cfg", [dict(narrow_below=0), dict(narrow_below=1 << 30),
+                                 dict(narrow_below=4096, narrow_reg_cap=5), dict(reg_cap_blocks=0, narrow_reg_cap=8)],
+                         ids=["one_variant", "always_narrow", "narrow_cap5", "narrow_wider_than_wide"])
+def test_kernel_variant_switching(hvm, workloads, config_goldens, cfg):
+    # Turns move between the two kernel variants (different grids) at host
+    # polls; the next turn is re-planned for the new grid. Every setting gives
+    # the reference's interaction count and normal form.
+    cases = {"tree_sum_d12": workloads.tree_sum(12), "bitonic_sort_2p12": workloads.bitonic_sort(12),
+             "skewed_fold_2p10": workloads.skewed_fold(10), "countdown_100000": workloads.countdown(100000)}
+    with hvm.Runtime(device=0, **cfg) as r:
+        for name, code in cases.items():
+            res, st = run(r, code)
+            g = config_goldens[name]
+            assert st.itrs == g["itrs"], name
+            assert hashlib.sha256(hvm.canonical(res).encode()).hexdigest() == g["canonical_sha256"], name
+
+
 def test_repeat_runs_identical(hvm, rt, workloads):
     code = workloads.bitonic_sort(10)
     outs = {run(rt, code)[0] for _ in range(3)}
