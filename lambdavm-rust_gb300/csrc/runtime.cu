@@ -839,6 +839,19 @@ static std::vector<bool> recursive_defs(const std::vector<HostDef>& defs) {
   return rec;
 }
 
+// A def name as it may appear in a `//` comment of generated code: the
+// front-end's name characters, anything else (a trailing backslash would
+// splice the next line into the comment) as '?'.
+static std::string comment_name(const std::string& name) {
+  std::string r;
+  for (char ch : name) {
+    const bool ok = (ch >= 'a' && ch <= 'z') || (ch >= 'A' && ch <= 'Z') || (ch >= '0' && ch <= '9') || ch == '_' ||
+                    ch == '.' || ch == '-' || ch == '/';
+    r += ok ? ch : '?';
+  }
+  return r;
+}
+
 // CUDA source of the compiled calls for a book (see compiled_call_nodes in
 // the evaluator): per recursive def, its node stores and its links with the
 // fresh node / var bases added to the def-local indices.
@@ -877,8 +890,7 @@ static std::string compiled_calls_source(const std::vector<HostDef>& defs) {
   o += "  switch (fid) {\n";
   for (size_t f = 0; f < defs.size(); f++) {
     if (!pick[f]) continue;
-    snprintf(line, sizeof line, "    case %zuu:  // %s\n", f, defs[f].name.c_str());
-    o += line;
+    o += "    case " + std::to_string(f) + "u:  // " + comment_name(defs[f].name) + "\n";
     const Pair* nodes = flat.data() + hdr[f].off + hdr[f].rbag_len;
     for (uint32_t i = 0; i < hdr[f].node_len; i++) {
       snprintf(line, sizeof line, "      nstore(d, nb + %uu, new_pair(", i);
@@ -893,8 +905,7 @@ static std::string compiled_calls_source(const std::vector<HostDef>& defs) {
   o += "  switch (fid) {\n";
   for (size_t f = 0; f < defs.size(); f++) {
     if (!pick[f]) continue;
-    snprintf(line, sizeof line, "    case %zuu:  // %s\n      switch (i) {\n", f, defs[f].name.c_str());
-    o += line;
+    o += "    case " + std::to_string(f) + "u:  // " + comment_name(defs[f].name) + "\n      switch (i) {\n";
     const Pair* links = flat.data() + hdr[f].off;
     for (uint32_t i = 0; i < hdr[f].rbag_len; i++) {
       snprintf(line, sizeof line, "        case %uu: x = ", i);

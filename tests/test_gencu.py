@@ -104,6 +104,21 @@ def test_compiled_calls_pick_the_recursive_defs(hvm, workloads, make):
     assert "main" not in got
 
 
+def test_compiled_calls_long_names(hvm, workloads):
+    # Def names of any length end up whole in the generated comments, one
+    # case per line, so no generated statement can fall into a comment.
+    long = "loop_" + "x" * 200
+    code = workloads.countdown(1000).replace("@loop", "@" + long)
+    src = hvm.compile_calls(code)
+    cases = re.findall(r"^    case \d+u:  // (.*)$", src, re.M)
+    assert sorted(set(cases)) == sorted({long, long + "__C0"})
+    # Apart from the comments, the code is the short-named program's.
+    short = hvm.compile_calls(workloads.countdown(1000))
+    strip = lambda t: re.sub(r"//[^\n]*", "", t)
+    assert strip(src) == strip(short)
+    assert "nstore(" in strip(src)
+
+
 def test_gen_cu_compiled_compiles(hvm, tmp_path, workloads):
     src_file = tmp_path / "bitonic.hvm"
     src_file.write_text(workloads.bitonic_sort(8))
