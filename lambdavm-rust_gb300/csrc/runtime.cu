@@ -688,12 +688,24 @@ struct HostDef {
 // not allocate, publish and take it (two atomic exchanges and a fence). The
 // remaining vars are renumbered densely. Interactions and normal forms are
 // unchanged: the same redexes are formed, only without the detour.
-static void join_links(const HostDef& h, std::vector<Pair>& links, std::vector<Pair>& nodes, uint32_t& vars_len) {
+// Scratch buffers of join_links, reused from def to def (a book may hold
+// thousands of defs; their loading is on the host's critical path).
+struct JoinScratch {
   struct L { Port x, y; bool live; };
   std::vector<L> ls;
+  std::vector<uint8_t> in_node;
+  std::vector<uint32_t> map;
+};
+
+static void join_links(const HostDef& h, std::vector<Pair>& links, std::vector<Pair>& nodes, uint32_t& vars_len,
+                       JoinScratch& sc) {
+  using L = JoinScratch::L;
+  std::vector<L>& ls = sc.ls;
+  ls.clear();
   for (Pair p : h.rbag) ls.push_back({get_fst(p), get_snd(p), true});
   ls.push_back({h.root, CALLER_PORT, true});
-  std::vector<uint8_t> in_node(h.vars_len, 0);
+  std::vector<uint8_t>& in_node = sc.in_node;
+  in_node.assign(h.vars_len, 0);
   for (Pair p : h.node)
     for (Port q : {get_fst(p), get_snd(p)})
       if (get_tag(q) == VAR) in_node[get_val(q)] = 1;
@@ -722,7 +734,8 @@ static void join_links(const HostDef& h, std::vector<Pair>& links, std::vector<P
     }
   }
   // Dense renumbering of the vars still in use.
-  std::vector<uint32_t> map(h.vars_len, ~0u);
+  std::vector<uint32_t>& map = sc.map;
+  map.assign(h.vars_len, ~0u);
   uint32_t next = 0;
   auto renum = [&](Port q) -> Port {
     if (q == CALLER_PORT || get_tag(q) != VAR) return q;
@@ -744,13 +757,17 @@ static void def_tables(const std::vector<HostDef>& defs, std::vector<DefHdr>& hd
                        uint32_t& max_nodes, uint32_t& max_vars) {
   hdr.assign(defs.size(), DefHdr{});
   flat.clear();
+  size_t words = 1;
+  for (const HostDef& h : defs) words += h.rbag.size() + 1 + h.node.size();
+  flat.reserve(words);
   max_nodes = 1;
   max_vars = 1;
+  JoinScratch sc;
+  std::vector<Pair> links, nodes;
   for (size_t f = 0; f < defs.size(); f++) {
     const HostDef& h = defs[f];
-    std::vector<Pair> links, nodes;
     uint32_t vars_len = 0;
-    join_links(h, links, nodes, vars_len);
+    join_links(h, links, nodes, vars_len, sc);
     hdr[f] = DefHdr{h.node_len, (uint32_t)links.size(), vars_len, h.safe ? 1u : 0u, 0, (uint32_t)flat.size(), 1, 0};
     flat.insert(flat.end(), links.begin(), links.end());
     flat.insert(flat.end(), nodes.begin(), nodes.end());
