@@ -3,6 +3,11 @@ runtime outputs (tests/golden/*.json): same normal form and same interaction
 count, with one worker and with several (work stealing)."""
 from __future__ import annotations
 
+import os
+import re
+import subprocess
+import tempfile
+
 import pytest
 
 
@@ -41,3 +46,38 @@ def test_oracle_planted_mistake_is_caught(hvm, oracle, ref_programs):
     assert bad != p["code"]
     out = oracle(bad)
     assert hvm.canonical(out["result"]) != hvm.canonical(p["result"])
+
+
+REF_BIN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "..", "oracle", "_ref", "hvm_ref")
+
+
+def _run_reference_runtime(hvm, code: str) -> dict:
+    buf = hvm.book_from_text(code)
+    with tempfile.NamedTemporaryFile(suffix=".bin", delete=False) as f:
+        buf.tofile(f.name)
+        path = f.name
+    try:
+        r = subprocess.run([REF_BIN, path], capture_output=True, text=True, timeout=600)
+    finally:
+        os.unlink(path)
+    assert r.returncode == 0, r.stderr
+    return {"result": re.search(r"^Result: (.*)$", r.stdout, re.M).group(1),
+            "itrs": int(re.search(r"^- ITRS: (\d+)$", r.stdout, re.M).group(1))}
+
+
+@pytest.mark.skipif(not os.path.exists(REF_BIN),
+                    reason="the reference's C runtime is built only where its sources are")
+@pytest.mark.parametrize("make", [
+    lambda W: W.bitonic_sum(6, 11), lambda W: W.bitonic_sum(7, 12), lambda W: W.bitonic_sum(8, 13),
+    lambda W: W.bitonic_sort(7, seed=99), lambda W: W.skewed_fold(9, seed=7), lambda W: W.skewed_fold(8, seed=8),
+    lambda W: W.tree_sum(9), lambda W: W.countdown(777),
+], ids=["bsum6_s11", "bsum7_s12", "bsum8_s13", "bitonic7_s99", "skewed9_s7", "skewed8_s8", "tree9", "count777"])
+def test_oracle_matches_reference_runtime_live(hvm, oracle, workloads, make):
+    # Seeded nets that no golden holds: the restatement against the
+    # reference's own C runtime, run here on the same buffers.
+    code = make(workloads)
+    want = _run_reference_runtime(hvm, code)
+    for threads in (1, 3):
+        got = oracle(code, threads=threads)
+        assert got["itrs"] == want["itrs"], threads
+        assert hvm.canonical(got["result"]) == hvm.canonical(want["result"]), threads
