@@ -81,3 +81,47 @@ def test_oracle_matches_reference_runtime_live(hvm, oracle, workloads, make):
         got = oracle(code, threads=threads)
         assert got["itrs"] == want["itrs"], threads
         assert hvm.canonical(got["result"]) == hvm.canonical(want["result"]), threads
+
+
+REF_SRC = os.environ.get("REF_SRC", "/root/reference/src")
+
+
+@pytest.mark.skipif(not os.path.exists(os.path.join(REF_SRC, "hvm.c")),
+                    reason="the reference's C sources exist only where the reference is checked out")
+def test_gen_c_compiled_mode_matches_run_c(hvm, workloads, ref_programs, config_goldens):
+    # The reference's compiled C mode (`hvm gen-c`: per-def C functions with
+    # the SWITCH / OPER / COPY / ANNI / VOID fast paths, restated by
+    # oracle/gen_c.py and spliced into the reference's own hvm.c/run.c) gives
+    # the same normal forms and the same interaction counts as `hvm run-c`,
+    # with one worker and with four: each fast path counts exactly the
+    # interactions it short-cuts.
+    import hashlib
+    import importlib.util
+    from concurrent.futures import ThreadPoolExecutor
+    spec = importlib.util.spec_from_file_location(
+        "gen_c", os.path.join(os.path.dirname(os.path.abspath(__file__)), "..", "oracle", "gen_c.py"))
+    gen_c = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(gen_c)
+    jobs = []
+    for p in ref_programs:
+        if "result" in p:
+            jobs.append((re.sub(r"\W", "_", p["name"]), p["code"], p["itrs"], lambda r, p=p: hvm.canonical(r) ==
+                         hvm.canonical(p["result"])))
+    makers = {"tree_sum_d12": workloads.tree_sum(12), "bitonic_sort_2p8": workloads.bitonic_sort(8),
+              "skewed_fold_2p10": workloads.skewed_fold(10), "countdown_100000": workloads.countdown(100000)}
+    for name, code in makers.items():
+        g = config_goldens[name]
+        jobs.append((name, code, g["itrs"], lambda r, g=g: hashlib.sha256(hvm.canonical(r).encode()).hexdigest() ==
+                     g["canonical_sha256"]))
+
+    def check(job):
+        name, code, itrs, same = job
+        words = hvm.book_from_text(code)
+        return [(name, t, out["itrs"] == itrs, same(out["result"]))
+                for t in (0, 2) for out in [gen_c.build_and_run(words, name, tpc_l2=t)]]
+
+    with ThreadPoolExecutor(max_workers=8) as ex:
+        rows = [r for rs in ex.map(check, jobs) for r in rs]
+    assert len(rows) >= 30
+    for name, t, itrs_ok, nf_ok in rows:
+        assert itrs_ok and nf_ok, (name, t)
