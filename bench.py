@@ -24,6 +24,7 @@ import ctypes
 import hashlib
 import importlib
 import json
+import math
 import os
 import re
 import statistics
@@ -41,6 +42,16 @@ GOLDEN = os.path.join(ROOT, "tests", "golden", "configs.json")
 PEAKS = os.path.join(ROOT, "MEASURED_PEAKS.json")
 TRAFFIC = os.path.join(ROOT, "profiles", "turn_kernel_bitonic_2p14.md")
 ORACLE = os.path.join(ROOT, "oracle", "_build", "hvm_oracle")
+REF_C = os.path.join(ROOT, "oracle", "_ref", "hvm_ref")
+REF_CU = os.path.join(ROOT, "oracle", "_ref", "hvm_ref_cu")
+REF_PROGRAMS = os.path.join(ROOT, "tests", "golden", "reference_programs.json")
+# The reference CUDA runtime's global allocator loops forever once a thread's
+# slice of the node space is full (src/hvm.cu:880-893: it prints "OOM" and
+# keeps scanning); on the bitonic sorts of these configs it did, and it was
+# stopped by a timeout. It is run only on the workloads where it completed.
+REF_CU_UNAVAILABLE = ("the reference CUDA runtime never finished the bitonic-sort configs: on the 2^12-key sort "
+                      "its global allocator looped printing OOM (src/hvm.cu:880-893) until a 240 s timeout killed "
+                      "it, so it is not run on them")
 
 BATCH_GOLDEN = os.path.join(ROOT, "tests", "golden", "batch_mixed_4096.json")
 
@@ -346,6 +357,7 @@ def read_traffic_per_itr() -> float | None:
 
 
 def run_oracle(book, threads: int) -> tuple[int, float, str]:
+    """The oracle port (oracle/hvm_oracle.c); seconds = its normalisation time."""
     with tempfile.NamedTemporaryFile(suffix=".bin", delete=False) as f:
         book.tofile(f.name)
         path = f.name
@@ -360,36 +372,183 @@ def run_oracle(book, threads: int) -> tuple[int, float, str]:
     return itrs, ns / 1e9, res
 
 
+def run_reference_c(path: str) -> tuple[int, float, str]:
+    """The reference's own C runtime (`hvm run-c`: src/run.c + src/hvm.c built
+    by oracle/Makefile) on a book file. Seconds = its own TIME (boot,
+    normalise, readback and print, src/hvm.c:1759-1779), taken at full
+    precision from its MIPS line."""
+    out = subprocess.run([REF_C, path], capture_output=True, text=True, check=True, timeout=1800).stdout
+    itrs = int(re.search(r"^- ITRS: (\d+)$", out, re.M).group(1))
+    mips = float(re.search(r"^- MIPS: ([0-9.]+)$", out, re.M).group(1))
+    res = re.search(r"^Result: (.*)$", out, re.M).group(1)
+    return itrs, itrs / (mips * 1e6), res
+
+
+def reference_threads() -> int:
+    """Worker threads of the reference's C runtime: 2^TPC_L2 with TPC_L2 =
+    floor(log2(cores)) (build.rs:2-3; oracle/Makefile uses the same)."""
+    return 1 << int(math.log2(os.cpu_count() or 1))
+
+
+def cpu_reference_available() -> bool:
+    return os.access(REF_C, os.X_OK)
+
+
+def ensure_oracles() -> None:
+    """Builds the CPU checkers only (never this repository's library)."""
+    if not os.path.exists(ORACLE):
+        subprocess.run(["make", "-s", "-C", os.path.join(ROOT, "oracle")], check=True)
+    if not cpu_reference_available() and os.path.isfile(os.path.join(ROOT, "oracle", "_ref", "src", "run.c")):
+        subprocess.run(["make", "-s", "-C", os.path.join(ROOT, "oracle"), "ref"], check=True)
+
+
+def oracle_module():
+    """oracle/book.py: the reference's front-end and result canonicaliser
+    restated in Python (test infrastructure)."""
+    if os.path.join(ROOT, "oracle") not in sys.path:
+        sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    return importlib.import_module("book")
+
+
+def arm_config(desc: str, golden: dict) -> dict:
+    """The `config` both arms print (identical, so the lines compare)."""
+    return {"workload": desc, "itrs_per_step": golden["itrs"],
+            "l2": "each step clears the 6 GB node/var space (> L2) before evaluating",
+            "parity": "interaction count checked every step; normal form SHA-256 checked"}
+
+
+def canon_sha(canonical, text: str) -> str:
+    return hashlib.sha256(canonical(text).encode()).hexdigest()
+
+
+def time_cpu_reference(book, golden, canonical, runs: int) -> dict:
+    """cpu_baseline: the reference's `hvm run-c` (or, where it was not built,
+    the oracle port) on this host's cores, `runs` full evaluations; parity
+    checked on every run."""
+    if cpu_reference_available():
+        with tempfile.NamedTemporaryFile(suffix=".bin", delete=False) as f:
+            book.tofile(f.name)
+            path = f.name
+        try:
+            secs = []
+            for _ in range(runs):
+                itrs, s, res = run_reference_c(path)
+                if itrs != golden["itrs"] or canon_sha(canonical, res) != golden["canonical_sha256"]:
+                    raise SystemExit("the reference C runtime disagrees with its own golden")
+                secs.append(s)
+        finally:
+            os.unlink(path)
+        kind, cores = "reference", reference_threads()
+        sample = (f"{runs} full evaluation(s) of the same workload ({golden['itrs']} interactions) by the "
+                  f"reference's hvm_c (src/run.c + src/hvm.c, -O3 -DIO), {cores} worker threads; time = its "
+                  "own TIME (boot, normalise, print)")
+    else:
+        secs = []
+        for _ in range(runs):
+            itrs, s, _ = run_oracle(book, os.cpu_count() or 1)
+            if itrs != golden["itrs"]:
+                raise SystemExit("oracle interaction count differs from the golden")
+            secs.append(s)
+        kind, cores = "port", os.cpu_count() or 1
+        sample = (f"{runs} full evaluation(s) of the same workload ({golden['itrs']} interactions) by the "
+                  f"oracle port, {cores} worker threads (the reference's sources were not staged)")
+    mean = statistics.mean(secs)
+    return {"value": golden["itrs"] / mean, "unit": UNIT, "cores": cores, "kind": kind, "sample": sample,
+            "seconds": secs}
+
+
+def bench_reference(args, code, golden, desc, ws, rank, canonical):
+    """The reference arm: the reference's own CPU implementation of the path,
+    `hvm run-c` (src/run.c + src/hvm.c compiled from the staged reference
+    sources), on the host cores; the oracle port only where those sources
+    are absent. This process never loads this repository's library: the
+    book comes from the front-end restated in oracle/book.py."""
+    if rank != 0:
+        return None
+    ensure_oracles()
+    book = oracle_module().book_from_text(code)
+    cb = time_cpu_reference(book, golden, canonical, args.warmup + args.steps)
+    times = cb.pop("seconds")[args.warmup:]
+    value = golden["itrs"] / statistics.mean(times)
+    cb["value"] = value
+    return {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": statistics.mean(times) * 1e3,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u32", "data": "synthetic",
+        "config": arm_config(desc, golden),
+        "cpu_baseline": cb,
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+
+
+def run_reference_cu(path: str, timeout: float = 120) -> tuple[int, float, str]:
+    """The reference's own CUDA runtime (src/run.cu + src/hvm.cu rebuilt for
+    sm_103a by oracle/Makefile) on a book file: interaction count, wall time
+    of the hvm_cu call (the driver's `- WALL`), printed result."""
+    out = subprocess.run([REF_CU, path], capture_output=True, text=True, check=True, timeout=timeout).stdout
+    itrs = int(re.search(r"^- ITRS: (\d+)$", out, re.M).group(1))
+    wall = float(re.search(r"^- WALL: ([0-9.]+)s$", out, re.M).group(1))
+    res = re.search(r"^Result: (.*)$", out, re.M)
+    return itrs, wall, res.group(1) if res else ""
+
+
+def bench_reference_cuda(hvm, W, reps: int = 3) -> dict:
+    """The reference's CUDA runtime beside this evaluator on the same GPU, on
+    the workloads where it completes: the recursive tree sum d=20 and the
+    reference's own sum_tree example. Its time is the wall time of the hvm_cu
+    call (context created beforehand) minus that of a one-node book (the
+    call's fixed costs: book upload, the 6 GB net allocation, its init
+    kernel); ours is the wall time of one evaluation with the book resident
+    (hvm_gb300_run). Both checked against the reference C runtime's goldens."""
+    if not os.access(REF_CU, os.X_OK):
+        return {"unavailable": "the reference CUDA runtime was not built (its sources were not staged)"}
+    golden = json.load(open(GOLDEN))
+    progs = {p["name"]: p for p in json.load(open(REF_PROGRAMS))}
+    cases = [("tree_sum_d20", W.tree_sum(20), golden["tree_sum_d20"]),
+             ("examples/sum_tree", progs["examples/sum_tree/main.hvm"]["code"], progs["examples/sum_tree/main.hvm"])]
+    tmp = tempfile.mkdtemp(prefix="hvm_refcu_")
+    out = {"kind": "the reference's src/run.cu + src/hvm.cu (hvm_cu) rebuilt for sm_103a",
+           "bitonic_sort_2p16": {"unavailable": REF_CU_UNAVAILABLE}}
+    try:
+        null = os.path.join(tmp, "null.bin")
+        hvm.book_from_text("@main = 1\n").tofile(null)
+        fixed = statistics.median([run_reference_cu(null)[1] for _ in range(reps)])
+        out["fixed_call_s"] = fixed
+        for name, code, g in cases:
+            path = os.path.join(tmp, name.replace("/", "_") + ".bin")
+            book = hvm.book_from_text(code)
+            book.tofile(path)
+            walls, ok = [], True
+            for _ in range(reps):
+                itrs, wall, res = run_reference_cu(path)
+                walls.append(wall)
+                ok = ok and itrs == g["itrs"] and hvm.canonical(res) == hvm.canonical(g["result"])
+            ref_s = max(statistics.median(walls) - fixed, 1e-9)
+            with hvm.Runtime(device=0) as rt:
+                rt.load(book)
+                st = rt.run()
+                ours_ok = st.itrs == g["itrs"] and hvm.canonical(rt.result()) == hvm.canonical(g["result"])
+                secs = []
+                for _ in range(max(reps, 5)):
+                    t0 = time.perf_counter()
+                    rt.run()
+                    secs.append(time.perf_counter() - t0)
+            ours_s = statistics.median(secs)
+            out[name] = {"itrs": g["itrs"], "reference_cuda": {"value": g["itrs"] / ref_s, "unit": UNIT,
+                                                               "seconds": ref_s, "parity": bool(ok)},
+                         "gb300": {"value": g["itrs"] / ours_s, "unit": UNIT, "seconds": ours_s,
+                                   "parity": bool(ours_ok)},
+                         "gb300_over_reference_cuda": ref_s / ours_s}
+    except (subprocess.SubprocessError, OSError, AttributeError) as e:
+        out["error"] = f"{type(e).__name__}: {e}"[:300]
+    return out
+
+
 def ensure_built():
     pkg = importlib.import_module("lambdavm-rust_gb300")
     if not os.path.exists(pkg.LIB_PATH) or not os.path.exists(ORACLE):
         importlib.import_module("__graft_entry__").build()
     return pkg
-
-
-def bench_reference(args, book, golden, desc, ws, rank):
-    """The reference's CPU evaluator (its work-stealing pthreads algorithm,
-    restated in oracle/hvm_oracle.c) on all host cores, same workload."""
-    if rank != 0:
-        return None
-    threads = os.cpu_count() or 1
-    times = []
-    for i in range(args.warmup + args.steps):
-        itrs, secs, _ = run_oracle(book, threads)
-        if itrs != golden["itrs"]:
-            raise SystemExit(f"oracle interaction count {itrs} != golden {golden['itrs']}")
-        if i >= args.warmup:
-            times.append(secs)
-    value = golden["itrs"] / statistics.mean(times)
-    return {
-        "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws,
-        "steps": args.steps, "warmup": args.warmup, "ms_per_step": statistics.mean(times) * 1e3,
-        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u32", "data": "synthetic",
-        "config": {"workload": desc, "itrs_per_step": golden["itrs"]},
-        "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
-                         "sample": f"full workload ({golden['itrs']} interactions) per step, {threads} worker threads"},
-        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
-    }
 
 
 def bench_gpu(args, hvm, book, golden, desc, ws, rank, local, dist):
@@ -499,19 +658,15 @@ def bench_gpu(args, hvm, book, golden, desc, ws, rank, local, dist):
                            "frac": ach / peak_l2 if ach else None, "peak_2gb_region": peak_far,
                            "frac_of_2gb_region": ach / peak_far if ach else None,
                            "atomics_per_interaction": api, "peak_source": "measured by hvm_gb300_atomic_peak"}
-    # CPU baseline: the oracle port on this host's cores, one full evaluation.
-    threads = os.cpu_count() or 1
-    c_itrs, c_secs, _ = run_oracle(book, threads)
-    cpu = {"value": c_itrs / c_secs, "unit": UNIT, "cores": threads, "kind": "port",
-           "sample": f"one full evaluation of the same workload ({c_itrs} interactions), {threads} worker threads"}
+    # CPU baseline: the reference's run-c on this host's cores, one full evaluation.
+    cpu = time_cpu_reference(book, golden, hvm.canonical, 1)
+    cpu.pop("seconds")
     return {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": secs_max / args.steps * 1e3, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "u32", "data": "synthetic",
-        "config": {"workload": desc, "itrs_per_step": golden["itrs"], "policy": "fixed",
-                   "threads": counters.threads, "parallelism": f"replicas x{ws}",
-                   "l2": "each step clears the 6 GB node/var space (> L2) before evaluating",
-                   "parity": "interaction count checked every step; normal form SHA-256 checked"},
+        "config": arm_config(desc, golden),
+        "run": {"policy": "fixed", "threads": counters.threads, "parallelism": f"replicas x{ws}"},
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
         "gpu_launches": launches,
         "roofline": roofline,
@@ -519,6 +674,28 @@ def bench_gpu(args, hvm, book, golden, desc, ws, rank, local, dist):
         "cpu_baseline": cpu,
         "clocks": clocks,
     }
+
+
+def profile_case(args) -> None:
+    """One benchmark net with small node/var spaces, for profilers: ncu
+    replays each captured kernel many times and saves/restores device memory
+    between passes, so a profiling run should hold little memory and launch
+    few kernels. Prints the interaction count, turns and times (and, with
+    --prof, the turn kernel's per-phase counters)."""
+    hvm = ensure_built()
+    W = importlib.import_module("lambdavm-rust_gb300.workloads")
+    make = {"bitonic": W.bitonic_sort, "tree_sum": W.tree_sum, "skewed": W.skewed_fold}[args.profile_case]
+    with hvm.Runtime(device=0, node_log2=args.space_log2, vars_log2=args.space_log2, ring_log2=24,
+                     profile=1 if args.prof else 0) as rt:
+        rt.load(make(args.log2n))
+        for _ in range(args.runs):
+            st = rt.run()
+            print(f"itrs {st.itrs} turns {st.turns} ms {st.seconds * 1e3:.3f} kernel_ms {st.kernel_ms:.3f}",
+                  flush=True)
+            if args.prof:
+                names = ("rounds", "lanes", "link_steps", "cyc_loop", "cyc_load", "cyc_write", "cyc_fence",
+                         "cyc_link")
+                print(json.dumps(dict(zip(names, st.prof))), flush=True)
 
 
 def main():
@@ -529,11 +706,30 @@ def main():
     ap.add_argument("--impl", choices=["gb300", "reference"], default="gb300")
     ap.add_argument("--workload", choices=sorted(WORKLOADS), default="bitonic_sort_2p16")
     ap.add_argument("--no-batch", action="store_true", help="skip the 4096-net batch report of the default line")
+    ap.add_argument("--profile-case", choices=["bitonic", "tree_sum", "skewed"],
+                    help="evaluate one small case for a profiler instead of benchmarking (see profile_case)")
+    ap.add_argument("--log2n", type=int, default=14, help="--profile-case: keys / depth / elements (log2)")
+    ap.add_argument("--space-log2", type=int, default=26, help="--profile-case: node and var space, 2^k words")
+    ap.add_argument("--runs", type=int, default=1, help="--profile-case: evaluations")
+    ap.add_argument("--prof", action="store_true", help="--profile-case: per-phase cycle counters")
     args = ap.parse_args()
+    if args.profile_case:
+        profile_case(args)
+        return
     ws, rank, local = dist_env()
+    key, make, desc = WORKLOADS[args.workload]
+    if args.impl == "reference" and key is not None:
+        # The package is imported for its pure-Python generators only; books
+        # and the canonical form come from oracle/book.py, so this arm never
+        # loads the repository's library.
+        W = importlib.import_module("lambdavm-rust_gb300.workloads")
+        golden = json.load(open(GOLDEN))[key]
+        line = bench_reference(args, make(W), golden, desc, ws, rank, oracle_module().canonical)
+        if line:
+            print(json.dumps(line), flush=True)
+        return
     hvm = ensure_built()
     W = importlib.import_module("lambdavm-rust_gb300.workloads")
-    key, make, desc = WORKLOADS[args.workload]
     if args.workload == "compiled_calls":
         if args.impl == "reference" or rank != 0:
             if rank == 0:
@@ -581,11 +777,6 @@ def main():
         return
     golden = json.load(open(GOLDEN))[key]
     book = hvm.book_from_text(make(W))
-    if args.impl == "reference":
-        line = bench_reference(args, book, golden, desc, ws, rank)
-        if line:
-            print(json.dumps(line), flush=True)
-        return
     dist = Dist(ws, rank, local, use_cuda=True)
     try:
         line = bench_gpu(args, hvm, book, golden, desc, ws, rank, local, dist)
@@ -593,6 +784,8 @@ def main():
             line["batched"] = bench_batch(hvm, W, args)
             line["batched_learned"] = bench_batch(hvm, W, args, plain_sample=0, policy="learned")
             line["scheduler"] = bench_scheduler(hvm, W)
+        if line is not None:
+            line["reference_cuda"] = bench_reference_cuda(hvm, W)
     finally:
         dist.close()
     if line:

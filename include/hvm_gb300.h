@@ -257,9 +257,9 @@ void hvm_gb300_reset_counters(hvm_gb300_runtime* rt);
 /* ---- Allocation-free evaluation ---------------------------------------------------
  *
  * No counterpart in the reference. For callers that may not allocate device
- * memory -- code that runs while a CUDA graph is being captured elsewhere in
- * the process, or whose device memory belongs to another allocator or pool --
- * this evaluates a small net inside one fixed device array of about 20 MB
+ * memory -- a host whose device memory belongs to another allocator or pool,
+ * or an embedding that must not fail on allocation -- this evaluates a small
+ * net inside one fixed device array of about 20 MB
  * that the library holds on every GPU that loads it, until the process exits.
  * It calls no cudaMalloc, cudaFree or other allocating routine.
  *
@@ -267,12 +267,16 @@ void hvm_gb300_reset_counters(hvm_gb300_runtime* rt);
  * <= 2^18 node/redex pairs in total, <= 32 nodes and <= 32 vars per
  * definition (the reference CUDA loader's own limit is 64); net <= 2^20 node
  * words and 2^20 var words, at most 8,192 words of each kind per thread of
- * the fixed 2,048-thread grid; normal form <= 2^16 entries. A book beyond
- * the book limits is rejected with a message in `err`; a net that outgrows
- * the memory limits fails with "out of node memory".
+ * the fixed 2,048-thread grid; at most 2^18 redexes pending at once (the
+ * fixed redex ring); normal form <= 2^16 entries. A book beyond the book
+ * limits is rejected with a message in `err`; a net that outgrows the memory
+ * limits fails with "out of node memory", one that outgrows the ring with
+ * "redex ring overflow".
  *
- * Same evaluation as hvm_gb300_run on the current device: boot @main, normalise,
- * readback expansion. The normal form is returned breadth-first: out_ports[k]
+ * Same evaluation as hvm_gb300_run on the current device (boot @main,
+ * normalise, readback expansion) without the IO layer: a normal form that
+ * asks for an IO call is refused with an error. Its copies, memsets and
+ * launches are synchronous calls on the default stream. The normal form is returned breadth-first: out_ports[k]
  * is a port with its var chain resolved; for a node port (CON, DUP, OPR, SWI)
  * its two children are entries out_kids[k] and out_kids[k] + 1 (out_kids is
  * meaningless for other ports). `*out_len` receives the entry count and

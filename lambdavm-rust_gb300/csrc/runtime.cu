@@ -30,6 +30,7 @@
 #include <cstdlib>
 #include <cstring>
 #include <string>
+#include <mutex>
 #include <vector>
 
 #include "hvm_defs.h"
@@ -2448,11 +2449,11 @@ extern "C" void hvm_cu(const uint32_t* book_buffer) {
 // hvm_gb300_run_noalloc evaluates a small net without allocating any memory:
 // the whole net (node and var spaces, redex ring, page lists, control block,
 // book tables and the readback buffers) lives in one fixed device array of
-// NOALLOC_ARENA_BYTES. It serves callers that may not call cudaMalloc — code
-// running while a CUDA graph is being captured elsewhere in the process, a
+// NOALLOC_ARENA_BYTES. It serves callers that may not call cudaMalloc — a
 // host whose device memory is owned by another allocator or a pool that must
 // not fragment, or an embedding that has to guarantee the call cannot fail on
-// allocation. The array is held by every GPU that loads the library until the
+// allocation. Its copies, memsets and launches are synchronous calls on the
+// default stream. The array is held by every GPU that loads the library until the
 // process exits. All calls share it, so calls that overlap on the GPU race
 // with each other; each call clears what must start at zero before it runs.
 // The first call on a device resolves the array's device address
@@ -2498,6 +2499,7 @@ namespace noalloc {
 
 constexpr int MAX_DEVICES = 64;
 static unsigned char* g_arena_dev[MAX_DEVICES];  // device address of the arena, per device
+static std::mutex g_arena_mu;                    // guards g_arena_dev (first calls from several threads)
 
 // Builds the device book tables from the raw buffer already in the arena:
 // thread 0 lays out the def headers (the host has validated the buffer),
@@ -2610,10 +2612,12 @@ static int expand(Ctx& x, Port p, Port& out) {
   return 0;
 }
 
-// The IO loop's constructor walk without IO builtins (src/run.c:65-97, 740-810).
+// The IO loop's constructor walk (src/run.c:65-97, 778-810). A normal form
+// that asks for an IO call is refused: this entry point has no IO layer.
 static int readback_walk(Ctx& x) {
-  Port root, lam, app, arg;
+  Port root, lam, app, arg, first = 0;
   Pair n;
+  uint32_t tag, nargs = 0;
   if (peek(x, ROOT, root) || expand(x, root, lam)) return -1;
   if (get_tag(lam) != CON) return 0;
   if (node_load(x, get_val(lam), n) || expand(x, get_fst(n), app)) return -1;
@@ -2621,10 +2625,18 @@ static int readback_walk(Ctx& x) {
   Pair app_n;
   if (node_load(x, get_val(app), app_n) || expand(x, get_fst(app_n), arg)) return -1;
   if (get_tag(arg) != NUM) return 0;
+  tag = get_u24(get_val(arg));
   for (;;) {
     if (expand(x, get_snd(app_n), app)) return -1;
     if (get_tag(app) != CON) break;
     if (node_load(x, get_val(app), app_n) || expand(x, get_fst(app_n), arg)) return -1;
+    if (nargs++ == 0) first = arg;
+  }
+  if (tag == IO_CALL_TAG && nargs >= 1 && get_tag(first) == CON) {
+    Pair magic;
+    if (node_load(x, get_val(first), magic)) return -1;
+    if (get_val(get_fst(magic)) == new_u24(IO_MAGIC_0) && get_val(get_snd(magic)) == new_u24(IO_MAGIC_1))
+      return failf(x, "IO calls are not supported by hvm_gb300_run_noalloc");
   }
   return 0;
 }
@@ -2681,12 +2693,16 @@ extern "C" int hvm_gb300_run_noalloc(const uint32_t* book, size_t words, uint32_
   int dev = 0;
   if (cuda_ok(x, cudaGetDevice(&dev))) return -1;
   if (dev < 0 || dev >= MAX_DEVICES) return failf(x, "device ordinal out of range", dev);
-  if (!g_arena_dev[dev]) {
-    void* p = nullptr;
-    if (cuda_ok(x, cudaGetSymbolAddress(&p, g_noalloc_arena))) return -1;
-    g_arena_dev[dev] = (unsigned char*)p;
+  unsigned char* A = nullptr;
+  {
+    std::lock_guard<std::mutex> lock(g_arena_mu);
+    if (!g_arena_dev[dev]) {
+      void* p = nullptr;
+      if (cuda_ok(x, cudaGetSymbolAddress(&p, g_noalloc_arena))) return -1;
+      g_arena_dev[dev] = (unsigned char*)p;
+    }
+    A = g_arena_dev[dev];
   }
-  unsigned char* A = g_arena_dev[dev];
   x.arena = A;
   if (validate(x, book, words)) return -1;
 

@@ -39,7 +39,7 @@ def _worker(rank: int, ws: int, port: int, out):
         d.barrier()
         secs = d.max(1.0 + rank)           # slowest replica's timed region
         itrs = d.sum(1000.0 * (rank + 1))  # interactions of all replicas
-        ref = bench.bench_reference(None, None, None, None, ws_, rank_) if rank_ != 0 else "rank0"
+        ref = bench.bench_reference(None, None, None, None, ws_, rank_, None) if rank_ != 0 else "rank0"
         out.put((rank_, secs, itrs, ref))
     finally:
         d.close()

@@ -139,3 +139,27 @@ def test_snapshots_match_reference_c_runtime(hvm, ref_programs):
         assert hvm.canonical(p["result"]) == hvm.canonical(p["snapshot"]), p["name"]
         checked += 1
     assert checked >= 10
+
+
+def test_python_restatement_matches_library(hvm, ref_programs, workloads):
+    """oracle/book.py (the front-end restated in Python, used by the bench's
+    reference arm so that it never loads this library) and the library's C++
+    front-end serialise every reference program, IO program and seeded
+    workload to the same words."""
+    import json
+    import os
+    import sys
+    sys.path.insert(0, os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))), "oracle"))
+    import book as pybook
+
+    io = json.load(open(os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "io_programs.json")))
+    cases = [p["code"] for p in ref_programs if p["code"].strip()]
+    cases += [p["code"] for p in io["programs"]]
+    cases += [workloads.tree_sum(12), workloads.bitonic_sort(10), workloads.skewed_fold(10),
+              workloads.countdown(1000), workloads.bitonic_sum(6, 7)]
+    for code in cases:
+        a = hvm.book_from_text(code)
+        b = pybook.book_from_text(code)
+        assert a.shape == b.shape and (a == b).all()
+    with pytest.raises(pybook.ParseError):
+        pybook.book_from_text("")

@@ -1,12 +1,12 @@
 """The allocation-free entry point, hvm_gb300_run_noalloc.
 
-Some callers cannot allocate device memory while they evaluate a net: code
-that runs while another part of the process is capturing a CUDA graph, or a
-host whose device memory is handed out by its own pool. The entry point
-evaluates a small net inside a fixed device array the library holds, and
-must give exactly what the normal entry point gives: the same normal form
-and the same interaction count, on two calls in a row (the second call runs
-on an array the first one left dirty).
+Some callers cannot allocate device memory while they evaluate a net: a
+host whose device memory is handed out by its own pool or allocator, or an
+embedding that must not fail on an allocation. The entry point evaluates a
+small net inside a fixed device array the library holds, and must give
+exactly what the reference's C runtime gives (its golden normal form and
+interaction count) and what the normal entry point gives, on two calls in a
+row (the second call runs on an array the first one left dirty).
 
 This file is collected last on purpose, so a run that stops at the first
 failure has already run every other test.
@@ -14,6 +14,9 @@ failure has already run every other test.
 from __future__ import annotations
 
 import ctypes
+import hashlib
+import json
+import os
 import struct
 
 import numpy as np
@@ -96,33 +99,56 @@ def run_noalloc(hvm, book: np.ndarray, cap: int = 1 << 16):
     return rc, ports[:n.value], kids[:n.value], itrs.value, err.value.decode()
 
 
-def programs(ref_programs, workloads):
+def programs(ref_programs, workloads, config_goldens):
+    """(name, code, golden) with the reference C runtime's result and count:
+    `golden` holds `result` (text) or `canonical_sha256`, and `itrs`."""
     # The fixed array is meant for small nets; the large examples (millions
     # of interactions) run through the normal entry point only.
     large = ("sum_tree", "sort_radix", "stress", "sum_rec", "sort_bitonic")
-    progs = [(p["name"], p["code"]) for p in ref_programs
+    progs = [(p["name"], p["code"], p) for p in ref_programs
              if "result" in p and not any(x in p["name"] for x in large)]
-    progs += [("tree_sum_d12", workloads.tree_sum(12)), ("bitonic_sort_2p8", workloads.bitonic_sort(8)),
-              ("skewed_fold_2p8", workloads.skewed_fold(8)), ("countdown_1000", workloads.countdown(1000))]
+    progs += [("tree_sum_d12", workloads.tree_sum(12), config_goldens["tree_sum_d12"]),
+              ("bitonic_sort_2p8", workloads.bitonic_sort(8), config_goldens["bitonic_sort_2p8"]),
+              ("skewed_fold_2p10", workloads.skewed_fold(10), config_goldens["skewed_fold_2p10"])]
     return progs
 
 
-def test_noalloc_matches_normal_entry_point_twice(hvm, ref_programs, workloads):
-    # The existing entry point gives the expected normal form and count.
+def matches_golden(hvm, canon: str, golden: dict) -> bool:
+    if "result" in golden:
+        return canon == hvm.canonical(golden["result"])
+    return hashlib.sha256(canon.encode()).hexdigest() == golden["canonical_sha256"]
+
+
+def test_noalloc_matches_goldens_and_normal_entry_point_twice(hvm, ref_programs, workloads, config_goldens):
+    progs = programs(ref_programs, workloads, config_goldens)
+    # The existing entry point on the same books.
     expected = {}
     with hvm.Runtime(device=0) as rt:
-        for name, code in programs(ref_programs, workloads):
+        for name, code, _ in progs:
             rt.load(code)
             st = rt.run()
             expected[name] = (hvm.canonical(rt.result()), st.itrs)
-    for name, code in programs(ref_programs, workloads):
+    for name, code, golden in progs:
         book = hvm.book_from_text(code)
         names = def_names(book)
         for call in range(2):
             rc, ports, kids, itrs, err = run_noalloc(hvm, book)
             assert rc == 0, (name, call, err)
-            assert itrs == expected[name][1], (name, call)
-            assert hvm.canonical(render(ports, kids, names)) == expected[name][0], (name, call)
+            canon = hvm.canonical(render(ports, kids, names))
+            assert itrs == golden["itrs"], (name, call)
+            assert matches_golden(hvm, canon, golden), (name, call)
+            assert (canon, itrs) == expected[name], (name, call)
+
+
+def test_noalloc_refuses_io_calls(hvm):
+    # A program whose normal form asks for an IO call (it opens a file):
+    # this entry point has no IO layer, so it answers an error.
+    io = json.load(open(os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "io_programs.json")))
+    code = next(p["code"] for p in io["programs"] if p["name"].endswith("open3.hvm"))
+    for _ in range(2):
+        rc, _, _, _, err = run_noalloc(hvm, hvm.book_from_text(code))
+        assert rc != 0
+        assert "IO calls are not supported" in err
 
 
 def test_noalloc_rejects_books_beyond_its_limits(hvm):
