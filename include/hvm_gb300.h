@@ -99,6 +99,15 @@ typedef struct {
                                  others the `reg_cap_blocks` one; the host switches between its polls */
   uint32_t narrow_reg_cap;    /* 0 (default: no register cap, no spills), or 5/6/8: the register cap of
                                  that narrow variant */
+  uint32_t rule_select;       /* 0 = every lane with a redex interacts each round; 1 (default) = a warp
+                                 runs one rule class per round (no allocation: LINK/VOID/ERAS/ANNI; CALL;
+                                 COMM; OPER/SWIT), the class of most lanes' next redex, a lane that has
+                                 waited 4 rounds going first; 2 = one rule per round */
+  uint32_t fast_calls;        /* CALL-time fast paths of the reference's compiled C mode (src/cmp.rs:
+                                 110-290), same interaction counts: 0 = off (default); 1 = a def whose
+                                 root is `(?((s1 s2) r) r)` called with `(#X R)` switches on the spot;
+                                 2 = also, a def whose root is a CON called with a CON annihilates it
+                                 on the spot */
 } hvm_gb300_config;
 
 typedef struct {

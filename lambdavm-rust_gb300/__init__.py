@@ -51,6 +51,8 @@ class Config(ctypes.Structure):
         ("turn_budget_cap", ctypes.c_uint32),
         ("narrow_below", ctypes.c_uint32),
         ("narrow_reg_cap", ctypes.c_uint32),
+        ("rule_select", ctypes.c_uint32),
+        ("fast_calls", ctypes.c_uint32),
     ]
 
 

@@ -42,8 +42,19 @@ struct DefHdr {
   uint32_t joined;  // 1: the rbag holds every link of a call, the root's included
                     // (its caller end written as CALLER_PORT), with vars that
                     // only wired two links removed; 0: the book's own layout
-  uint32_t pad;
+  uint32_t fast;    // CALL-time fast paths (src/cmp.rs:110-290), see fast_kind()
 };
+
+// DefHdr::fast, for joined defs whose root is a CON node (the root link is
+// then the last link) of at most 32 nodes and vars. Bits 0-1: 0 none,
+// FAST_ANNI (the root CON meets a CON caller), FAST_SWITCH (the root is
+// `(?((s1 s2) r) r)`: a switch whose result is the call's result, fed by a
+// caller `(#X R)`); bits 2-6 the root node, 7-11 the switch node, 12-16 its
+// CON node, 17-21 the var r. The def's table then holds two more pairs after
+// its nodes: the root's two ports, and (s1, s2).
+constexpr uint32_t FAST_ANNI = 1, FAST_SWITCH = 2;
+__host__ __device__ __forceinline__ uint32_t fast_kind(uint32_t f) { return f & 3u; }
+__host__ __device__ __forceinline__ uint32_t fast_field(uint32_t f, int k) { return (f >> (2 + 5 * k)) & 31u; }
 
 // Stands for the other side of a CALL's redex in a joined def's link list
 // (a REF to a fid no book can have).
@@ -144,6 +155,8 @@ struct Dev {
   uint32_t nthreads;
   uint32_t ndefs;
   uint32_t steal_min;         // a lane gives a redex to an empty lane of its warp once it holds this many
+  uint32_t rule_select;       // 0: every lane runs its redex each round; 1/2: one rule class / rule per round
+  uint32_t fast_calls;        // CALL-time fast paths: 0 off, 1 SWITCH pattern, 2 SWITCH and ANNI
   const DefHdr* defs;
   const Pair* book;
   Ctl* ctl;
@@ -193,7 +206,22 @@ struct TState {
   bool dirty;                 // wrote fresh words not yet ordered by a fence
   unsigned long long hist[8];
   bool dead;                  // set after a fatal status: stop interacting
+  uint32_t waited;            // rounds this lane's next redex has waited for its rule class
 };
+
+// Rule classes for per-round selection: mode 1 groups the rules by the code
+// they run -- no allocation (LINK, VOID, ERAS, ANNI), CALL, COMM, one or two
+// fresh nodes (OPER, SWIT); mode 2 uses the rule itself. Only a scheduling
+// choice: plan_redex still decides what the interaction is.
+constexpr uint32_t RULE_WAIT_MAX = 4;  // rounds a lane may wait before its class goes first
+__device__ __forceinline__ uint32_t rule_class(uint32_t mode, Pair r) {
+  const Rule rule = get_rule(get_fst(r), get_snd(r));
+  if (mode == 2) return rule;
+  if (rule == CALL) return 1;
+  if (rule == COMM) return 2;
+  if (rule == OPER || rule == SWIT) return 3;
+  return 0;
+}
 
 // Local redex deque: the thread pops and pushes at the top (LIFO, depth
 // first, like the reference's per-thread bags); when it is full, the oldest
@@ -465,6 +493,9 @@ struct Plan {
   Numb cv;              // OPER: the result when both sides are numbers
   bool oper_num;        // OPER: B1 is a number
   bool counted;         // counts as an interaction (every rule but LINK)
+  uint32_t fpad;        // CALL: the def's fast-path word (0 unless the caller is a CON)
+  uint32_t fast;        // CALL: 0, or the fast path taken: 1 ANNI, 2 SWITCH on 0, 3 SWITCH on X > 0
+  Port f1, f2;          // CALL fast path: the def-side ports of its two links
 #ifdef HVM_COMPILED_CALLS
   uint32_t fid;         // CALL: the def
 #endif
@@ -521,6 +552,17 @@ __device__ __forceinline__ void link_pair(const Dev& d, uint32_t gid, const Plan
       break;
     case SWIT: x = new_port(CON, p.n0); y = get_fst(p.B); break;
     default: {  // CALL
+      if (p.fast && i + 1 >= p.rbag_len) {
+        // The root link (the last one) becomes the fast path's two links
+        // (src/cmp.rs:120-245): ANNI root ~ (B1 B2): r1 ~ B1, r2 ~ B2;
+        // SWITCH on 0: s1 ~ R, s2 ~ *; on X > 0: s1 ~ *, s2 ~ b = (#(X-1) R).
+        const bool second = i + 1 > p.rbag_len;
+        x = relocate(d, gid, p, second ? p.f2 : p.f1);
+        if (p.fast == 1) y = second ? get_snd(p.B) : get_fst(p.B);
+        else if (p.fast == 2) y = second ? new_port(ERA, 0) : get_snd(p.B);
+        else y = second ? new_port(CON, get_val(p.b)) : new_port(ERA, 0);
+        break;
+      }
 #ifdef HVM_COMPILED_CALLS
       if (d.compiled && p.contig && compiled_call_link(p.fid, i, p.nbase, p.vbase, p.b, x, y)) break;
 #endif
@@ -547,6 +589,8 @@ __device__ __forceinline__ bool plan_redex(const Dev& d, TState& t, Pair r, Plan
   p.a = a; p.b = b;
   p.counted = rule != LINK;
   p.node_len = p.rbag_len = p.vars_len = 0;
+  p.fpad = 0;
+  p.fast = 0;
   if (rule == CALL) {
     uint32_t fid = get_val(a) & 0xFFFFFFFu;
     if (fid >= d.ndefs) { set_status(d, ST_BAD_REF, fid); t.dead = true; return false; }
@@ -556,8 +600,12 @@ __device__ __forceinline__ bool plan_redex(const Dev& d, TState& t, Pair r, Plan
     } else {
       p.node_len = h.node_len; p.rbag_len = h.rbag_len; p.vars_len = h.vars_len;
       p.off = h.off; p.root = h.root; p.joined = h.joined != 0;
+      // CALL-time fast paths, as configured: 1 the SWITCH pattern only, 2 also ANNI.
+      if (d.fast_calls && get_tag(b) == CON && (d.fast_calls >= 2 || fast_kind(h.fast) == FAST_SWITCH))
+        p.fpad = h.fast;
 #ifdef HVM_COMPILED_CALLS
       p.fid = fid;
+      if (d.compiled) p.fpad = 0;  // compiled calls write every node of the def
 #endif
     }
   }
@@ -626,10 +674,21 @@ __device__ __forceinline__ int lockstep_round(const Dev& d, TState& t, bool has,
   // 2. load the principal nodes
   const bool needA = rule == ANNI || rule == COMM;
   const bool needB = rule == ERAS || rule == ANNI || rule == COMM || rule == OPER || rule == SWIT;
+  const bool peekB = rule == CALL && fast_kind(p.fpad);  // a CALL fast path needs the caller's node
   if (needA) p.A = nload(d, get_val(p.a));
-  if (needB) p.B = nload(d, get_val(p.b));
+  if (needB || peekB) p.B = nload(d, get_val(p.b));
   int rc = IR_DONE;
   if ((needA && p.A == 0) || (needB && p.B == 0)) rc = IR_RETRY;  // not yet visible: re-try later
+  if (peekB && p.B != 0) {
+    // Fast SWITCH when the caller's first port is a number, else fast ANNI.
+    const bool sw = fast_kind(p.fpad) == FAST_SWITCH && get_tag(get_fst(p.B)) == NUM;
+    p.fast = sw ? (get_u24(get_val(get_fst(p.B))) == 0 ? 2u : 3u) : d.fast_calls >= 2 ? 1u : 0u;
+    if (p.fast) {
+      const Pair q = __ldg((const unsigned long long*)&d.book[p.off + p.rbag_len + p.node_len + (sw ? 1 : 0)]);
+      p.f1 = get_fst(q);
+      p.f2 = get_snd(q);
+    }
+  }
   long long c1 = 0;
   if (wp) { __syncwarp(); c1 = clock64(); }
 
@@ -719,16 +778,40 @@ __device__ __forceinline__ int lockstep_round(const Dev& d, TState& t, bool has,
           if (rc != IR_DONE) break;
         }
         const Pair* nodes = d.book + p.off + p.rbag_len;
+        // A fast path leaves out the nodes it consumes: the root (ANNI), or
+        // the root, the switch and its CON (SWITCH).
+        const uint32_t skip = !p.fast ? 0u
+                            : p.fast == 1 ? 1u << fast_field(p.fpad, 0)
+                            : (1u << fast_field(p.fpad, 0)) | (1u << fast_field(p.fpad, 1)) | (1u << fast_field(p.fpad, 2));
 #ifdef HVM_COMPILED_CALLS
         if (!(d.compiled && p.contig && compiled_call_nodes(d, p.fid, p.nbase, p.vbase)))
 #endif
         for (uint32_t i = 0; i < p.node_len; i++) {
-          Pair q = __ldg((const unsigned long long*)&nodes[i]);
           uint32_t at = p.contig ? p.nbase + i : d.nloc[(size_t)i * d.nthreads + t.gid];
+          if ((skip >> i) & 1u) {
+            if (!p.contig) nstore(d, at, 0);  // taken (marked) one by one: give it back
+            continue;
+          }
+          Pair q = __ldg((const unsigned long long*)&nodes[i]);
           nstore(d, at, new_pair(relocate(d, t.gid, p, get_fst(q)), relocate(d, t.gid, p, get_snd(q))));
         }
+        t.live_nodes -= __popc(skip);
+        if (p.fast) {
+          // The caller's node: consumed, or reused as (#(X-1) R).
+          if (p.fast == 3) {
+            nstore(d, get_val(p.b), new_pair(new_port(NUM, new_u24(get_u24(get_val(get_fst(p.B))) - 1)), get_snd(p.B)));
+          } else {
+            nstore(d, get_val(p.b), 0);
+            t.live_nodes--;
+          }
+          if (p.fast >= 2) {  // the switch's result var r is consumed with it
+            const uint32_t r = fast_field(p.fpad, 3);
+            vstore(d, p.contig ? p.vbase + r : d.vloc[(size_t)r * d.nthreads + t.gid], 0);
+            t.live_vars--;
+          }
+        }
         made = p.node_len > 0 || p.vars_len > 0;
-        p.nlinks = p.rbag_len + (p.joined ? 0 : 1);
+        p.nlinks = p.rbag_len + (p.joined ? 0 : 1) + (p.fast ? 1 : 0);
         break;
       }
     }
@@ -783,7 +866,15 @@ __device__ __forceinline__ int lockstep_round(const Dev& d, TState& t, bool has,
     wp->v[PROF_CYC_LINK] += c4 - c3;
   }
   if (has && rc == IR_RETRY) { push(d, t, r); t.retries++; }
-  if (has && rc == IR_DONE && p.counted) { t.itrs++; t.hist[rule]++; }
+  if (has && rc == IR_DONE && p.counted) {
+    t.itrs++;
+    t.hist[rule]++;
+    if (p.fast) {  // the interactions a fast path performs in place (src/cmp.rs:147, 191, 220, 253)
+      t.itrs += p.fast == 1 ? 1 : 3;
+      t.hist[ANNI] += p.fast == 1 ? 1 : 2;
+      if (p.fast >= 2) t.hist[SWIT]++;
+    }
+  }
   return rc;
 }
 

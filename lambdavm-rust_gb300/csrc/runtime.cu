@@ -220,6 +220,7 @@ __global__ void __launch_bounds__(128, MIN_BLOCKS_128 > 0 ? MIN_BLOCKS_128 : 1) 
   t.dirty = false;
   for (int i = 0; i < 8; i++) t.hist[i] = 0;
   t.dead = false;
+  t.waited = 0;
 
   // Static share of the input: items base + gid + k*N, k < s.
   for (uint32_t k = 0; k < s; k++) {
@@ -281,7 +282,23 @@ __global__ void __launch_bounds__(128, MIN_BLOCKS_128 > 0 ? MIN_BLOCKS_128 : 1) 
       }
       break;
     }
-    const bool has = t.len > 0;
+    // Rule selection (d.rule_select != 0): the warp runs one class of rules
+    // per round -- the class of the most lanes' next redex, or of a lane that
+    // has waited RULE_WAIT_MAX rounds -- and the other lanes keep their
+    // redex for a later round, so only that class's code path executes.
+    bool go = t.len > 0;
+    if (d.rule_select) {
+      const uint32_t cls = go ? rule_class(d.rule_select, slot(t, t.len - 1)) : 0xFFu;
+      const unsigned same = __match_any_sync(0xFFFFFFFFu, cls);
+      unsigned key = 0;
+      if (go) key = (t.waited >= RULE_WAIT_MAX ? 1u << 12 : 0u) | ((unsigned)__popc(same) << 5) | (31u - lane);
+      key = __reduce_max_sync(0xFFFFFFFFu, key);
+      const uint32_t chosen = __shfl_sync(0xFFFFFFFFu, cls, 31u - (key & 31u));
+      const bool run = go && cls == chosen;
+      t.waited = run || !go ? 0 : t.waited + 1;
+      go = run;
+    }
+    const bool has = go;
     const Pair r = has ? pop(t) : 0;
     lockstep_round(d, t, has, r, prof_on ? &prof : nullptr);
     if (__any_sync(0xFFFFFFFFu, t.dead)) break;
@@ -752,14 +769,39 @@ static void join_links(const HostDef& h, std::vector<Pair>& links, std::vector<P
   vars_len = next;
 }
 
+// The CALL-time fast paths a def allows (DefHdr::fast). The reference's
+// compiled C mode checks, at each call, whether the caller's port already
+// has the shape the def's root would interact with (src/cmp.rs:110-290):
+// a root CON meeting a CON node is annihilated on the spot, and a root
+// `(?((s1 s2) r) r)` meeting `(#X R)` is switched on the spot, adding the
+// interactions it performs (1, and 3) by hand. Only the top-level pattern is
+// taken here; the def's other nodes are created as in any call. Needs the
+// root link last in the joined link list, and fields of 5 bits.
+static uint32_t fast_word(const HostDef& h, const std::vector<Pair>& links, const std::vector<Pair>& nodes,
+                          uint32_t vars_len) {
+  if (get_tag(h.root) != CON || h.node_len > 32 || vars_len > 32 || links.empty()) return 0;
+  if (links.back() != new_pair(h.root, CALLER_PORT)) return 0;
+  const uint32_t ri = get_val(h.root);
+  const Port a1 = get_fst(nodes[ri]), a2 = get_snd(nodes[ri]);
+  uint32_t w = FAST_ANNI | ri << 2;
+  if (get_tag(a1) == SWI && get_tag(a2) == VAR) {
+    const Pair sw = nodes[get_val(a1)];
+    const Port a11 = get_fst(sw), a12 = get_snd(sw);
+    if (get_tag(a11) == CON && a12 == a2)
+      w = FAST_SWITCH | ri << 2 | get_val(a1) << 7 | get_val(a11) << 12 | get_val(a2) << 17;
+  }
+  return w;
+}
+
 // The device's def tables for a book: per def a header, then its links (the
-// redexes and the root link, joined) and its nodes, all defs in one array.
+// redexes and the root link, joined) and its nodes (and, for a def with a
+// fast path, its two pairs of fast-path ports), all defs in one array.
 static void def_tables(const std::vector<HostDef>& defs, std::vector<DefHdr>& hdr, std::vector<Pair>& flat,
                        uint32_t& max_nodes, uint32_t& max_vars) {
   hdr.assign(defs.size(), DefHdr{});
   flat.clear();
   size_t words = 1;
-  for (const HostDef& h : defs) words += h.rbag.size() + 1 + h.node.size();
+  for (const HostDef& h : defs) words += h.rbag.size() + 3 + h.node.size();
   flat.reserve(words);
   max_nodes = 1;
   max_vars = 1;
@@ -769,9 +811,16 @@ static void def_tables(const std::vector<HostDef>& defs, std::vector<DefHdr>& hd
     const HostDef& h = defs[f];
     uint32_t vars_len = 0;
     join_links(h, links, nodes, vars_len, sc);
-    hdr[f] = DefHdr{h.node_len, (uint32_t)links.size(), vars_len, h.safe ? 1u : 0u, 0, (uint32_t)flat.size(), 1, 0};
+    const uint32_t fast = fast_word(h, links, nodes, vars_len);
+    hdr[f] = DefHdr{h.node_len, (uint32_t)links.size(), vars_len, h.safe ? 1u : 0u, 0, (uint32_t)flat.size(), 1, fast};
     flat.insert(flat.end(), links.begin(), links.end());
     flat.insert(flat.end(), nodes.begin(), nodes.end());
+    if (fast_kind(fast)) {
+      // The fast paths' def-side ports: the root's two, then the switch's CON's two.
+      const Pair root = nodes[fast_field(fast, 0)];
+      flat.push_back(root);
+      flat.push_back(fast_kind(fast) == FAST_SWITCH ? nodes[fast_field(fast, 2)] : root);
+    }
     if (h.node_len > max_nodes) max_nodes = h.node_len;
     if (vars_len > max_vars) max_vars = vars_len;
   }
@@ -979,6 +1028,10 @@ class Runtime {
   int sms = 0;
   // Host injection region per space (0 = nodes, 1 = vars): [lo, hi) words, next candidate.
   uint32_t host_lo[2] = {0, 0}, host_hi[2] = {0, 0}, host_next[2] = {0, 0};
+  // Pools' high-water marks (pages handed out) since the last clear, and
+  // whether they were read after the last turn ran (else clear everything).
+  uint64_t used_node_pages = 0, used_var_pages = 0;
+  bool marks_valid = false;
   uint32_t* list_buf = nullptr;          // device list readback: LIST_READ_MAX values + info
   uint32_t max_pages = MAX_PAGES;        // page-list capacity per thread and space
   // Scheduler policy written into the control block at every reset.
@@ -1066,6 +1119,10 @@ class Runtime {
     d.nthreads = nthreads;
     if (cfg.steal_min == 1 || cfg.steal_min > cap) return fail("steal_min must be 0 or in [2, stack_cap]");
     d.steal_min = cfg.steal_min ? cfg.steal_min : 2;
+    if (cfg.rule_select > 2) return fail("rule_select must be 0, 1 or 2");
+    d.rule_select = cfg.rule_select;
+    if (cfg.fast_calls > 2) return fail("fast_calls must be 0, 1 or 2");
+    d.fast_calls = cfg.fast_calls;
     // Pages: a power of two of words, at most 512 node / 1024 var words, and
     // small enough that every thread starts with one page and at least as
     // many pages again remain in the pool.
@@ -1129,10 +1186,34 @@ class Runtime {
   }
 
   // Clears the whole net (node/var words, ring, cursors, counters).
+  // Clears the net for the next evaluation. Device code writes net words
+  // only in pages the allocator handed out -- below the pools' high-water
+  // marks, which every control-block read records -- and in the host region
+  // and ROOT vars above the pools' ends; so after a run whose marks were
+  // read, only those words are cleared, and the whole space otherwise.
+  int clear_net() {
+    const uint64_t n_nodes = 1ull << cfg.node_log2, n_vars = 1ull << cfg.vars_log2;
+    if (!marks_valid) {
+      CK(cudaMemset(mem_node, 0, n_nodes * sizeof(Pair)));
+      CK(cudaMemset(mem_vars, 0, n_vars * sizeof(Port)));
+    } else {
+      const uint64_t nlo = std::min<uint64_t>(used_node_pages, d.npool_end) << d.nspace.page_log2;
+      const uint64_t vlo = std::min<uint64_t>(used_var_pages, d.vpool_end) << d.vspace.page_log2;
+      const uint64_t ntop = (uint64_t)d.npool_end << d.nspace.page_log2;
+      const uint64_t vtop = (uint64_t)d.vpool_end << d.vspace.page_log2;
+      CK(cudaMemset(mem_node, 0, nlo * sizeof(Pair)));
+      CK(cudaMemset(mem_vars, 0, vlo * sizeof(Port)));
+      CK(cudaMemset((Pair*)mem_node + ntop, 0, (n_nodes - ntop) * sizeof(Pair)));
+      CK(cudaMemset((Port*)mem_vars + vtop, 0, (n_vars - vtop) * sizeof(Port)));
+    }
+    marks_valid = false;
+    used_node_pages = used_var_pages = 0;
+    return 0;
+  }
+
   int reset_net() {
     result_valid = false;
-    CK(cudaMemset(mem_node, 0, (1ull << cfg.node_log2) * sizeof(Pair)));
-    CK(cudaMemset(mem_vars, 0, (1ull << cfg.vars_log2) * sizeof(Port)));
+    if (clear_net()) return -1;
     // The top `nroots` var words are ROOT vars: no page that holds one is handed out.
     d.vpool_end = (uint32_t)(((1ull << cfg.vars_log2) - nroots) >> d.vspace.page_log2);
     // The last pages below each pool's end are the host's: IO results are
@@ -1389,6 +1470,9 @@ class Runtime {
   int read_ctl(Ctl& h) {
     CK(cudaMemcpy(&h, ctl, sizeof(Ctl), cudaMemcpyDeviceToHost));
     d2h_bytes += sizeof(Ctl);
+    used_node_pages = std::max(used_node_pages, (uint64_t)h.npool_next);
+    used_var_pages = std::max(used_var_pages, (uint64_t)h.vpool_next);
+    marks_valid = true;
     return 0;
   }
 
@@ -1439,6 +1523,7 @@ class Runtime {
       events.push_back(e);
     }
     if (g && ensure_graph()) return -1;
+    marks_valid = false;  // until the control block is read after these turns
     for (uint32_t i = 0; i < units; i++) {
       CK(cudaEventRecord(events[2 * i]));
       if (g) CK(cudaGraphLaunch(gexec, 0));
@@ -2245,6 +2330,8 @@ extern "C" void hvm_gb300_default_config(hvm_gb300_config* c) {
   c->turn_budget_cap = 1024;
   c->narrow_below = 1024;
   c->narrow_reg_cap = 0;
+  c->rule_select = 1;
+  c->fast_calls = 0;
 }
 
 extern "C" int hvm_gb300_create(const hvm_gb300_config* cfg, hvm_gb300_runtime** out) {

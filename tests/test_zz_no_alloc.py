@@ -109,7 +109,7 @@ def programs(ref_programs, workloads, config_goldens):
              if "result" in p and not any(x in p["name"] for x in large)]
     progs += [("tree_sum_d12", workloads.tree_sum(12), config_goldens["tree_sum_d12"]),
               ("bitonic_sort_2p8", workloads.bitonic_sort(8), config_goldens["bitonic_sort_2p8"]),
-              ("skewed_fold_2p10", workloads.skewed_fold(10), config_goldens["skewed_fold_2p10"])]
+              ("countdown_100000", workloads.countdown(100000), config_goldens["countdown_100000"])]
     return progs
 
 
