@@ -137,7 +137,7 @@ def bench_batch(hvm, W, args, plain_sample: int = 128, policy: str = "fixed", cf
     return out
 
 
-BATCH_TUNE_SPACE = {"rule_select": (0, 1), "policy": ("fixed", "learned")}
+BATCH_TUNE_SPACE = {"fast_calls": (0, 1, 2), "policy": ("fixed", "learned")}
 
 
 def bench_batch_tuned(hvm, W, args, space: dict | None = None) -> dict:
@@ -721,12 +721,18 @@ def profile_case(args) -> None:
     W = importlib.import_module("lambdavm-rust_gb300.workloads")
     make = {"bitonic": W.bitonic_sort, "tree_sum": W.tree_sum, "skewed": W.skewed_fold}[args.profile_case]
     with hvm.Runtime(device=0, node_log2=args.space_log2, vars_log2=args.space_log2, ring_log2=24,
-                     profile=1 if args.prof else 0) as rt:
+                     profile=1 if args.prof else 0, trace_cap=4096 if args.trace else 0) as rt:
         rt.load(make(args.log2n))
         for _ in range(args.runs):
             st = rt.run()
             print(f"itrs {st.itrs} turns {st.turns} ms {st.seconds * 1e3:.3f} kernel_ms {st.kernel_ms:.3f}",
                   flush=True)
+            if args.trace:
+                # Interactions per turn; turn k is the k-th turn-kernel launch of the run.
+                prev = 0
+                for k, r in enumerate(rt.trace()):
+                    print(f"turn {k} itrs {r['itrs'] - prev}", flush=True)
+                    prev = r["itrs"]
             if args.prof:
                 names = ("rounds", "lanes", "link_steps", "cyc_loop", "cyc_load", "cyc_write", "cyc_fence",
                          "cyc_link")
@@ -740,13 +746,15 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["gb300", "reference"], default="gb300")
     ap.add_argument("--workload", choices=sorted(WORKLOADS), default="bitonic_sort_2p16")
-    ap.add_argument("--no-batch", action="store_true", help="skip the 4096-net batch report of the default line")
+    ap.add_argument("--no-batch", action="store_true",
+                    help="skip the 4096-net batch, scheduler and reference-CUDA reports of the default line")
     ap.add_argument("--profile-case", choices=["bitonic", "tree_sum", "skewed"],
                     help="evaluate one small case for a profiler instead of benchmarking (see profile_case)")
     ap.add_argument("--log2n", type=int, default=14, help="--profile-case: keys / depth / elements (log2)")
     ap.add_argument("--space-log2", type=int, default=26, help="--profile-case: node and var space, 2^k words")
     ap.add_argument("--runs", type=int, default=1, help="--profile-case: evaluations")
     ap.add_argument("--prof", action="store_true", help="--profile-case: per-phase cycle counters")
+    ap.add_argument("--trace", action="store_true", help="--profile-case: interactions per turn")
     args = ap.parse_args()
     if args.profile_case:
         profile_case(args)
@@ -791,7 +799,7 @@ def main():
             at = importlib.import_module("lambdavm-rust_gb300.autotune")
             gold = json.load(open(BATCH_GOLDEN))
             sample = [hvm.book_from_text(code) for code, _ in W.mixed_batch(gold["count"])]
-            space = {"reg_cap_blocks": (5, 8), "graph_turns": (0, 4), "policy": ("fixed", "learned")}
+            space = {"reg_cap_blocks": (5, 8), "fast_calls": (0, 1), "graph_turns": (0, 4), "policy": ("fixed", "learned")}
             best, rows = at.tune_batch(sample, BATCH_INFLIGHT, BATCH_LIVE_FRAC, space=space)
             best = dict(best)
             policy = best.pop("policy")
@@ -821,7 +829,7 @@ def main():
             line["batched_tuned"] = bench_batch_tuned(hvm, W, args)
             line["config4"] = config4_report(line["batched"], line["batched_learned"], line["batched_tuned"])
             line["scheduler"] = bench_scheduler(hvm, W)
-        if line is not None:
+        if line is not None and not args.no_batch:
             line["reference_cuda"] = bench_reference_cuda(hvm, W)
     finally:
         dist.close()

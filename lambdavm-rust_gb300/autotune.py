@@ -10,6 +10,9 @@ returns the fastest configuration:
                   128 threads per SM; 5 or 8 = that many blocks per SM)
   stack_cap       redexes per thread in the shared-memory deque
   graph_turns     0 = one launch per turn; k = CUDA-graph replays of k turns
+  rule_select     0 = every lane interacts each round; 1 = one rule class per round
+  fast_calls      CALL-time fast paths: 0 off, 1 SWITCH pattern, 2 SWITCH and ANNI
+                  (compiled in for register caps 0 and 8 only)
   policy          the fixed turn policy or the learned one
 
 Every candidate's interaction count and results are checked against the first
@@ -34,7 +37,7 @@ hvm = importlib.import_module("lambdavm-rust_gb300")
 DEFAULT_SPACE = {
     "reg_cap_blocks": (0, 5, 8),
     "stack_cap": (8, 16),
-    "graph_turns": (0, 4),
+    "fast_calls": (0, 1),
     "policy": ("fixed", "learned"),
 }
 
@@ -42,7 +45,9 @@ DEFAULT_SPACE = {
 def candidates(space: dict | None = None) -> list[dict]:
     space = space or DEFAULT_SPACE
     keys = list(space)
-    return [dict(zip(keys, vals)) for vals in itertools.product(*(space[k] for k in keys))]
+    out = [dict(zip(keys, vals)) for vals in itertools.product(*(space[k] for k in keys))]
+    # The fast-path kernel variants exist for register caps 0 and 8 only.
+    return [c for c in out if not (c.get("fast_calls") and c.get("reg_cap_blocks", 8) not in (0, 8))]
 
 
 def make_runtime(cand: dict, device: int = 0, weights=None, **extra):

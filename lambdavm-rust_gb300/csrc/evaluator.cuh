@@ -286,7 +286,7 @@ __device__ __forceinline__ void ld_cg_v4(const void* p, unsigned long long& a, u
 
 constexpr uint32_t CHUNK = 32;  // words per scanned chunk (256 B of nodes, 128 B of vars)
 constexpr uint32_t MAX_DRY_PAGES = 4;  // full cycles over a lane's pages before out-of-memory
-constexpr uint32_t SOFT_RUN_CHUNKS = 32;  // chunks a CALL scans for a contiguous run before taking single words
+constexpr uint32_t SOFT_RUN_CHUNKS = 64;  // chunks a CALL scans for a contiguous run before taking single words
 constexpr uint32_t SOFT_GRAB_PAGES = 8;   // a contiguous-run request may take pages up to this many owned
 
 // Bit i of the result is set when word base+i is free and may be handed out.
@@ -532,6 +532,7 @@ __device__ __forceinline__ Port relocate(const Dev& d, uint32_t gid, const Plan&
 }
 
 // The i-th port pair of the lane's rule (src/hvm.c:852-1070).
+template <bool FAST>
 __device__ __forceinline__ void link_pair(const Dev& d, uint32_t gid, const Plan& p, uint32_t i, Port& x, Port& y) {
   switch (p.rule) {
     case LINK: x = p.a; y = p.b; break;
@@ -552,7 +553,7 @@ __device__ __forceinline__ void link_pair(const Dev& d, uint32_t gid, const Plan
       break;
     case SWIT: x = new_port(CON, p.n0); y = get_fst(p.B); break;
     default: {  // CALL
-      if (p.fast && i + 1 >= p.rbag_len) {
+      if (FAST && p.fast && i + 1 >= p.rbag_len) {
         // The root link (the last one) becomes the fast path's two links
         // (src/cmp.rs:120-245): ANNI root ~ (B1 B2): r1 ~ B1, r2 ~ B2;
         // SWITCH on 0: s1 ~ R, s2 ~ *; on X > 0: s1 ~ *, s2 ~ b = (#(X-1) R).
@@ -580,6 +581,7 @@ __device__ __forceinline__ void link_pair(const Dev& d, uint32_t gid, const Plan
 }
 
 // Plans lane's interaction on redex r; returns false for an invalid REF.
+template <bool FAST>
 __device__ __forceinline__ bool plan_redex(const Dev& d, TState& t, Pair r, Plan& p) {
   Port a = get_fst(r), b = get_snd(r);
   Rule rule = get_rule(a, b);
@@ -601,7 +603,7 @@ __device__ __forceinline__ bool plan_redex(const Dev& d, TState& t, Pair r, Plan
       p.node_len = h.node_len; p.rbag_len = h.rbag_len; p.vars_len = h.vars_len;
       p.off = h.off; p.root = h.root; p.joined = h.joined != 0;
       // CALL-time fast paths, as configured: 1 the SWITCH pattern only, 2 also ANNI.
-      if (d.fast_calls && get_tag(b) == CON && (d.fast_calls >= 2 || fast_kind(h.fast) == FAST_SWITCH))
+      if (FAST && d.fast_calls && get_tag(b) == CON && (d.fast_calls >= 2 || fast_kind(h.fast) == FAST_SWITCH))
         p.fpad = h.fast;
 #ifdef HVM_COMPILED_CALLS
       p.fid = fid;
@@ -622,9 +624,10 @@ struct Slot {
 
 // Takes the lane's next port pairs into an idle slot, wiring on the spot every
 // pair that needs no exchange (both sides principal: a new redex).
+template <bool FAST>
 __device__ __forceinline__ void slot_fill(const Dev& d, TState& t, const Plan& p, uint32_t& next, Slot& s) {
   while (!s.busy && next < p.nlinks) {
-    link_pair(d, t.gid, p, next++, s.X, s.Y);
+    link_pair<FAST>(d, t.gid, p, next++, s.X, s.Y);
     if (get_tag(s.X) != VAR && get_tag(s.Y) == VAR) { Port z = s.X; s.X = s.Y; s.Y = z; }
     if (get_tag(s.X) != VAR) push(d, t, new_pair(s.X, s.Y));
     else { s.busy = true; s.entered = false; }
@@ -662,19 +665,20 @@ __device__ __forceinline__ void slot_result(const Dev& d, TState& t, Slot& s, ui
 
 // Runs one round for the warp: every lane with `has` interacts on `r`.
 // Returns the lane's outcome (IR_DONE / IR_RETRY / IR_FATAL).
+template <bool FAST>
 __device__ __forceinline__ int lockstep_round(const Dev& d, TState& t, bool has, Pair r, WarpProf* wp) {
   long long c0 = wp ? clock64() : 0;
   Plan p;
   p.rule = IDLE_RULE;
   p.nlinks = 0;
   p.A = p.B = 0;
-  if (has && !plan_redex(d, t, r, p)) has = false;
+  if (has && !plan_redex<FAST>(d, t, r, p)) has = false;
   const uint32_t rule = p.rule;
 
   // 2. load the principal nodes
   const bool needA = rule == ANNI || rule == COMM;
   const bool needB = rule == ERAS || rule == ANNI || rule == COMM || rule == OPER || rule == SWIT;
-  const bool peekB = rule == CALL && fast_kind(p.fpad);  // a CALL fast path needs the caller's node
+  const bool peekB = FAST && rule == CALL && fast_kind(p.fpad);  // a CALL fast path needs the caller's node
   if (needA) p.A = nload(d, get_val(p.a));
   if (needB || peekB) p.B = nload(d, get_val(p.b));
   int rc = IR_DONE;
@@ -780,7 +784,7 @@ __device__ __forceinline__ int lockstep_round(const Dev& d, TState& t, bool has,
         const Pair* nodes = d.book + p.off + p.rbag_len;
         // A fast path leaves out the nodes it consumes: the root (ANNI), or
         // the root, the switch and its CON (SWITCH).
-        const uint32_t skip = !p.fast ? 0u
+        const uint32_t skip = !FAST || !p.fast ? 0u
                             : p.fast == 1 ? 1u << fast_field(p.fpad, 0)
                             : (1u << fast_field(p.fpad, 0)) | (1u << fast_field(p.fpad, 1)) | (1u << fast_field(p.fpad, 2));
 #ifdef HVM_COMPILED_CALLS
@@ -796,7 +800,7 @@ __device__ __forceinline__ int lockstep_round(const Dev& d, TState& t, bool has,
           nstore(d, at, new_pair(relocate(d, t.gid, p, get_fst(q)), relocate(d, t.gid, p, get_snd(q))));
         }
         t.live_nodes -= __popc(skip);
-        if (p.fast) {
+        if (FAST && p.fast) {
           // The caller's node: consumed, or reused as (#(X-1) R).
           if (p.fast == 3) {
             nstore(d, get_val(p.b), new_pair(new_port(NUM, new_u24(get_u24(get_val(get_fst(p.B))) - 1)), get_snd(p.B)));
@@ -811,7 +815,7 @@ __device__ __forceinline__ int lockstep_round(const Dev& d, TState& t, bool has,
           }
         }
         made = p.node_len > 0 || p.vars_len > 0;
-        p.nlinks = p.rbag_len + (p.joined ? 0 : 1) + (p.fast ? 1 : 0);
+        p.nlinks = p.rbag_len + (p.joined ? 0 : 1) + (FAST && p.fast ? 1 : 0);
         break;
       }
     }
@@ -839,8 +843,8 @@ __device__ __forceinline__ int lockstep_round(const Dev& d, TState& t, bool has,
   Slot s0, s1;
   s0.busy = s1.busy = false;
   for (uint32_t guard = 0; guard < (1u << 24); guard++) {
-    slot_fill(d, t, p, next, s0);
-    slot_fill(d, t, p, next, s1);
+    slot_fill<FAST>(d, t, p, next, s0);
+    slot_fill<FAST>(d, t, p, next, s1);
     if (!__any_sync(0xFFFFFFFFu, s0.busy || s1.busy)) break;
     if (fence_due) { __threadfence(); fence_due = false; t.dirty = false; }
     steps++;
@@ -869,7 +873,7 @@ __device__ __forceinline__ int lockstep_round(const Dev& d, TState& t, bool has,
   if (has && rc == IR_DONE && p.counted) {
     t.itrs++;
     t.hist[rule]++;
-    if (p.fast) {  // the interactions a fast path performs in place (src/cmp.rs:147, 191, 220, 253)
+    if (FAST && p.fast) {  // the interactions a fast path performs in place (src/cmp.rs:147, 191, 220, 253)
       t.itrs += p.fast == 1 ? 1 : 3;
       t.hist[ANNI] += p.fast == 1 ? 1 : 2;
       if (p.fast >= 2) t.hist[SWIT]++;

@@ -183,7 +183,9 @@ __device__ void apply_policy(Ctl* c, const float* o, unsigned long long pending,
 
 // MIN_BLOCKS_128 > 0 asks the compiler to fit that many 128-thread blocks per
 // SM (a register cap); the runtime picks the variant from the configuration.
-template <int MIN_BLOCKS_128>
+// FAST compiles in the CALL-time fast paths (Dev::fast_calls); kept out of
+// the default variants because their code alone costs the others registers.
+template <int MIN_BLOCKS_128, bool FAST>
 __global__ void __launch_bounds__(128, MIN_BLOCKS_128 > 0 ? MIN_BLOCKS_128 : 1) turn_kernel(Dev d, uint32_t cap) {
   extern __shared__ unsigned long long smem_stack[];
   Ctl* c = d.ctl;
@@ -300,7 +302,7 @@ __global__ void __launch_bounds__(128, MIN_BLOCKS_128 > 0 ? MIN_BLOCKS_128 : 1) 
     }
     const bool has = go;
     const Pair r = has ? pop(t) : 0;
-    lockstep_round(d, t, has, r, prof_on ? &prof : nullptr);
+    lockstep_round<FAST>(d, t, has, r, prof_on ? &prof : nullptr);
     if (__any_sync(0xFFFFFFFFu, t.dead)) break;
     // The stop flag is tested one round after it was loaded, so its L2
     // latency hides behind a whole round (a short round would otherwise wait
@@ -1090,11 +1092,14 @@ class Runtime {
     // The turn kernel variant (register cap) and its grid; with `narrow_below`,
     // a second variant runs the turns that start with fewer pending redexes.
     auto make_variant = [&](uint32_t reg_cap, Variant& v) -> int {
+      // The fast-path variants exist for the caps the defaults use.
+      const bool fast = cfg.fast_calls != 0;
+      if (fast && reg_cap != 0 && reg_cap != 8) return fail("fast_calls needs reg_cap_blocks / narrow_reg_cap 0 or 8");
       switch (reg_cap) {
-        case 0: v.fn = turn_kernel<0>; break;
-        case 5: v.fn = turn_kernel<5>; break;
-        case 6: v.fn = turn_kernel<6>; break;
-        case 8: v.fn = turn_kernel<8>; break;
+        case 0: v.fn = fast ? turn_kernel<0, true> : turn_kernel<0, false>; break;
+        case 5: v.fn = turn_kernel<5, false>; break;
+        case 6: v.fn = turn_kernel<6, false>; break;
+        case 8: v.fn = fast ? turn_kernel<8, true> : turn_kernel<8, false>; break;
         default: return fail("reg_cap_blocks / narrow_reg_cap must be 0, 5, 6 or 8");
       }
       CK(cudaFuncSetAttribute(v.fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
@@ -2642,7 +2647,7 @@ static int normalize(Ctx& x) {
   unsigned long long last_itrs = ~0ull, last_pending = ~0ull;
   uint64_t stalled = 0, turns = 0;
   for (;;) {
-    for (uint32_t i = 0; i < batch; i++) turn_kernel<8><<<BLOCKS, THREADS, (size_t)THREADS * CAP * sizeof(Pair)>>>(x.d, CAP);
+    for (uint32_t i = 0; i < batch; i++) turn_kernel<8, false><<<BLOCKS, THREADS, (size_t)THREADS * CAP * sizeof(Pair)>>>(x.d, CAP);
     if (cuda_ok(x, cudaGetLastError()) || read_ctl(x, h)) return -1;
     turns += batch;
     if (h.status) return failf(x, status_text(h.status), h.err_info);

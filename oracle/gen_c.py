@@ -43,7 +43,8 @@ import sys
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 ROOT = os.path.dirname(HERE)
-REF_SRC = os.environ.get("REF_SRC", "/root/reference/src")
+# The reference sources as staged by `make -C oracle stage` (or $REF_SRC).
+REF_SRC = os.environ.get("REF_SRC", os.path.join(HERE, "_ref", "src"))
 OUT_DIR = os.path.join(HERE, "_ref", "genc")
 
 VAR, REF, ERA, NUM, CON, DUP, OPR, SWI = range(8)

@@ -163,3 +163,15 @@ def test_python_restatement_matches_library(hvm, ref_programs, workloads):
         assert a.shape == b.shape and (a == b).all()
     with pytest.raises(pybook.ParseError):
         pybook.book_from_text("")
+
+
+def test_workloads_never_divide(workloads):
+    """u24/i24 division and remainder by zero are undefined in the reference
+    (SIGFPE on x86) and yield 0 here. The benchmark workloads contain no
+    division or remainder operator at all, so they never reach that case."""
+    import re
+    texts = [workloads.tree_sum(8), workloads.bitonic_sort(6), workloads.skewed_fold(6),
+             workloads.countdown(10), workloads.bitonic_sum(6, 7)]
+    texts += [code for code, _ in workloads.mixed_batch(64)]
+    for code in texts:
+        assert not re.search(r"\[:?[/%]", code)

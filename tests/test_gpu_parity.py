@@ -80,6 +80,30 @@ def test_kernel_variant_switching(hvm, workloads, config_goldens, cfg):
             assert hashlib.sha256(hvm.canonical(res).encode()).hexdigest() == g["canonical_sha256"], name
 
 
+@pytest.mark.parametrize("cfg", [dict(fast_calls=1), dict(fast_calls=2), dict(fast_calls=2, rule_select=0),
+                                 dict(fast_calls=1, reg_cap_blocks=0), dict(rule_select=2)],
+                         ids=["fast_switch", "fast_switch_anni", "fast_all_lanes", "fast_uncapped", "rule_per_round"])
+def test_scheduling_options(hvm, workloads, config_goldens, ref_programs, cfg):
+    # CALL-time fast paths (the reference's compiled-mode short-cuts, adding
+    # by hand the interactions they perform) and the per-round rule
+    # selection change how the net is reduced, never the normal form or the
+    # interaction count.
+    cases = {"tree_sum_d12": workloads.tree_sum(12), "bitonic_sort_2p12": workloads.bitonic_sort(12),
+             "skewed_fold_2p10": workloads.skewed_fold(10), "countdown_100000": workloads.countdown(100000)}
+    with hvm.Runtime(device=0, **cfg) as r:
+        for name, code in cases.items():
+            res, st = run(r, code)
+            g = config_goldens[name]
+            assert st.itrs == g["itrs"], name
+            assert hashlib.sha256(hvm.canonical(res).encode()).hexdigest() == g["canonical_sha256"], name
+        for prog in ref_programs:
+            if "result" not in prog:
+                continue
+            res, st = run(r, prog["code"])
+            assert st.itrs == prog["itrs"], prog["name"]
+            assert hvm.canonical(res) == hvm.canonical(prog["result"]), prog["name"]
+
+
 def test_repeat_runs_identical(hvm, rt, workloads):
     code = workloads.bitonic_sort(10)
     outs = {run(rt, code)[0] for _ in range(3)}

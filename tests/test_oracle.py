@@ -83,11 +83,12 @@ def test_oracle_matches_reference_runtime_live(hvm, oracle, workloads, make):
         assert hvm.canonical(got["result"]) == hvm.canonical(want["result"]), threads
 
 
-REF_SRC = os.environ.get("REF_SRC", "/root/reference/src")
+# The reference sources as staged by `make -C oracle stage` (or $REF_SRC).
+REF_SRC = os.environ.get("REF_SRC", os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))), "oracle", "_ref", "src"))
 
 
 @pytest.mark.skipif(not os.path.exists(os.path.join(REF_SRC, "hvm.c")),
-                    reason="the reference's C sources exist only where the reference is checked out")
+                    reason="the reference's C sources were not staged (make -C oracle stage)")
 def test_gen_c_compiled_mode_matches_run_c(hvm, workloads, ref_programs, config_goldens):
     # The reference's compiled C mode (`hvm gen-c`: per-def C functions with
     # the SWITCH / OPER / COPY / ANNI / VOID fast paths, restated by
