@@ -84,7 +84,9 @@ typedef struct {
   uint32_t stop_frac_q8;      /* a turn ends once busy threads < (1 - f/256) x initially busy */
   uint32_t trace_cap;         /* record up to this many turns (0 = off), see hvm_gb300_trace */
   uint32_t reg_cap_blocks;    /* 0, or 5/6/8: cap registers so that many 128-thread blocks fit per SM */
-  uint32_t profile;           /* 1 = collect per-warp round counters into hvm_gb300_stats.prof */
+  uint32_t profile;           /* 1 = collect per-warp round counters into hvm_gb300_stats.prof (a
+                                 separately compiled kernel variant: register caps 0 and 8, no
+                                 fast_calls) */
   uint32_t graph_turns;       /* 0 = one launch per turn; k > 0 = turns run as replays of a CUDA
                                  graph of k launches (captured once per loaded book/batch) */
   uint32_t node_page_log2;    /* allocator page of 2^k node words (0 = 9; 5..12) */

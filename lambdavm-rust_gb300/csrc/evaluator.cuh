@@ -201,10 +201,10 @@ struct TState {
   uint32_t gid;
   Alloc na, va;               // node / var allocators
   unsigned long long base;    // ring index of this turn's first input (overflow check)
-  unsigned long long itrs, leak, retries;
+  uint32_t itrs, leak, retries;  // this turn's counts: budget-bounded, so 32 bits suffice
   int live_nodes, live_vars;  // words taken minus words freed in this turn
   bool dirty;                 // wrote fresh words not yet ordered by a fence
-  unsigned long long hist[8];
+  uint32_t hist[8];
   bool dead;                  // set after a fatal status: stop interacting
   uint32_t waited;            // rounds this lane's next redex has waited for its rule class
 };
@@ -484,7 +484,8 @@ struct Plan {
   Pair A, B;            // principal nodes of a and b (when the rule takes them)
   uint32_t rule;        // LINK..SWIT; IDLE_RULE for a lane without a redex
   uint32_t nlinks;      // port pairs to wire
-  uint32_t n0, n1, n2, n3, v0, v1, v2, v3;  // fresh words of COMM/OPER/SWIT
+  // COMM/OPER/SWIT take their fresh nodes (and COMM its vars) as one run each,
+  // at nbase + k and vbase + k.
   uint32_t node_len, rbag_len, vars_len, off;  // CALL: the def
   uint32_t nbase, vbase;  // CALL: first fresh node / var (contiguous runs), or
   bool contig;            //       per-word scratch tables when the def is large
@@ -542,16 +543,15 @@ __device__ __forceinline__ void link_pair(const Dev& d, uint32_t gid, const Plan
       y = i == 0 ? get_fst(p.B) : get_snd(p.B);
       break;
     case COMM: {
-      uint32_t n = i == 0 ? p.n0 : i == 1 ? p.n1 : i == 2 ? p.n2 : p.n3;
-      x = new_port(i < 2 ? get_tag(p.b) : get_tag(p.a), n);
+      x = new_port(i < 2 ? get_tag(p.b) : get_tag(p.a), p.nbase + i);
       y = i == 0 ? get_fst(p.A) : i == 1 ? get_snd(p.A) : i == 2 ? get_fst(p.B) : get_snd(p.B);
       break;
     }
     case OPER:
       if (p.oper_num) { x = new_port(NUM, p.cv); y = get_snd(p.B); }
-      else { x = get_fst(p.B); y = new_port(OPR, p.n0); }
+      else { x = get_fst(p.B); y = new_port(OPR, p.nbase); }
       break;
-    case SWIT: x = new_port(CON, p.n0); y = get_fst(p.B); break;
+    case SWIT: x = new_port(CON, p.nbase); y = get_fst(p.B); break;
     default: {  // CALL
       if (FAST && p.fast && i + 1 >= p.rbag_len) {
         // The root link (the last one) becomes the fast path's two links
@@ -707,13 +707,15 @@ __device__ __forceinline__ int lockstep_round(const Dev& d, TState& t, bool has,
       case VOID: p.nlinks = 0; break;
       case ERAS: case ANNI: p.nlinks = 2; break;
       case COMM: {
-        p.n0 = alloc_node(d, t); p.n1 = alloc_node(d, t); p.n2 = alloc_node(d, t); p.n3 = alloc_node(d, t);
-        p.v0 = alloc_var(d, t); p.v1 = alloc_var(d, t); p.v2 = alloc_var(d, t); p.v3 = alloc_var(d, t);
-        if (!(p.n0 && p.n1 && p.n2 && p.n3 && p.v0 && p.v1 && p.v2 && p.v3)) { rc = IR_FATAL; break; }
-        nstore(d, p.n0, new_pair(new_port(VAR, p.v0), new_port(VAR, p.v1)));
-        nstore(d, p.n1, new_pair(new_port(VAR, p.v2), new_port(VAR, p.v3)));
-        nstore(d, p.n2, new_pair(new_port(VAR, p.v0), new_port(VAR, p.v2)));
-        nstore(d, p.n3, new_pair(new_port(VAR, p.v1), new_port(VAR, p.v3)));
+        // Vars first (taken as NONE), then the nodes, filled right below (no mark).
+        p.vbase = alloc_run<true>(d, t, t.va, 4);
+        p.nbase = p.vbase ? alloc_run<false, false>(d, t, t.na, 4) : 0;
+        if (!p.vbase || !p.nbase) { rc = IR_FATAL; break; }
+        const uint32_t v = p.vbase;
+        nstore(d, p.nbase + 0, new_pair(new_port(VAR, v + 0), new_port(VAR, v + 1)));
+        nstore(d, p.nbase + 1, new_pair(new_port(VAR, v + 2), new_port(VAR, v + 3)));
+        nstore(d, p.nbase + 2, new_pair(new_port(VAR, v + 0), new_port(VAR, v + 2)));
+        nstore(d, p.nbase + 3, new_pair(new_port(VAR, v + 1), new_port(VAR, v + 3)));
         made = true;
         p.nlinks = 4;
         break;
@@ -724,9 +726,9 @@ __device__ __forceinline__ int lockstep_round(const Dev& d, TState& t, bool has,
         if (p.oper_num) {
           p.cv = operate(get_val(p.a), get_val(b1));
         } else {
-          p.n0 = alloc_node(d, t);
-          if (!p.n0) { rc = IR_FATAL; break; }
-          nstore(d, p.n0, new_pair(p.a, get_snd(p.B)));
+          p.nbase = alloc_run<false, false>(d, t, t.na, 1);
+          if (!p.nbase) { rc = IR_FATAL; break; }
+          nstore(d, p.nbase, new_pair(p.a, get_snd(p.B)));
           made = true;
         }
         p.nlinks = 1;
@@ -734,14 +736,13 @@ __device__ __forceinline__ int lockstep_round(const Dev& d, TState& t, bool has,
       }
       case SWIT: {
         uint32_t n = get_u24(get_val(p.a));
-        p.n0 = alloc_node(d, t);
-        p.n1 = n == 0 ? 1u : alloc_node(d, t);
-        if (!p.n0 || !p.n1) { rc = IR_FATAL; break; }
+        p.nbase = alloc_run<false, false>(d, t, t.na, n == 0 ? 1 : 2);
+        if (!p.nbase) { rc = IR_FATAL; break; }
         if (n == 0) {
-          nstore(d, p.n0, new_pair(get_snd(p.B), new_port(ERA, 0)));
+          nstore(d, p.nbase, new_pair(get_snd(p.B), new_port(ERA, 0)));
         } else {
-          nstore(d, p.n0, new_pair(new_port(ERA, 0), new_port(CON, p.n1)));
-          nstore(d, p.n1, new_pair(new_port(NUM, new_u24(n - 1)), get_snd(p.B)));
+          nstore(d, p.nbase, new_pair(new_port(ERA, 0), new_port(CON, p.nbase + 1)));
+          nstore(d, p.nbase + 1, new_pair(new_port(NUM, new_u24(n - 1)), get_snd(p.B)));
         }
         made = true;
         p.nlinks = 1;

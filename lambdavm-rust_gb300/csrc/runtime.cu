@@ -183,9 +183,10 @@ __device__ void apply_policy(Ctl* c, const float* o, unsigned long long pending,
 
 // MIN_BLOCKS_128 > 0 asks the compiler to fit that many 128-thread blocks per
 // SM (a register cap); the runtime picks the variant from the configuration.
-// FAST compiles in the CALL-time fast paths (Dev::fast_calls); kept out of
-// the default variants because their code alone costs the others registers.
-template <int MIN_BLOCKS_128, bool FAST>
+// FAST compiles in the CALL-time fast paths (Dev::fast_calls) and PROF the
+// per-phase clock counters (Ctl::prof); both are kept out of the default
+// variants because their code alone costs the others registers.
+template <int MIN_BLOCKS_128, bool FAST, bool PROF>
 __global__ void __launch_bounds__(128, MIN_BLOCKS_128 > 0 ? MIN_BLOCKS_128 : 1) turn_kernel(Dev d, uint32_t cap) {
   extern __shared__ unsigned long long smem_stack[];
   Ctl* c = d.ctl;
@@ -235,7 +236,7 @@ __global__ void __launch_bounds__(128, MIN_BLOCKS_128 > 0 ? MIN_BLOCKS_128 : 1) 
   const unsigned lt_mask = (1u << lane) - 1;
   Pair* warp_stk = t.stk - lane;  // lane j's deque starts at warp_stk + j
   WarpProf prof;
-  const bool prof_on = __ldcg(&c->prof_on) != 0;
+  const bool prof_on = PROF && __ldcg(&c->prof_on) != 0;
   for (int i = 0; i < 8; i++) prof.v[i] = 0;
   long long t_loop = clock64();
   // The turn's input is [base, in_end) and `head` only grows: once a claim
@@ -1092,14 +1093,16 @@ class Runtime {
     // The turn kernel variant (register cap) and its grid; with `narrow_below`,
     // a second variant runs the turns that start with fewer pending redexes.
     auto make_variant = [&](uint32_t reg_cap, Variant& v) -> int {
-      // The fast-path variants exist for the caps the defaults use.
-      const bool fast = cfg.fast_calls != 0;
-      if (fast && reg_cap != 0 && reg_cap != 8) return fail("fast_calls needs reg_cap_blocks / narrow_reg_cap 0 or 8");
+      // The fast-path and profiling variants exist for the caps the defaults use.
+      const bool fast = cfg.fast_calls != 0, prof = cfg.profile != 0;
+      if (fast && prof) return fail("profile and fast_calls are not compiled together");
+      if ((fast || prof) && reg_cap != 0 && reg_cap != 8)
+        return fail("fast_calls and profile need reg_cap_blocks / narrow_reg_cap 0 or 8");
       switch (reg_cap) {
-        case 0: v.fn = fast ? turn_kernel<0, true> : turn_kernel<0, false>; break;
-        case 5: v.fn = turn_kernel<5, false>; break;
-        case 6: v.fn = turn_kernel<6, false>; break;
-        case 8: v.fn = fast ? turn_kernel<8, true> : turn_kernel<8, false>; break;
+        case 0: v.fn = fast ? turn_kernel<0, true, false> : prof ? turn_kernel<0, false, true> : turn_kernel<0, false, false>; break;
+        case 5: v.fn = turn_kernel<5, false, false>; break;
+        case 6: v.fn = turn_kernel<6, false, false>; break;
+        case 8: v.fn = fast ? turn_kernel<8, true, false> : prof ? turn_kernel<8, false, true> : turn_kernel<8, false, false>; break;
         default: return fail("reg_cap_blocks / narrow_reg_cap must be 0, 5, 6 or 8");
       }
       CK(cudaFuncSetAttribute(v.fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
@@ -2647,7 +2650,7 @@ static int normalize(Ctx& x) {
   unsigned long long last_itrs = ~0ull, last_pending = ~0ull;
   uint64_t stalled = 0, turns = 0;
   for (;;) {
-    for (uint32_t i = 0; i < batch; i++) turn_kernel<8, false><<<BLOCKS, THREADS, (size_t)THREADS * CAP * sizeof(Pair)>>>(x.d, CAP);
+    for (uint32_t i = 0; i < batch; i++) turn_kernel<8, false, false><<<BLOCKS, THREADS, (size_t)THREADS * CAP * sizeof(Pair)>>>(x.d, CAP);
     if (cuda_ok(x, cudaGetLastError()) || read_ctl(x, h)) return -1;
     turns += batch;
     if (h.status) return failf(x, status_text(h.status), h.err_info);
