@@ -227,13 +227,17 @@ int hvm_gb300_trace(hvm_gb300_runtime* rt, hvm_gb300_turn* out, size_t cap, size
  *      (HVM_GB300_POLICY_PARAMS floats), evaluated on the device by the turn's
  *      last block from the 16 features of hvm_gb300_turn;
  * mode HVM_GB300_POLICY_CONSTANT `constants[0..2]` while fewer redexes than
- *      threads are pending, `constants[3..5]` otherwise.
+ *      threads are pending, `constants[3..5]` otherwise;
+ * mode HVM_GB300_POLICY_SCRIPT  per turn: the decision at the close of turn k
+ *      is `weights[3k .. 3k+2]` (`n_weights` = 3 x turns; later turns keep the
+ *      fixed policy) -- a probe for searching schedules turn by turn.
  * A negative (or non-finite) output keeps the fixed policy's choice. The policy
  * changes only the order of reduction: normal forms and interaction counts are
  * the same under every policy. */
 #define HVM_GB300_POLICY_FIXED 0u
 #define HVM_GB300_POLICY_LEARNED 1u
 #define HVM_GB300_POLICY_CONSTANT 2u
+#define HVM_GB300_POLICY_SCRIPT 3u
 #define HVM_GB300_POLICY_PARAMS 5443
 int hvm_gb300_set_policy(hvm_gb300_runtime* rt, uint32_t mode, const float* weights, size_t n_weights,
                          const float* constants);

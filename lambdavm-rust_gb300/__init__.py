@@ -92,7 +92,7 @@ class _Stats(ctypes.Structure):
 
 
 # Turn scheduler modes and the MLP's shape (include/hvm_gb300.h).
-POLICY_FIXED, POLICY_LEARNED, POLICY_CONSTANT = 0, 1, 2
+POLICY_FIXED, POLICY_LEARNED, POLICY_CONSTANT, POLICY_SCRIPT = 0, 1, 2, 3
 POLICY_IN, POLICY_HID, POLICY_OUT = 16, 64, 3
 POLICY_PARAMS = POLICY_HID * POLICY_IN + POLICY_HID + POLICY_HID * POLICY_HID + POLICY_HID + POLICY_OUT * POLICY_HID + POLICY_OUT
 
@@ -393,7 +393,8 @@ class Runtime:
         with `weights` (POLICY_PARAMS floats), or POLICY_CONSTANT with 6
         `constants` (budget, stop fraction, static share while fewer redexes
         than threads are pending, then the same three otherwise; -1 keeps the
-        fixed policy's choice)."""
+        fixed policy's choice), or POLICY_SCRIPT with `weights` = 3 floats per
+        turn (the decision at the close of turn k; -1 or later turns: fixed)."""
         w = _floats(weights) if weights is not None else None
         c = _floats(constants) if constants is not None else None
         self._check(lib().hvm_gb300_set_policy(self._h, mode, w, len(w) if w is not None else 0, c))

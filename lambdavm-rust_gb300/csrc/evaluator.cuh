@@ -121,6 +121,7 @@ struct alignas(128) Ctl {
   unsigned int vpool_next;          // next page id of the var pool
   TurnRecord* trace;                // per-turn records (null = off)
   unsigned int trace_cap;
+  unsigned int policy_script_len;   // POLICY_SCRIPT: turns the script covers
 };
 
 constexpr Pair NODE_MARK = ~0ull;

@@ -29,7 +29,9 @@ constexpr int POLICY_W3 = POLICY_B2 + POLICY_HID;
 constexpr int POLICY_B3 = POLICY_W3 + POLICY_OUT * POLICY_HID;
 constexpr int POLICY_PARAMS = POLICY_B3 + POLICY_OUT;
 
-enum : uint32_t { POLICY_FIXED = 0, POLICY_LEARNED = 1, POLICY_CONSTANT = 2 };
+// POLICY_SCRIPT: the decision at the close of turn k is script[3k .. 3k+2]
+// (Ctl::policy_w, Ctl::policy_script_len turns; -1 or past the end: fixed).
+enum : uint32_t { POLICY_FIXED = 0, POLICY_LEARNED = 1, POLICY_CONSTANT = 2, POLICY_SCRIPT = 3 };
 
 __device__ __forceinline__ float policy_sigmoid(float x) { return 1.0f / (1.0f + __expf(-x)); }
 

@@ -398,6 +398,10 @@ __global__ void __launch_bounds__(128, MIN_BLOCKS_128 > 0 ? MIN_BLOCKS_128 : 1) 
     if (mode == POLICY_CONSTANT) {
       const int k = pending < d.nthreads ? 0 : 3;
       outp[0] = c->policy_const[k]; outp[1] = c->policy_const[k + 1]; outp[2] = c->policy_const[k + 2];
+    } else if (mode == POLICY_SCRIPT) {
+      const unsigned long long k = c->turns;  // the turn being closed
+      const bool in = c->policy_w && k < c->policy_script_len;
+      for (int o = 0; o < POLICY_OUT; o++) outp[o] = in ? c->policy_w[3 * k + o] : -1.f;
     } else if (mode != POLICY_LEARNED || !c->policy_w) {
       outp[0] = outp[1] = outp[2] = -1.f;
     }
@@ -1041,6 +1045,8 @@ class Runtime {
   uint32_t policy_mode = POLICY_FIXED;
   float policy_const[6] = {-1.f, -1.f, -1.f, -1.f, -1.f, -1.f};
   float* mem_policy = nullptr;
+  float* mem_script = nullptr;          // POLICY_SCRIPT decisions, 3 floats per turn
+  size_t script_cap = 0, script_len = 0;
   double norm_seconds = 0;
   uint64_t norm_calls = 0;
   // Measurement: device time of turn kernels (events around each launch),
@@ -1067,11 +1073,13 @@ class Runtime {
 
   void release() {
     void* ps[] = {mem_node, mem_vars, mem_ring, mem_cur, mem_scratch, mem_defs, mem_book, g_out, g_kids, g_info, ctl,
-                  mem_trace, mem_roots, mem_free, mem_mains, mem_policy, list_buf};
+                  mem_trace, mem_roots, mem_free, mem_mains, mem_policy, mem_script, list_buf};
     for (void* p : ps) if (p) cudaFree(p);
     mem_node = mem_vars = mem_ring = mem_cur = mem_scratch = mem_defs = mem_book = mem_trace = mem_roots = mem_free =
         mem_mains = nullptr;
     mem_policy = nullptr;
+    mem_script = nullptr;
+    script_cap = script_len = 0;
     list_buf = nullptr;
     defs_bytes = book_bytes = scratch_bytes = 0;
     g_out = nullptr; g_kids = nullptr; g_info = nullptr; ctl = nullptr;
@@ -1270,7 +1278,9 @@ class Runtime {
   }
 
   int write_policy() {
-    const float* w = policy_mode == POLICY_LEARNED ? mem_policy : nullptr;
+    const float* w = policy_mode == POLICY_LEARNED ? mem_policy : policy_mode == POLICY_SCRIPT ? mem_script : nullptr;
+    const unsigned sl = policy_mode == POLICY_SCRIPT ? (unsigned)script_len : 0u;
+    CK(cudaMemcpy(&ctl->policy_script_len, &sl, sizeof(sl), cudaMemcpyHostToDevice));
     CK(cudaMemcpy(&ctl->policy_mode, &policy_mode, sizeof(policy_mode), cudaMemcpyHostToDevice));
     CK(cudaMemcpy(&ctl->policy_const, policy_const, sizeof(policy_const), cudaMemcpyHostToDevice));
     CK(cudaMemcpy(&ctl->policy_w, &w, sizeof(w), cudaMemcpyHostToDevice));
@@ -1280,7 +1290,19 @@ class Runtime {
   }
 
   int set_policy(uint32_t mode, const float* weights, size_t n, const float* constants) {
-    if (mode > POLICY_CONSTANT) return fail("unknown policy mode");
+    if (mode > POLICY_SCRIPT) return fail("unknown policy mode");
+    if (mode == POLICY_SCRIPT) {
+      if ((!weights && n) || n % 3 || n / 3 > (1u << 20)) return fail("a policy script is 3 floats per turn");
+      if (n > script_cap) {
+        if (mem_script) cudaFree(mem_script);
+        mem_script = nullptr;
+        script_cap = 0;
+        CK(cudaMalloc((void**)&mem_script, n * sizeof(float)));
+        script_cap = n;
+      }
+      if (n) CK(cudaMemcpy(mem_script, weights, n * sizeof(float), cudaMemcpyHostToDevice));
+      script_len = n / 3;
+    }
     if (mode == POLICY_LEARNED) {
       if (!weights || n != (size_t)POLICY_PARAMS) return fail("learned policy needs HVM_GB300_POLICY_PARAMS weights");
       for (size_t i = 0; i < n; i++)

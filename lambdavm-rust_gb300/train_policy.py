@@ -2,19 +2,20 @@
 
 The reference schedules turns with a fixed SEED/GROW/WORK policy
 (src/hvm.cu:1509-1548); this runtime's fixed policy is its counterpart and the
-learned policy is trained to imitate the fastest schedule found per net:
+learned policy is trained on decisions that measured faster:
 
-1. Every training net (and, with --streams, two continuously batched slices
-   of the 4096-net mixed pool) runs under the fixed policy and under a grid of constant
-   schedules (per regime: while fewer redexes than threads are pending, and
-   otherwise), with per-turn tracing on. Each run records, at the close of every
-   turn, the 16 scheduler features and the next turn's parameters in the
-   policy's output space (budget, stop fraction, static share).
-2. Per net, the run with the lowest device time wins; its (features, next
-   parameters) pairs join the training set, each net weighted equally.
+1. Labels (default, `--labels search`): every training net runs under the
+   fixed policy with per-turn tracing; then, for each turn k, each candidate
+   decision (budget, stop fraction) is applied at the close of turn k alone
+   (POLICY_SCRIPT; the fixed policy decides every other turn from the state it
+   meets) and the run timed. The fastest decision labels turn k's 16 features
+   when it beats the fixed run by 2 %; otherwise the fixed decision does.
+   (`--labels constant`: the best of a grid of constant schedules per net
+   labels all of that net's turns.)
+2. Each net's turns are weighted equally.
 3. The MLP is trained on the GPU (hvm_gb300_policy_train: full-batch Adam, one
    CUDA-graph replay per epoch) and written to a JSON file with the per-net
-   timings of the fixed, best constant and learned schedules.
+   timings of the fixed and learned schedules.
 
 Normal forms and interaction counts are the same under every schedule; each
 run is checked against the fixed policy's.
@@ -142,6 +143,55 @@ def collect(nets, reps: int, trace_cap: int, log=print):
     return np.concatenate(xs), np.concatenate(ts), np.concatenate(ws), report
 
 
+# Candidate decisions for the per-turn search (output space: budget 64 << 10 o0
+# rounds -- 64, 256, 512, 1024, the default turn cap --, stop fraction; the
+# static share keeps the fixed policy's choice).
+SEARCH_ACTIONS = tuple((b, f, -1.0) for b in (0.0, 0.2, 0.3, 0.4) for f in (0.0, 0.5))
+
+
+def search(nets, reps: int, trace_cap: int, max_turns: int = 48, margin: float = 0.02, log=print):
+    """Per-decision labels by local search: for each turn k of a net's run
+    under the fixed policy, every candidate decision is tried at the close of
+    turn k alone (the fixed policy decides every other turn, from the state it
+    then meets), and the fastest run labels turn k's features -- when it beats
+    the fixed run by `margin`, else the fixed policy's own decision is the
+    label. Device time, best of `reps`; every run is checked against the
+    fixed run's normal form and interaction count."""
+    xs, ts, ws, report = [], [], [], []
+    for name, code in nets:
+        if isinstance(code, list):
+            continue  # streams: a run is seconds long, too long to search turn by turn
+        with hvm.Runtime(device=0, trace_cap=trace_cap) as rt:
+            rt.load(code)
+            rt.set_policy(hvm.POLICY_FIXED)
+            fixed_ms, st0 = timed_run(rt, reps)
+            want = _outcome(rt, st0, False)
+            trace = rt.trace()
+            turns = min(len(trace) - 1, max_turns)
+            feats, labels, moved = [], [], 0
+            for k in range(turns):
+                best_ms, best = fixed_ms * (1.0 - margin), None
+                for act in SEARCH_ACTIONS:
+                    rt.set_policy(hvm.POLICY_SCRIPT, weights=[-1.0] * (3 * k) + list(act))
+                    ms, st = timed_run(rt, reps)
+                    if _outcome(rt, st, False) != want:
+                        raise RuntimeError(f"{name}: decision {act} at turn {k} changed the result")
+                    if ms < best_ms:
+                        best_ms, best = ms, act
+                feats.append(trace[k]["features"])
+                out = list(trace[k]["outputs"]) if best is None else [best[0], best[1], trace[k]["outputs"][2]]
+                labels.append(out)
+                moved += best is not None
+            if feats:
+                xs.append(np.array(feats, dtype=np.float32))
+                ts.append(np.clip(np.array(labels, dtype=np.float32), 0.0, 1.0))
+                ws.append(np.full(len(feats), 1.0 / len(feats), dtype=np.float32))
+            report.append({"net": name, "itrs": want[1], "fixed_ms": round(fixed_ms, 3), "turns": len(trace),
+                           "searched": turns, "relabelled": moved})
+            log(f"{name:28s} fixed={fixed_ms:8.2f} ms turns={len(trace)} searched={turns} relabelled={moved}")
+    return np.concatenate(xs), np.concatenate(ts), np.concatenate(ws), report
+
+
 def init_weights(seed: int = 1) -> np.ndarray:
     """He-uniform hidden layers, small output layer, zero biases."""
     rng = np.random.default_rng(seed)
@@ -183,10 +233,15 @@ def main() -> None:
     ap.add_argument("--seed", type=int, default=1)
     ap.add_argument("--streams", type=int, default=0,
                     help="also train on two continuously batched streams of this many nets each")
+    ap.add_argument("--labels", choices=("search", "constant"), default="search",
+                    help="per-decision local search (default), or the best constant schedule per net")
     args = ap.parse_args()
     t0 = time.time()
     nets = training_nets() + (training_streams(args.streams) if args.streams else [])
-    x, t, sw, report = collect(nets, args.reps, args.trace_cap)
+    if args.labels == "search":
+        x, t, sw, report = search(nets, args.reps, args.trace_cap)
+    else:
+        x, t, sw, report = collect(nets, args.reps, args.trace_cap)
     print(f"collected {len(x)} turns from {len(nets)} nets in {time.time() - t0:.1f} s")
     w0 = init_weights(args.seed)
     loss0, _ = hvm.policy_grad(w0, x, t, sw)
@@ -197,7 +252,7 @@ def main() -> None:
     out = {
         "format": "hvm_gb300 turn-scheduler MLP 16-64-64-3, packed W1 b1 W2 b2 W3 b3 (float32)",
         "params": [float(v) for v in w],
-        "training": {"nets": report, "turns": int(len(x)), "epochs": args.epochs, "lr": args.lr,
+        "training": {"labels": args.labels, "nets": report, "turns": int(len(x)), "epochs": args.epochs, "lr": args.lr,
                      "loss_initial": loss0, "loss_final": loss, "seed": args.seed},
         "evaluation": rows,
     }

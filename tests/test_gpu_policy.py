@@ -139,6 +139,18 @@ def test_schedules_are_bit_exact(hvm, workloads, config_goldens, case):
         tr = rt.trace()
         assert tr and all(0.0 <= o <= 1.0 for r in tr for o in r["outputs"])
         assert all(np.isfinite(r["features"]).all() for r in tr)
+        # A per-turn script (the local search's probe): random decisions at
+        # every turn, then one decision at a single turn.
+        script = rng.uniform(0.0, 1.0, 3 * 64).astype(np.float32)
+        for s in (script, [-1.0] * 6 + [1.0, 0.0, -1.0]):
+            rt.set_policy(hvm.POLICY_SCRIPT, weights=s)
+            st = rt.run()
+            assert st.itrs == gold["itrs"]
+            assert _canon_sha(hvm, rt.result()) == gold["canonical_sha256"]
+        # The decision a script gives at turn 0 is the one the trace records.
+        rt.set_policy(hvm.POLICY_SCRIPT, weights=[0.3, 0.0, -1.0])  # 512 rounds (under the 1024 cap)
+        rt.run()
+        assert rt.trace()[0]["outputs"][:2] == pytest.approx([0.3, 0.0], abs=1e-6)
 
 
 def test_committed_policy_on_skewed_fold(hvm, workloads, config_goldens):
@@ -159,6 +171,8 @@ def test_policy_errors(hvm):
             rt.set_policy(hvm.POLICY_LEARNED, weights=[0.0] * 10)
         with pytest.raises(hvm.HvmError):
             rt.set_policy(7)
+        with pytest.raises(hvm.HvmError):
+            rt.set_policy(hvm.POLICY_SCRIPT, weights=[0.5] * 4)  # not 3 per turn
         bad = np.zeros(hvm.POLICY_PARAMS, dtype=np.float32)
         bad[5] = np.nan
         with pytest.raises(hvm.HvmError):
