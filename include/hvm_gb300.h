@@ -109,7 +109,11 @@ typedef struct {
                                  110-290), same interaction counts: 0 = off (default); 1 = a def whose
                                  root is `(?((s1 s2) r) r)` called with `(#X R)` switches on the spot;
                                  2 = also, a def whose root is a CON called with a CON annihilates it
-                                 on the spot */
+                                 on the spot (compiled for register caps 0, 5 and 8) */
+  uint32_t local_nets;        /* 1 = block-local nets in shared memory (the reference's LNet + LEAK,
+                                 src/hvm.cu:130-135, 1129-1174): fresh words of a turn in the block's
+                                 shared memory, copied out to HBM when a global var would point at
+                                 them and at the turn's end; 128-thread blocks, register caps 0/8 */
 } hvm_gb300_config;
 
 typedef struct {

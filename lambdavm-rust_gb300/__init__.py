@@ -53,6 +53,7 @@ class Config(ctypes.Structure):
         ("narrow_reg_cap", ctypes.c_uint32),
         ("rule_select", ctypes.c_uint32),
         ("fast_calls", ctypes.c_uint32),
+        ("local_nets", ctypes.c_uint32),
     ]
 
 

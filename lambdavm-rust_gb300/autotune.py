@@ -12,7 +12,7 @@ returns the fastest configuration:
   graph_turns     0 = one launch per turn; k = CUDA-graph replays of k turns
   rule_select     0 = every lane interacts each round; 1 = one rule class per round
   fast_calls      CALL-time fast paths: 0 off, 1 SWITCH pattern, 2 SWITCH and ANNI
-                  (compiled in for register caps 0 and 8 only)
+                  (compiled in for register caps 0, 5 and 8)
   policy          the fixed turn policy or the learned one
 
 Every candidate's interaction count and results are checked against the first
@@ -46,8 +46,8 @@ def candidates(space: dict | None = None) -> list[dict]:
     space = space or DEFAULT_SPACE
     keys = list(space)
     out = [dict(zip(keys, vals)) for vals in itertools.product(*(space[k] for k in keys))]
-    # The fast-path kernel variants exist for register caps 0 and 8 only.
-    return [c for c in out if not (c.get("fast_calls") and c.get("reg_cap_blocks", 8) not in (0, 8))]
+    # The fast-path kernel variants exist for register caps 0, 5 and 8.
+    return [c for c in out if not (c.get("fast_calls") and c.get("reg_cap_blocks", 8) not in (0, 5, 8))]
 
 
 def make_runtime(cand: dict, device: int = 0, weights=None, **extra):

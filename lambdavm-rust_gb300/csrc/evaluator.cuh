@@ -32,6 +32,7 @@ enum : uint32_t {
   ST_LINK_UNSET = 4,    // a link met a var word that was never created
   ST_LINK_LIMIT = 5,    // a substitution chain exceeded the iteration bound
   ST_BAD_REF = 6,       // a REF to a definition the book does not have
+  ST_DRAIN = 7,         // a turn's end could not make its local net global within the bound
 };
 
 // One book definition on the device. Pairs for a def are stored at
@@ -126,6 +127,14 @@ struct alignas(128) Ctl {
 
 constexpr Pair NODE_MARK = ~0ull;
 
+// Node and var indices below LOCAL_WORDS name a block's local net (shared
+// memory) in the local-net kernel variant; the global allocator never hands
+// them out (the first pages of each space are reserved in every variant).
+constexpr uint32_t LOCAL_WORDS = 2048;
+__host__ __device__ __forceinline__ uint32_t reserved_pages(uint32_t page_log2) {
+  return (LOCAL_WORDS + (1u << page_log2) - 1) >> page_log2;
+}
+
 struct PagedSpace {
   uint32_t page_log2;        // words per page = 1 << page_log2
   uint32_t max_pages;        // capacity of each thread's page list
@@ -155,6 +164,7 @@ struct Dev {
   uint32_t* vloc;             // CALL scratch: [max_def_vars][nthreads]
   uint32_t nthreads;
   uint32_t ndefs;
+  Pair* ovf;                  // local-net variant: OVF_CAP overflow entries per thread
   uint32_t steal_min;         // a lane gives a redex to an empty lane of its warp once it holds this many
   uint32_t rule_select;       // 0: every lane runs its redex each round; 1/2: one rule class / rule per round
   uint32_t fast_calls;        // CALL-time fast paths: 0 off, 1 SWITCH pattern, 2 SWITCH and ANNI
@@ -210,6 +220,64 @@ struct TState {
   uint32_t waited;            // rounds this lane's next redex has waited for its rule class
 };
 
+// ---- local nets (the local-net kernel variant) ----------------------------------
+//
+// As in the reference's CUDA runtime (src/hvm.cu:130-135, 1129-1174), a
+// block's fresh nodes and vars live in shared memory while a turn runs, and
+// nothing in global memory may point into it: indices below LOCAL_WORDS name
+// the block's local words. A lane owns a slice of LOCAL_SLICE nodes and vars.
+// The linker never writes a local port into a global var (it redirects a
+// local var, and turns a local node into a LEAK redex that copies it out);
+// a fresh global node never holds a local port; redexes that name local
+// words stay with the lane (its deque, and an overflow stack of its own in
+// global memory) until the turn's end, when every one of them is made
+// global -- its local ends wired to fresh global vars, its local nodes
+// copied out by LEAK -- before the flush to the ring.
+constexpr uint32_t LOCAL_SLICE = 16;      // local nodes and vars per lane (128-thread blocks)
+constexpr uint32_t OVF_CAP = 256;         // a lane's overflow stack
+constexpr uint32_t OVF_HIGH = OVF_CAP - 64;  // a warp whose lane holds more ends its turn
+__device__ __forceinline__ bool is_local(Port p) {
+  return (get_tag(p) == VAR || get_tag(p) >= CON) && get_val(p) < LOCAL_WORDS && p != 0;
+}
+__device__ __forceinline__ bool is_gvar(Port p) { return get_tag(p) == VAR && get_val(p) >= LOCAL_WORDS; }
+__device__ __forceinline__ bool local_pair(Pair r) { return is_local(get_fst(r)) || is_local(get_snd(r)); }
+
+// The local-net variant's per-block arrays follow the deques in dynamic
+// shared memory: local nodes, local vars, then each lane's overflow length;
+// a lane's slice starts at threadIdx.x * LOCAL_SLICE, and its overflow stack
+// (global memory, read and written by that lane only) at gid * OVF_CAP. They
+// are computed rather than kept in the thread state, which the default
+// variants share.
+__device__ __forceinline__ Pair* lnode_of(const TState& t) { return t.stk - threadIdx.x + (size_t)t.stride * t.cap; }
+__device__ __forceinline__ Port* lvar_of(const TState& t) { return (Port*)(lnode_of(t) + LOCAL_WORDS); }
+__device__ __forceinline__ uint32_t& ovf_len_of(const TState& t) { return ((uint32_t*)(lvar_of(t) + LOCAL_WORDS))[threadIdx.x]; }
+__device__ __forceinline__ Pair* ovf_of(const Dev& d, const TState& t) { return d.ovf + (size_t)t.gid * OVF_CAP; }
+__device__ __forceinline__ uint32_t lbase_of() { return threadIdx.x * LOCAL_SLICE; }
+
+// Net word access that resolves local indices to the block's shared arrays.
+template <bool LOCAL>
+__device__ __forceinline__ Pair n_load(const Dev& d, const TState& t, uint32_t i) {
+  if (LOCAL && i < LOCAL_WORDS) return ((volatile Pair*)lnode_of(t))[i];
+  return nload(d, i);
+}
+template <bool LOCAL>
+__device__ __forceinline__ void n_store(const Dev& d, const TState& t, uint32_t i, Pair p) {
+  if (LOCAL && i < LOCAL_WORDS) ((volatile Pair*)lnode_of(t))[i] = p;
+  else nstore(d, i, p);
+}
+template <bool LOCAL>
+__device__ __forceinline__ void v_store(const Dev& d, const TState& t, uint32_t i, Port p) {
+  if (LOCAL && i < LOCAL_WORDS) ((volatile Port*)lvar_of(t))[i] = p;
+  else vstore(d, i, p);
+}
+template <bool LOCAL>
+__device__ __forceinline__ Port v_exch(const Dev& d, const TState& t, uint32_t i, Port p) {
+  if (LOCAL && i < LOCAL_WORDS) return atomicExch(&lvar_of(t)[i], p);
+  return vexch(d, i, p);
+}
+// Live-word accounting counts global words only (local ones end with the turn).
+__device__ __forceinline__ int global_words(uint32_t i, int n) { return i < LOCAL_WORDS ? 0 : n; }
+
 // Rule classes for per-round selection: mode 1 groups the rules by the code
 // they run -- no allocation (LINK, VOID, ERAS, ANNI), CALL, COMM, one or two
 // fresh nodes (OPER, SWIT); mode 2 uses the rule itself. Only a scheduling
@@ -232,7 +300,19 @@ __device__ __forceinline__ Pair& slot(TState& t, uint32_t i) {
   return t.stk[(size_t)((t.lo + i) & (t.cap - 1)) * t.stride];
 }
 
+template <bool LOCAL = false>
 __device__ __forceinline__ void spill_oldest(const Dev& d, TState& t, uint32_t k) {
+  if constexpr (LOCAL) {
+    // Local-net variant: the spilled redexes may name local words, so they
+    // stay with the lane; a warp ends its turn before an overflow fills.
+    uint32_t& n = ovf_len_of(t);
+    if (n + k > OVF_CAP) { set_status(d, ST_RING_FULL, 2); t.dead = true; return; }
+    for (uint32_t i = 0; i < k; i++) ovf_of(d, t)[n + i] = slot(t, i);
+    n += k;
+    t.lo = (t.lo + k) & (t.cap - 1);
+    t.len -= k;
+    return;
+  }
   unsigned long long at = atomicAdd(&d.ctl->tail, (unsigned long long)k);
   if (at + k - t.base > d.ring_mask + 1) { set_status(d, ST_RING_FULL, 0); t.dead = true; return; }
   for (uint32_t i = 0; i < k; i++) d.ring[(at + i) & d.ring_mask] = slot(t, i);
@@ -241,9 +321,10 @@ __device__ __forceinline__ void spill_oldest(const Dev& d, TState& t, uint32_t k
   t.leak += k;
 }
 
+template <bool LOCAL = false>
 __device__ __forceinline__ void push(const Dev& d, TState& t, Pair r) {
   if (t.len == t.cap) {
-    spill_oldest(d, t, t.cap / 2);
+    spill_oldest<LOCAL>(d, t, t.cap / 2);
     if (t.dead) return;
   }
   slot(t, t.len) = r;
@@ -431,6 +512,40 @@ __device__ __forceinline__ uint32_t alloc_run(const Dev& d, TState& t, Alloc& a,
 }
 
 __device__ __forceinline__ uint32_t alloc_node(const Dev& d, TState& t) { return alloc_run<false>(d, t, t.na, 1); }
+
+// Local-net variant: n (<= LOCAL_SLICE) consecutive free words of the lane's
+// slice of the block's local net, or 0. The slice's words are read afresh
+// (other lanes free words in it when they take them); taken vars are created
+// (NONE) at once, taken nodes are written by the caller before the lane's
+// next allocation.
+template <bool VARS>
+__device__ __forceinline__ uint32_t lalloc(TState& t, uint32_t n) {
+  uint32_t m = 0;
+  if (VARS) {
+    const unsigned at = (unsigned)__cvta_generic_to_shared(lvar_of(t) + lbase_of());
+    #pragma unroll
+    for (int k = 0; k < (int)LOCAL_SLICE / 4; k++) {
+      unsigned x, y, z, w;
+      asm volatile("ld.shared.v4.u32 {%0,%1,%2,%3}, [%4];" : "=r"(x), "=r"(y), "=r"(z), "=r"(w) : "r"(at + 16 * k) : "memory");
+      m |= ((x == 0) | (y == 0) << 1 | (z == 0) << 2 | (w == 0) << 3) << (4 * k);
+    }
+  } else {
+    const unsigned at = (unsigned)__cvta_generic_to_shared(lnode_of(t) + lbase_of());
+    #pragma unroll
+    for (int k = 0; k < (int)LOCAL_SLICE / 2; k++) {
+      unsigned long long x, y;
+      asm volatile("ld.shared.v2.u64 {%0,%1}, [%2];" : "=l"(x), "=l"(y) : "r"(at + 16 * k) : "memory");
+      m |= ((x == 0) | (y == 0) << 1) << (2 * k);
+    }
+  }
+  if (threadIdx.x == 0) m &= ~1u;  // index 0 is never handed out
+  const uint32_t r = runs_of(m, n);
+  if (!r) return 0;
+  const uint32_t at = lbase_of() + (__ffs(r) - 1);
+  if (VARS)
+    for (uint32_t i = 0; i < n; i++) ((volatile Port*)lvar_of(t))[at + i] = NONE;
+  return at;
+}
 __device__ __forceinline__ uint32_t alloc_var(const Dev& d, TState& t) { return alloc_run<true>(d, t, t.va, 1); }
 
 // Loads a thread's allocator state at turn start; it resumes at the chunk it
@@ -498,11 +613,18 @@ struct Plan {
   uint32_t fpad;        // CALL: the def's fast-path word (0 unless the caller is a CON)
   uint32_t fast;        // CALL: 0, or the fast path taken: 1 ANNI, 2 SWITCH on 0, 3 SWITCH on X > 0
   Port f1, f2;          // CALL fast path: the def-side ports of its two links
+  Port lx1, ly1, lx2, ly2;  // local-net variant: extra links of LEAK, GLOBALIZE and a fresh global
+                            // node's fixed-up port
 #ifdef HVM_COMPILED_CALLS
   uint32_t fid;         // CALL: the def
 #endif
 };
 constexpr uint32_t IDLE_RULE = 8;
+// Local-net variant only: LEAK copies a local node out to a global var's
+// target (src/hvm.cu:1129-1174); GLOBALIZE, at a turn's end, wires a redex's
+// local ends to fresh global vars so the redex can go to the ring. Neither
+// counts as an interaction.
+constexpr uint32_t LEAK_RULE = 9, GLOB_RULE = 10;
 
 #ifdef HVM_COMPILED_CALLS
 // Compiled calls (the reference's compile_book for its CUDA target,
@@ -534,8 +656,17 @@ __device__ __forceinline__ Port relocate(const Dev& d, uint32_t gid, const Plan&
 }
 
 // The i-th port pair of the lane's rule (src/hvm.c:852-1070).
-template <bool FAST>
+template <bool FAST, bool LOCAL>
 __device__ __forceinline__ void link_pair(const Dev& d, uint32_t gid, const Plan& p, uint32_t i, Port& x, Port& y) {
+  if (LOCAL && (p.rule == LEAK_RULE || p.rule == GLOB_RULE || ((p.rule == OPER || p.rule == SWIT) && i > 0))) {
+    // LEAK: the global var ~ the copied node, then its children's wires;
+    // GLOBALIZE: its wires; OPER/SWIT: link 1 is the fixed-up port's wire.
+    const uint32_t j = p.rule == LEAK_RULE ? i : p.rule == GLOB_RULE ? i + 1 : i;
+    if (j == 0) { x = p.a; y = new_port(get_tag(p.b), p.nbase); }
+    else if (j == 1) { x = p.lx1; y = p.ly1; }
+    else { x = p.lx2; y = p.ly2; }
+    return;
+  }
   switch (p.rule) {
     case LINK: x = p.a; y = p.b; break;
     case ERAS: x = p.a; y = i == 0 ? get_fst(p.B) : get_snd(p.B); break;
@@ -582,15 +713,22 @@ __device__ __forceinline__ void link_pair(const Dev& d, uint32_t gid, const Plan
 }
 
 // Plans lane's interaction on redex r; returns false for an invalid REF.
-template <bool FAST>
-__device__ __forceinline__ bool plan_redex(const Dev& d, TState& t, Pair r, Plan& p) {
+template <bool FAST, bool LOCAL>
+__device__ __forceinline__ bool plan_redex(const Dev& d, TState& t, Pair r, Plan& p, bool drain) {
   Port a = get_fst(r), b = get_snd(r);
-  Rule rule = get_rule(a, b);
+  uint32_t rule = get_rule(a, b);
   // REF ~ ROOT is a call (src/hvm.c:1090-1092); a batch has one ROOT var per net.
   if (get_tag(a) == REF && get_tag(b) == VAR && get_val(b) >= ROOT_VAR - d.extra_roots) rule = CALL;
   else if (should_swap(a, b)) { Port x = a; a = b; b = x; }
   p.a = a; p.b = b;
-  p.counted = rule != LINK;
+  if (LOCAL) {
+    // A global var meeting a local node is a LEAK; at a turn's end every
+    // other redex that names local words is made global.
+    if (rule == LINK && is_gvar(a) && get_tag(b) >= CON && get_val(b) < LOCAL_WORDS) rule = LEAK_RULE;
+    else if (drain) rule = GLOB_RULE;
+  }
+  if constexpr (LOCAL) p.counted = rule != LINK && rule != LEAK_RULE && rule != GLOB_RULE;
+  else p.counted = rule != LINK;
   p.node_len = p.rbag_len = p.vars_len = 0;
   p.fpad = 0;
   p.fast = 0;
@@ -625,63 +763,102 @@ struct Slot {
 
 // Takes the lane's next port pairs into an idle slot, wiring on the spot every
 // pair that needs no exchange (both sides principal: a new redex).
-template <bool FAST>
+template <bool FAST, bool LOCAL>
 __device__ __forceinline__ void slot_fill(const Dev& d, TState& t, const Plan& p, uint32_t& next, Slot& s) {
   while (!s.busy && next < p.nlinks) {
-    link_pair<FAST>(d, t.gid, p, next++, s.X, s.Y);
+    link_pair<FAST, LOCAL>(d, t.gid, p, next++, s.X, s.Y);
     if (get_tag(s.X) != VAR && get_tag(s.Y) == VAR) { Port z = s.X; s.X = s.Y; s.Y = z; }
-    if (get_tag(s.X) != VAR) push(d, t, new_pair(s.X, s.Y));
+    if (get_tag(s.X) != VAR) push<LOCAL>(d, t, new_pair(s.X, s.Y));
     else { s.busy = true; s.entered = false; }
   }
 }
 
 // The exchange this slot needs next: enter Y while it is a var
 // (src/hvm.c:793-808), then publish X -> Y.
+// Local-net variant, before a slot's next step: a global var may not be
+// pointed at a local word. A local var is swapped in as the side written (it
+// then points at the global var, entered first); a local node becomes a LEAK
+// redex that copies it out (src/hvm.cu:1049-1079).
+template <bool LOCAL>
+__device__ __forceinline__ void slot_leak(const Dev& d, TState& t, Slot& s) {
+  if (!LOCAL || !s.busy) return;
+  const bool enter_step = !s.entered && get_tag(s.Y) == VAR;
+  if (enter_step || !is_gvar(s.X) || !is_local(s.Y)) return;
+  if (get_tag(s.Y) == VAR) {
+    Port z = s.X; s.X = s.Y; s.Y = z;
+    s.entered = false;
+  } else {
+    push<LOCAL>(d, t, new_pair(s.X, s.Y));
+    s.busy = false;
+  }
+}
+
 __device__ __forceinline__ void slot_request(const Slot& s, uint32_t& addr, Port& put) {
   const bool enter_step = !s.entered && get_tag(s.Y) == VAR;
   addr = enter_step ? get_val(s.Y) : get_val(s.X);
   put = enter_step ? NONE : s.Y;
 }
 
+template <bool LOCAL>
 __device__ __forceinline__ void slot_result(const Dev& d, TState& t, Slot& s, uint32_t addr, Port got) {
   if (!s.busy) return;
   const bool enter_step = !s.entered && get_tag(s.Y) == VAR;
   if (enter_step) {
     if (got == NONE || got == 0) s.entered = true;
-    else { vstore(d, addr, 0); t.live_vars--; s.Y = got; }
+    else {
+      if constexpr (LOCAL) { v_store<LOCAL>(d, t, addr, 0); t.live_vars -= global_words(addr, 1); }
+      else { vstore(d, addr, 0); t.live_vars--; }
+      s.Y = got;
+    }
   } else if (got == NONE) {
     s.busy = false;  // the other side will find Y here
   } else if (got == 0) {
     set_status(d, ST_LINK_UNSET, addr); t.dead = true; s.busy = false;
   } else {
     // The other side had published `got` for X: take X and wire got ~ Y.
-    vstore(d, addr, 0);
-    t.live_vars--;
+    if constexpr (LOCAL) { v_store<LOCAL>(d, t, addr, 0); t.live_vars -= global_words(addr, 1); }
+    else { vstore(d, addr, 0); t.live_vars--; }
     s.X = got;
     s.entered = false;
     if (get_tag(s.X) != VAR && get_tag(s.Y) == VAR) { Port z = s.X; s.X = s.Y; s.Y = z; }
-    if (get_tag(s.X) != VAR) { push(d, t, new_pair(s.X, s.Y)); s.busy = false; }
+    if (get_tag(s.X) != VAR) { push<LOCAL>(d, t, new_pair(s.X, s.Y)); s.busy = false; }
   }
 }
 
 // Runs one round for the warp: every lane with `has` interacts on `r`.
 // Returns the lane's outcome (IR_DONE / IR_RETRY / IR_FATAL).
-template <bool FAST>
-__device__ __forceinline__ int lockstep_round(const Dev& d, TState& t, bool has, Pair r, WarpProf* wp) {
+// Local-net variant: a redex made global at a turn's end goes to the ring.
+__device__ __forceinline__ void ring_put(const Dev& d, TState& t, Pair r) {
+  const unsigned long long at = atomicAdd(&d.ctl->tail, 1ull);
+  if (at + 1 - t.base > d.ring_mask + 1) { set_status(d, ST_RING_FULL, 3); t.dead = true; return; }
+  d.ring[at & d.ring_mask] = r;
+  t.leak++;
+}
+
+// `drain` (local-net variant, at a turn's end): every redex given is made
+// global (LEAK or GLOBALIZE) instead of interacting. HREG selects how the
+// per-rule counters are indexed: by constant indices (the thread state then
+// lives in registers), or by the rule (which keeps the thread state in local
+// memory) -- measured faster for the 64-register variant, whose registers
+// cannot hold the state.
+template <bool FAST, bool LOCAL, bool HREG = true>
+__device__ __forceinline__ int lockstep_round(const Dev& d, TState& t, bool has, Pair r, WarpProf* wp,
+                                              bool drain = false) {
   long long c0 = wp ? clock64() : 0;
   Plan p;
   p.rule = IDLE_RULE;
   p.nlinks = 0;
   p.A = p.B = 0;
-  if (has && !plan_redex<FAST>(d, t, r, p)) has = false;
+  if (has && !plan_redex<FAST, LOCAL>(d, t, r, p, LOCAL && drain)) has = false;
   const uint32_t rule = p.rule;
 
   // 2. load the principal nodes
   const bool needA = rule == ANNI || rule == COMM;
-  const bool needB = rule == ERAS || rule == ANNI || rule == COMM || rule == OPER || rule == SWIT;
+  const bool needB = rule == ERAS || rule == ANNI || rule == COMM || rule == OPER || rule == SWIT ||
+                     (LOCAL && rule == LEAK_RULE);
   const bool peekB = FAST && rule == CALL && fast_kind(p.fpad);  // a CALL fast path needs the caller's node
-  if (needA) p.A = nload(d, get_val(p.a));
-  if (needB || peekB) p.B = nload(d, get_val(p.b));
+  if (needA) p.A = n_load<LOCAL>(d, t, get_val(p.a));
+  if (needB || peekB) p.B = n_load<LOCAL>(d, t, get_val(p.b));
   int rc = IR_DONE;
   if ((needA && p.A == 0) || (needB && p.B == 0)) rc = IR_RETRY;  // not yet visible: re-try later
   if (peekB && p.B != 0) {
@@ -700,23 +877,74 @@ __device__ __forceinline__ int lockstep_round(const Dev& d, TState& t, bool has,
   // 3. allocate; 4. write
   bool made = false;
   if (rc == IR_DONE && rule != IDLE_RULE) {
-    if (needA) nstore(d, get_val(p.a), 0);
-    if (needB) nstore(d, get_val(p.b), 0);
-    t.live_nodes -= (needA ? 1 : 0) + (needB ? 1 : 0);
-    switch (rule) {
+    if (needA) n_store<LOCAL>(d, t, get_val(p.a), 0);
+    if (needB) n_store<LOCAL>(d, t, get_val(p.b), 0);
+    if (LOCAL) t.live_nodes -= (needA ? global_words(get_val(p.a), 1) : 0) + (needB ? global_words(get_val(p.b), 1) : 0);
+    else t.live_nodes -= (needA ? 1 : 0) + (needB ? 1 : 0);
+    if constexpr (LOCAL) {
+      if (rule == LEAK_RULE) {
+        // a (a global var) ~ b (a local node, taken above): copy the node to
+        // a fresh global node whose local children become fresh global vars
+        // wired to them, and point a at the copy (src/hvm.cu:1136-1174).
+        const Port c1 = get_fst(p.B), c2 = get_snd(p.B);
+        const bool l1 = is_local(c1), l2 = is_local(c2);
+        p.nbase = alloc_run<false, false>(d, t, t.na, 1);
+        const uint32_t g1 = l1 ? alloc_run<true>(d, t, t.va, 1) : 1;
+        const uint32_t g2 = l2 ? alloc_run<true>(d, t, t.va, 1) : 1;
+        if (!p.nbase || !g1 || !g2) {
+          rc = IR_FATAL;
+        } else {
+          const Port n1 = l1 ? new_port(VAR, g1) : c1, n2 = l2 ? new_port(VAR, g2) : c2;
+          nstore(d, p.nbase, new_pair(n1, n2));
+          p.lx1 = l1 ? n1 : n2; p.ly1 = l1 ? c1 : c2;
+          p.lx2 = n2; p.ly2 = c2;
+          p.nlinks = 1 + (l1 ? 1 : 0) + (l2 ? 1 : 0);
+          made = true;
+        }
+      } else if (rule == GLOB_RULE) {
+        // Turn's end: each local end of the redex is wired to a fresh global
+        // var, and the redex, now global, goes to the ring.
+        const bool la = is_local(p.a), lb = is_local(p.b);
+        const uint32_t ga = la ? alloc_run<true>(d, t, t.va, 1) : 1;
+        const uint32_t gb = lb ? alloc_run<true>(d, t, t.va, 1) : 1;
+        if (!ga || !gb) {
+          rc = IR_FATAL;
+        } else {
+          const Port a2 = la ? new_port(VAR, ga) : p.a, b2 = lb ? new_port(VAR, gb) : p.b;
+          ring_put(d, t, new_pair(a2, b2));
+          p.lx1 = la ? a2 : b2; p.ly1 = la ? p.a : p.b;
+          p.lx2 = b2; p.ly2 = p.b;
+          p.nlinks = (la ? 1 : 0) + (lb ? 1 : 0);
+          made = true;
+        }
+      }
+    }
+    if (!LOCAL || (rule != LEAK_RULE && rule != GLOB_RULE)) switch (rule) {
       case LINK: p.nlinks = 1; break;
       case VOID: p.nlinks = 0; break;
       case ERAS: case ANNI: p.nlinks = 2; break;
       case COMM: {
-        // Vars first (taken as NONE), then the nodes, filled right below (no mark).
-        p.vbase = alloc_run<true>(d, t, t.va, 4);
-        p.nbase = p.vbase ? alloc_run<false, false>(d, t, t.na, 4) : 0;
+        // Vars first (taken as NONE), then the nodes, filled right below (no
+        // mark); in the block's local net when the lane's slice has room.
+        if constexpr (LOCAL) {
+          p.vbase = lalloc<true>(t, 4);
+          p.nbase = p.vbase ? lalloc<false>(t, 4) : 0;
+          if (p.vbase && !p.nbase)
+            for (uint32_t i = 0; i < 4; i++) v_store<LOCAL>(d, t, p.vbase + i, 0);
+          if (!p.nbase) {
+            p.vbase = alloc_run<true>(d, t, t.va, 4);
+            p.nbase = p.vbase ? alloc_run<false, false>(d, t, t.na, 4) : 0;
+          }
+        } else {
+          p.vbase = alloc_run<true>(d, t, t.va, 4);
+          p.nbase = p.vbase ? alloc_run<false, false>(d, t, t.na, 4) : 0;
+        }
         if (!p.vbase || !p.nbase) { rc = IR_FATAL; break; }
         const uint32_t v = p.vbase;
-        nstore(d, p.nbase + 0, new_pair(new_port(VAR, v + 0), new_port(VAR, v + 1)));
-        nstore(d, p.nbase + 1, new_pair(new_port(VAR, v + 2), new_port(VAR, v + 3)));
-        nstore(d, p.nbase + 2, new_pair(new_port(VAR, v + 0), new_port(VAR, v + 2)));
-        nstore(d, p.nbase + 3, new_pair(new_port(VAR, v + 1), new_port(VAR, v + 3)));
+        n_store<LOCAL>(d, t, p.nbase + 0, new_pair(new_port(VAR, v + 0), new_port(VAR, v + 1)));
+        n_store<LOCAL>(d, t, p.nbase + 1, new_pair(new_port(VAR, v + 2), new_port(VAR, v + 3)));
+        n_store<LOCAL>(d, t, p.nbase + 2, new_pair(new_port(VAR, v + 0), new_port(VAR, v + 2)));
+        n_store<LOCAL>(d, t, p.nbase + 3, new_pair(new_port(VAR, v + 1), new_port(VAR, v + 3)));
         made = true;
         p.nlinks = 4;
         break;
@@ -724,34 +952,71 @@ __device__ __forceinline__ int lockstep_round(const Dev& d, TState& t, bool has,
       case OPER: {
         Port b1 = get_fst(p.B);
         p.oper_num = get_tag(b1) == NUM;
+        p.nlinks = 1;
         if (p.oper_num) {
           p.cv = operate(get_val(p.a), get_val(b1));
         } else {
-          p.nbase = alloc_run<false, false>(d, t, t.na, 1);
+          if constexpr (LOCAL) {
+            p.nbase = lalloc<false>(t, 1);
+            if (!p.nbase) p.nbase = alloc_run<false, false>(d, t, t.na, 1);
+          } else {
+            p.nbase = alloc_run<false, false>(d, t, t.na, 1);
+          }
           if (!p.nbase) { rc = IR_FATAL; break; }
-          nstore(d, p.nbase, new_pair(p.a, get_snd(p.B)));
+          Port b2 = get_snd(p.B);
+          if constexpr (LOCAL) if (p.nbase >= LOCAL_WORDS && is_local(b2)) {
+            // Local-net variant: a fresh global node cannot hold a local
+            // port; a fresh global var takes its place, wired to it by one
+            // more link.
+            const uint32_t g = alloc_run<true>(d, t, t.va, 1);
+            if (!g) { rc = IR_FATAL; break; }
+            p.lx1 = new_port(VAR, g); p.ly1 = b2; p.nlinks = 2;
+            b2 = p.lx1;
+          }
+          n_store<LOCAL>(d, t, p.nbase, new_pair(p.a, b2));
           made = true;
         }
-        p.nlinks = 1;
         break;
       }
       case SWIT: {
         uint32_t n = get_u24(get_val(p.a));
-        p.nbase = alloc_run<false, false>(d, t, t.na, n == 0 ? 1 : 2);
-        if (!p.nbase) { rc = IR_FATAL; break; }
-        if (n == 0) {
-          nstore(d, p.nbase, new_pair(get_snd(p.B), new_port(ERA, 0)));
+        p.nlinks = 1;
+        if constexpr (LOCAL) {
+          p.nbase = lalloc<false>(t, n == 0 ? 1 : 2);
+          if (!p.nbase) p.nbase = alloc_run<false, false>(d, t, t.na, n == 0 ? 1 : 2);
         } else {
-          nstore(d, p.nbase, new_pair(new_port(ERA, 0), new_port(CON, p.nbase + 1)));
-          nstore(d, p.nbase + 1, new_pair(new_port(NUM, new_u24(n - 1)), get_snd(p.B)));
+          p.nbase = alloc_run<false, false>(d, t, t.na, n == 0 ? 1 : 2);
+        }
+        if (!p.nbase) { rc = IR_FATAL; break; }
+        Port b2 = get_snd(p.B);
+        if constexpr (LOCAL) if (p.nbase >= LOCAL_WORDS && is_local(b2)) {  // as in OPER
+          const uint32_t g = alloc_run<true>(d, t, t.va, 1);
+          if (!g) { rc = IR_FATAL; break; }
+          p.lx1 = new_port(VAR, g); p.ly1 = b2; p.nlinks = 2;
+          b2 = p.lx1;
+        }
+        if (n == 0) {
+          n_store<LOCAL>(d, t, p.nbase, new_pair(b2, new_port(ERA, 0)));
+        } else {
+          n_store<LOCAL>(d, t, p.nbase, new_pair(new_port(ERA, 0), new_port(CON, p.nbase + 1)));
+          n_store<LOCAL>(d, t, p.nbase + 1, new_pair(new_port(NUM, new_u24(n - 1)), b2));
         }
         made = true;
-        p.nlinks = 1;
         break;
       }
       default: {  // CALL (src/hvm.c:865-898)
         p.contig = p.node_len <= CHUNK && p.vars_len <= CHUNK;
-        if (p.contig) {
+        bool loc = false;
+        if (LOCAL && p.node_len <= LOCAL_SLICE && p.vars_len <= LOCAL_SLICE) {
+          // The def's words in the lane's slice of the local net, if it has room.
+          p.vbase = p.vars_len ? lalloc<true>(t, p.vars_len) : 0;
+          p.nbase = (p.node_len && (p.vbase || !p.vars_len)) ? lalloc<false>(t, p.node_len) : 0;
+          loc = (!p.vars_len || p.vbase) && (!p.node_len || p.nbase);
+          if (!loc && p.vbase)
+            for (uint32_t i = 0; i < p.vars_len; i++) v_store<LOCAL>(d, t, p.vbase + i, 0);
+          if (loc) p.contig = true;
+        }
+        if (p.contig && !loc) {
           // Vars first (taken as NONE), then the nodes: one contiguous run
           // each, so relocation is base + index. In a fragmented space the
           // runs may not be found quickly; then the words are taken one by
@@ -799,7 +1064,7 @@ __device__ __forceinline__ int lockstep_round(const Dev& d, TState& t, bool has,
             continue;
           }
           Pair q = __ldg((const unsigned long long*)&nodes[i]);
-          nstore(d, at, new_pair(relocate(d, t.gid, p, get_fst(q)), relocate(d, t.gid, p, get_snd(q))));
+          n_store<LOCAL>(d, t, at, new_pair(relocate(d, t.gid, p, get_fst(q)), relocate(d, t.gid, p, get_snd(q))));
         }
         t.live_nodes -= __popc(skip);
         if (FAST && p.fast) {
@@ -845,19 +1110,21 @@ __device__ __forceinline__ int lockstep_round(const Dev& d, TState& t, bool has,
   Slot s0, s1;
   s0.busy = s1.busy = false;
   for (uint32_t guard = 0; guard < (1u << 24); guard++) {
-    slot_fill<FAST>(d, t, p, next, s0);
-    slot_fill<FAST>(d, t, p, next, s1);
+    slot_fill<FAST, LOCAL>(d, t, p, next, s0);
+    slot_fill<FAST, LOCAL>(d, t, p, next, s1);
     if (!__any_sync(0xFFFFFFFFu, s0.busy || s1.busy)) break;
     if (fence_due) { __threadfence(); fence_due = false; t.dirty = false; }
     steps++;
+    slot_leak<LOCAL>(d, t, s0);
+    slot_leak<LOCAL>(d, t, s1);
     uint32_t a0, a1;
     Port q0, q1;
     slot_request(s0, a0, q0);
     slot_request(s1, a1, q1);
-    Port g0 = s0.busy ? vexch(d, a0, q0) : 0;
-    Port g1 = s1.busy ? vexch(d, a1, q1) : 0;
-    slot_result(d, t, s0, a0, g0);
-    slot_result(d, t, s1, a1, g1);
+    Port g0 = s0.busy ? v_exch<LOCAL>(d, t, a0, q0) : 0;
+    Port g1 = s1.busy ? v_exch<LOCAL>(d, t, a1, q1) : 0;
+    slot_result<LOCAL>(d, t, s0, a0, g0);
+    slot_result<LOCAL>(d, t, s1, a1, g1);
   }
 
   if (wp) {
@@ -871,10 +1138,23 @@ __device__ __forceinline__ int lockstep_round(const Dev& d, TState& t, bool has,
     wp->v[PROF_CYC_FENCE] += c3 - c2;
     wp->v[PROF_CYC_LINK] += c4 - c3;
   }
-  if (has && rc == IR_RETRY) { push(d, t, r); t.retries++; }
+  if (has && rc == IR_RETRY) { push<LOCAL>(d, t, r); t.retries++; }
+  if (LOCAL && has && rc == IR_DONE && rule == LEAK_RULE) t.hist[LINK]++;  // LEAK copies (not interactions)
   if (has && rc == IR_DONE && p.counted) {
     t.itrs++;
-    t.hist[rule]++;
+    if (!HREG) {
+      t.hist[rule]++;
+    } else {
+      switch (rule) {
+        case CALL: t.hist[CALL]++; break;
+        case VOID: t.hist[VOID]++; break;
+        case ERAS: t.hist[ERAS]++; break;
+        case ANNI: t.hist[ANNI]++; break;
+        case COMM: t.hist[COMM]++; break;
+        case OPER: t.hist[OPER]++; break;
+        default: t.hist[SWIT]++; break;
+      }
+    }
     if (FAST && p.fast) {  // the interactions a fast path performs in place (src/cmp.rs:147, 191, 220, 253)
       t.itrs += p.fast == 1 ? 1 : 3;
       t.hist[ANNI] += p.fast == 1 ? 1 : 2;

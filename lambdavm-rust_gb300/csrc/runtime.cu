@@ -65,6 +65,7 @@ static const char* status_text(uint32_t s) {
     case ST_LINK_UNSET: return "link met an uninitialised var";
     case ST_LINK_LIMIT: return "substitution chain too long";
     case ST_BAD_REF: return "reference to a missing definition";
+    case ST_DRAIN: return "local net not drained at the turn's end";
     default: return "unknown device error";
   }
 }
@@ -183,10 +184,11 @@ __device__ void apply_policy(Ctl* c, const float* o, unsigned long long pending,
 
 // MIN_BLOCKS_128 > 0 asks the compiler to fit that many 128-thread blocks per
 // SM (a register cap); the runtime picks the variant from the configuration.
-// FAST compiles in the CALL-time fast paths (Dev::fast_calls) and PROF the
-// per-phase clock counters (Ctl::prof); both are kept out of the default
-// variants because their code alone costs the others registers.
-template <int MIN_BLOCKS_128, bool FAST, bool PROF>
+// FAST compiles in the CALL-time fast paths (Dev::fast_calls), PROF the
+// per-phase clock counters (Ctl::prof) and LOCAL the block-local nets
+// (evaluator.cuh); each is kept out of the default variants because its code
+// alone costs the others registers.
+template <int MIN_BLOCKS_128, bool FAST, bool PROF, bool LOCAL>
 __global__ void __launch_bounds__(128, MIN_BLOCKS_128 > 0 ? MIN_BLOCKS_128 : 1) turn_kernel(Dev d, uint32_t cap) {
   extern __shared__ unsigned long long smem_stack[];
   Ctl* c = d.ctl;
@@ -224,12 +226,17 @@ __global__ void __launch_bounds__(128, MIN_BLOCKS_128 > 0 ? MIN_BLOCKS_128 : 1) 
   for (int i = 0; i < 8; i++) t.hist[i] = 0;
   t.dead = false;
   t.waited = 0;
+  if (LOCAL) {
+    // Each lane clears its own slice of the block's local net (128-thread blocks).
+    for (uint32_t i = 0; i < LOCAL_SLICE; i++) { lnode_of(t)[lbase_of() + i] = 0; lvar_of(t)[lbase_of() + i] = 0; }
+    ovf_len_of(t) = 0;
+  }
 
   // Static share of the input: items base + gid + k*N, k < s.
   for (uint32_t k = 0; k < s; k++) {
     unsigned long long at = base + t.gid + (unsigned long long)k * d.nthreads;
     if (at >= in_end) break;
-    push(d, t, (Pair)__ldcg((const unsigned long long*)&d.ring[at & d.ring_mask]));
+    push<LOCAL>(d, t, (Pair)__ldcg((const unsigned long long*)&d.ring[at & d.ring_mask]));
   }
 
   const unsigned lane = threadIdx.x & 31;
@@ -260,8 +267,10 @@ __global__ void __launch_bounds__(128, MIN_BLOCKS_128 > 0 ? MIN_BLOCKS_128 : 1) 
       Pair got = recv ? warp_stk[(size_t)dlo * t.stride + donor] : 0;
       __syncwarp();
       if (((give >> lane) & 1) && rg < m) { t.lo = (t.lo + 1) & (t.cap - 1); t.len--; }
-      if (recv) push(d, t, got);
+      if (recv) push<LOCAL>(d, t, got);
     }
+    // Local-net variant: a lane's own spilled redexes come back first.
+    if (LOCAL && t.len == 0 && ovf_len_of(t) > 0) push<LOCAL>(d, t, ovf_of(d, t)[--ovf_len_of(t)]);
     // Lanes still empty claim ring input, one atomic for the warp.
     unsigned empty = __ballot_sync(0xFFFFFFFFu, t.len == 0);
     if (empty && !ring_dry) {
@@ -273,7 +282,7 @@ __global__ void __launch_bounds__(128, MIN_BLOCKS_128 > 0 ? MIN_BLOCKS_128 : 1) 
       h = __shfl_sync(0xFFFFFFFFu, h, 0);
       unsigned k = __popc(empty & lt_mask);
       if (((empty >> lane) & 1) && h + k < in_end) {
-        push(d, t, (Pair)__ldcg((const unsigned long long*)&d.ring[(h + k) & d.ring_mask]));
+        push<LOCAL>(d, t, (Pair)__ldcg((const unsigned long long*)&d.ring[(h + k) & d.ring_mask]));
       }
       ring_dry = h + __popc(empty) >= in_end;
     }
@@ -303,13 +312,35 @@ __global__ void __launch_bounds__(128, MIN_BLOCKS_128 > 0 ? MIN_BLOCKS_128 : 1) 
     }
     const bool has = go;
     const Pair r = has ? pop(t) : 0;
-    lockstep_round<FAST>(d, t, has, r, prof_on ? &prof : nullptr);
+    lockstep_round<FAST, LOCAL, MIN_BLOCKS_128 != 8>(d, t, has, r, prof_on ? &prof : nullptr);
     if (__any_sync(0xFFFFFFFFu, t.dead)) break;
+    if (LOCAL && __any_sync(0xFFFFFFFFu, ovf_len_of(t) > OVF_HIGH)) break;  // end the turn before an overflow fills
     // The stop flag is tested one round after it was loaded, so its L2
     // latency hides behind a whole round (a short round would otherwise wait
     // for it).
     if (__shfl_sync(0xFFFFFFFFu, stop_flag, 0)) break;
     if (lane == 0) stop_flag = *(volatile unsigned*)&c->stop;
+  }
+
+  if (LOCAL) {
+    // Turn's end: every redex this lane holds that names local words is
+    // made global (GLOBALIZE; LEAK for the local nodes it reaches), the
+    // others go to the ring as they are; the block's local net then ends.
+    // A lane holds at most OVF_CAP + cap redexes and its block at most
+    // LOCAL_WORDS local nodes, each leaked once: the bound is generous.
+    for (uint32_t guard = 0;; guard++) {
+      if (t.len == 0 && ovf_len_of(t) > 0) push<LOCAL>(d, t, ovf_of(d, t)[--ovf_len_of(t)]);
+      bool has = t.len > 0 && !t.dead;
+      if (!__any_sync(0xFFFFFFFFu, has)) break;
+      if (guard >= (1u << 16)) {
+        if (lane == 0) set_status(d, ST_DRAIN, t.gid);
+        break;
+      }
+      const Pair r = has ? pop(t) : 0;
+      if (has && !local_pair(r)) { ring_put(d, t, r); has = false; }
+      lockstep_round<FAST, LOCAL, MIN_BLOCKS_128 != 8>(d, t, has, r, nullptr, true);
+      if (__any_sync(0xFFFFFFFFu, t.dead)) break;
+    }
   }
 
   if (prof_on && lane == 0) {
@@ -445,20 +476,21 @@ __global__ void __launch_bounds__(128, MIN_BLOCKS_128 > 0 ? MIN_BLOCKS_128 : 1) 
   }
 }
 
-// Gives thread g page g of each space and points both pools past them.
+// Gives thread g page g of each space (past the reserved first pages, whose
+// indices the local-net variant uses) and points both pools past them.
 __global__ void reset_alloc_kernel(Dev d) {
   uint32_t g = blockIdx.x * blockDim.x + threadIdx.x;
   if (g < d.nthreads) {
     for (const PagedSpace* sp : {&d.nspace, &d.vspace}) {
-      sp->lists[(size_t)g * sp->max_pages] = g;
+      sp->lists[(size_t)g * sp->max_pages] = g + reserved_pages(sp->page_log2);
       sp->counts[g] = 1;
       sp->pos[g] = 0;
       sp->off[g] = 0;
     }
   }
   if (g == 0) {
-    d.ctl->npool_next = d.nthreads;
-    d.ctl->vpool_next = d.nthreads;
+    d.ctl->npool_next = d.nthreads + reserved_pages(d.nspace.page_log2);
+    d.ctl->vpool_next = d.nthreads + reserved_pages(d.vspace.page_log2);
   }
 }
 
@@ -1046,6 +1078,7 @@ class Runtime {
   float policy_const[6] = {-1.f, -1.f, -1.f, -1.f, -1.f, -1.f};
   float* mem_policy = nullptr;
   float* mem_script = nullptr;          // POLICY_SCRIPT decisions, 3 floats per turn
+  void* mem_ovf = nullptr;              // local-net variant: per-thread overflow stacks
   size_t script_cap = 0, script_len = 0;
   double norm_seconds = 0;
   uint64_t norm_calls = 0;
@@ -1073,12 +1106,13 @@ class Runtime {
 
   void release() {
     void* ps[] = {mem_node, mem_vars, mem_ring, mem_cur, mem_scratch, mem_defs, mem_book, g_out, g_kids, g_info, ctl,
-                  mem_trace, mem_roots, mem_free, mem_mains, mem_policy, mem_script, list_buf};
+                  mem_trace, mem_roots, mem_free, mem_mains, mem_policy, mem_script, mem_ovf, list_buf};
     for (void* p : ps) if (p) cudaFree(p);
     mem_node = mem_vars = mem_ring = mem_cur = mem_scratch = mem_defs = mem_book = mem_trace = mem_roots = mem_free =
         mem_mains = nullptr;
     mem_policy = nullptr;
     mem_script = nullptr;
+    mem_ovf = nullptr;
     script_cap = script_len = 0;
     list_buf = nullptr;
     defs_bytes = book_bytes = scratch_bytes = 0;
@@ -1098,19 +1132,29 @@ class Runtime {
       return fail("node_log2/vars_log2 must be in [10, 29]");
     smem = (size_t)block * cap * sizeof(Pair);
     if (block > 128) return fail("threads_per_block must be <= 128");
+    if (cfg.local_nets > 1) return fail("local_nets must be 0 or 1");
+    if (cfg.local_nets) {
+      // The block's local net (LOCAL_WORDS nodes and vars: a slice per lane) follows the deques.
+      if (block * LOCAL_SLICE != LOCAL_WORDS) return fail("local_nets needs 128-thread blocks");
+      smem += (size_t)LOCAL_WORDS * (sizeof(Pair) + sizeof(Port)) + (size_t)block * sizeof(uint32_t);
+    }
     // The turn kernel variant (register cap) and its grid; with `narrow_below`,
     // a second variant runs the turns that start with fewer pending redexes.
     auto make_variant = [&](uint32_t reg_cap, Variant& v) -> int {
-      // The fast-path and profiling variants exist for the caps the defaults use.
-      const bool fast = cfg.fast_calls != 0, prof = cfg.profile != 0;
-      if (fast && prof) return fail("profile and fast_calls are not compiled together");
-      if ((fast || prof) && reg_cap != 0 && reg_cap != 8)
-        return fail("fast_calls and profile need reg_cap_blocks / narrow_reg_cap 0 or 8");
+      // The fast-path, profiling and local-net variants exist for the caps the defaults use.
+      const bool fast = cfg.fast_calls != 0, prof = cfg.profile != 0, local = cfg.local_nets != 0;
+      if ((fast ? 1 : 0) + (prof ? 1 : 0) + (local ? 1 : 0) > 1)
+        return fail("fast_calls, profile and local_nets are not compiled together");
+      if ((prof || local) && reg_cap != 0 && reg_cap != 8)
+        return fail("profile and local_nets need reg_cap_blocks / narrow_reg_cap 0 or 8");
+      if (fast && reg_cap == 6) return fail("fast_calls needs reg_cap_blocks / narrow_reg_cap 0, 5 or 8");
       switch (reg_cap) {
-        case 0: v.fn = fast ? turn_kernel<0, true, false> : prof ? turn_kernel<0, false, true> : turn_kernel<0, false, false>; break;
-        case 5: v.fn = turn_kernel<5, false, false>; break;
-        case 6: v.fn = turn_kernel<6, false, false>; break;
-        case 8: v.fn = fast ? turn_kernel<8, true, false> : prof ? turn_kernel<8, false, true> : turn_kernel<8, false, false>; break;
+        case 0: v.fn = fast ? turn_kernel<0, true, false, false> : prof ? turn_kernel<0, false, true, false>
+                     : local ? turn_kernel<0, false, false, true> : turn_kernel<0, false, false, false>; break;
+        case 5: v.fn = fast ? turn_kernel<5, true, false, false> : turn_kernel<5, false, false, false>; break;
+        case 6: v.fn = turn_kernel<6, false, false, false>; break;
+        case 8: v.fn = fast ? turn_kernel<8, true, false, false> : prof ? turn_kernel<8, false, true, false>
+                     : local ? turn_kernel<8, false, false, true> : turn_kernel<8, false, false, false>; break;
         default: return fail("reg_cap_blocks / narrow_reg_cap must be 0, 5, 6 or 8");
       }
       CK(cudaFuncSetAttribute(v.fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
@@ -1177,6 +1221,11 @@ class Runtime {
     // Page lists + counts + positions + offsets, for both spaces.
     CK(cudaMalloc(&mem_cur, 2ull * nthreads_max * (max_pages + 3) * sizeof(uint32_t)));
     CK(cudaMalloc((void**)&ctl, sizeof(Ctl)));
+    d.ovf = nullptr;
+    if (cfg.local_nets) {
+      CK(cudaMalloc((void**)&mem_ovf, (size_t)nthreads_max * OVF_CAP * sizeof(Pair)));
+      d.ovf = (Pair*)mem_ovf;
+    }
     {
       // One free-page ring per space, as large as the space's page count.
       uint64_t np = n_nodes >> d.nspace.page_log2, vp = n_vars >> d.vspace.page_log2;
@@ -1240,7 +1289,9 @@ class Runtime {
       const uint32_t hn = std::max<uint32_t>(1u, (uint32_t)(hn_words >> d.nspace.page_log2));
       const uint32_t hv = std::max<uint32_t>(1u, (uint32_t)(hv_words >> d.vspace.page_log2));
       const uint32_t nfull = (uint32_t)((1ull << cfg.node_log2) >> d.nspace.page_log2);
-      if (nfull <= nthreads_max + hn || d.vpool_end <= nthreads_max + hv) return fail("node/var space too small for the thread count");
+      if (nfull <= nthreads_max + hn + reserved_pages(d.nspace.page_log2) ||
+          d.vpool_end <= nthreads_max + hv + reserved_pages(d.vspace.page_log2))
+        return fail("node/var space too small for the thread count");
       d.npool_end = nfull - hn;
       d.vpool_end -= hv;
       host_lo[0] = d.npool_end << d.nspace.page_log2;
@@ -2362,6 +2413,7 @@ extern "C" void hvm_gb300_default_config(hvm_gb300_config* c) {
   c->narrow_reg_cap = 0;
   c->rule_select = 1;
   c->fast_calls = 0;
+  c->local_nets = 0;
 }
 
 extern "C" int hvm_gb300_create(const hvm_gb300_config* cfg, hvm_gb300_runtime** out) {
@@ -2672,7 +2724,7 @@ static int normalize(Ctx& x) {
   unsigned long long last_itrs = ~0ull, last_pending = ~0ull;
   uint64_t stalled = 0, turns = 0;
   for (;;) {
-    for (uint32_t i = 0; i < batch; i++) turn_kernel<8, false, false><<<BLOCKS, THREADS, (size_t)THREADS * CAP * sizeof(Pair)>>>(x.d, CAP);
+    for (uint32_t i = 0; i < batch; i++) turn_kernel<8, false, false, false><<<BLOCKS, THREADS, (size_t)THREADS * CAP * sizeof(Pair)>>>(x.d, CAP);
     if (cuda_ok(x, cudaGetLastError()) || read_ctl(x, h)) return -1;
     turns += batch;
     if (h.status) return failf(x, status_text(h.status), h.err_info);

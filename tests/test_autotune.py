@@ -16,11 +16,10 @@ def test_candidates_cover_the_space():
     assert {tuple(sorted(c.items())) for c in cands} == {
         tuple(sorted({"reg_cap_blocks": r, "graph_turns": g, "policy": p}.items()))
         for r in (5, 8) for g in (0, 4) for p in ("fixed", "learned")}
-    # The default space, less the fast-path candidates at register cap 5
-    # (the fast-path kernel variants exist for caps 0 and 8 only).
+    # The default space (the fast-path kernel variants exist for every cap it holds).
     default = at.candidates()
-    assert len(default) == 3 * 2 * 2 * 2 - 2 * 2
-    assert not any(c["fast_calls"] and c["reg_cap_blocks"] == 5 for c in default)
+    assert len(default) == 3 * 2 * 2 * 2
+    assert not at.candidates({"reg_cap_blocks": (6,), "fast_calls": (1,)})
 
 
 @pytest.mark.gpu

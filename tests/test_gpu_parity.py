@@ -81,12 +81,15 @@ def test_kernel_variant_switching(hvm, workloads, config_goldens, cfg):
 
 
 @pytest.mark.parametrize("cfg", [dict(fast_calls=1), dict(fast_calls=2), dict(fast_calls=2, rule_select=0),
-                                 dict(fast_calls=1, reg_cap_blocks=0), dict(rule_select=2)],
-                         ids=["fast_switch", "fast_switch_anni", "fast_all_lanes", "fast_uncapped", "rule_per_round"])
+                                 dict(fast_calls=1, reg_cap_blocks=0), dict(rule_select=2), dict(local_nets=1),
+                                 dict(local_nets=1, reg_cap_blocks=0, narrow_below=0)],
+                         ids=["fast_switch", "fast_switch_anni", "fast_all_lanes", "fast_uncapped", "rule_per_round",
+                              "local_nets", "local_nets_uncapped"])
 def test_scheduling_options(hvm, workloads, config_goldens, ref_programs, cfg):
     # CALL-time fast paths (the reference's compiled-mode short-cuts, adding
-    # by hand the interactions they perform) and the per-round rule
-    # selection change how the net is reduced, never the normal form or the
+    # by hand the interactions they perform), the per-round rule selection
+    # and the block-local nets (fresh words in shared memory, LEAK to HBM)
+    # change how the net is reduced, never the normal form or the
     # interaction count.
     cases = {"tree_sum_d12": workloads.tree_sum(12), "bitonic_sort_2p12": workloads.bitonic_sort(12),
              "skewed_fold_2p10": workloads.skewed_fold(10), "countdown_100000": workloads.countdown(100000)}
