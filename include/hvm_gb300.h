@@ -307,6 +307,40 @@ void hvm_gb300_reset_counters(hvm_gb300_runtime* rt);
 int hvm_gb300_run_noalloc(const uint32_t* book_buffer, size_t words, uint32_t* out_ports, uint32_t* out_kids,
                           size_t out_cap, size_t* out_len, uint64_t* out_itrs, char* err, size_t err_cap);
 
+/* ---- DL_CALL libraries -----------------------------------------------------------
+ *
+ * An IO program's DL_CALL (handle, symbol, argument) calls `symbol` from a
+ * library DL_OPEN loaded as `hvm_gb300_dl_fn` with the net and the argument
+ * port, and wraps the port it returns in Ok: the signature of the reference's
+ * run-cu, `Port (*)(GNet*, Port)` (src/run.cu:795-813). Ports are the
+ * reference's 32-bit words (tag in the low 3 bits). Inside such a call the
+ * library reads and extends the device net with the functions below, which
+ * replace the host-side net functions run-cu exports (src/hvm.cu:1842-1893,
+ * src/run.cu:102-285). Each returns 0, or -1 after recording the error, in
+ * which case the DL_CALL, and the run, fail with it.
+ */
+typedef struct hvm_gb300_io hvm_gb300_io;
+typedef uint32_t (*hvm_gb300_dl_fn)(hvm_gb300_io* net, uint32_t arg);
+
+/* Follows substituted vars from `port` and normalises a REF met there
+ * (gnet_expand, src/hvm.cu:1871-1882). */
+int hvm_gb300_io_expand(hvm_gb300_io* net, uint32_t port, uint32_t* out);
+/* The two ports of the node a CON/DUP/OPR/SWI port points to
+ * (gnet_node_load, src/hvm.cu:1842-1846). */
+int hvm_gb300_io_node_load(hvm_gb300_io* net, uint32_t port, uint32_t* fst, uint32_t* snd);
+/* Places a new node (fst, snd) in the net; `*out` = a `tag` port to it
+ * (gnet_make_node, src/hvm.cu:1885-1893). */
+int hvm_gb300_io_make_node(hvm_gb300_io* net, uint32_t tag, uint32_t fst, uint32_t snd, uint32_t* out);
+/* Reads a right-nested tuple of at most `size` elements into `elems`
+ * (gnet_readback_tup, src/run.cu:102-117). */
+int hvm_gb300_io_readback_tup(hvm_gb300_io* net, uint32_t port, uint32_t size, uint32_t* elems, uint32_t* n);
+/* Reads a lambda-encoded list of bytes; `out == NULL` queries the length
+ * (gnet_readback_bytes, src/run.cu:124-163). */
+int hvm_gb300_io_readback_bytes(hvm_gb300_io* net, uint32_t port, uint8_t* out, size_t cap, size_t* len);
+/* Places a lambda-encoded list of bytes in the net (gnet_inject_bytes,
+ * src/run.cu:267-285). */
+int hvm_gb300_io_inject_bytes(hvm_gb300_io* net, const uint8_t* bytes, size_t len, uint32_t* out);
+
 /* Last error message of `rt` ("" if none). */
 const char* hvm_gb300_error(const hvm_gb300_runtime* rt);
 

@@ -2107,6 +2107,7 @@ class Runtime {
   }
   static FILE** io_files() { static FILE* files[256]; return files; }
   static void** io_dylibs() { static void* libs[256]; return libs; }
+  bool io_failed = false;  // set by an hvm_gb300_io_* call that failed inside a DL_CALL
 
   // One IO function call (src/run.c:430-770); `ret` receives its result.
   int io_call(const std::string& name, Port argm, Port& ret) {
@@ -2217,9 +2218,25 @@ class Runtime {
       return inject_ok(new_port(ERA, 0), ret);
     }
     if (name == "DL_CALL") {
-      // The reference hands the library its own CPU net structures
-      // (src/run.c:716-739); a device-resident net has no such ABI.
-      return inject_io_err_str("DL_CALL is not available with the GPU runtime", ret);
+      // (handle, symbol, argument) (src/run.cu:795-813): the symbol is called
+      // as `Port fn(net, arg)` with this runtime as the net handle (the
+      // hvm_gb300_io_* functions read and extend the device net); the port it
+      // returns is wrapped in Ok.
+      if (read_tup(argm, 3, tup)) return -1;
+      if (tup.size() != 3) return inject_io_err(IO_ERR_TYPE_TAG, 0, ret);
+      if (get_tag(tup[0]) != NUM || get_u24(get_val(tup[0])) >= 256 || !io_dylibs()[get_u24(get_val(tup[0]))])
+        return inject_io_err(IO_ERR_TYPE_TAG, 0, ret);
+      std::string sym;
+      if (read_bytes(tup[1], sym)) return -1;
+      dlerror();
+      void* f = dlsym(io_dylibs()[get_u24(get_val(tup[0]))], sym.c_str());
+      const char* e = dlerror();
+      if (e) return inject_io_err_str(e, ret);
+      if (!f) return inject_io_err_str("symbol resolves to NULL", ret);
+      io_failed = false;
+      const Port r = reinterpret_cast<hvm_gb300_dl_fn>(f)(reinterpret_cast<hvm_gb300_io*>(this), tup[2]);
+      if (io_failed) return -1;
+      return inject_ok(r, ret);
     }
     return inject_io_err(IO_ERR_NAME_TAG, 0, ret);
   }
@@ -2571,6 +2588,96 @@ extern "C" int hvm_gb300_result(hvm_gb300_runtime* r, char* out, size_t cap, siz
     memcpy(out, s.data(), s.size());
     out[s.size()] = 0;
   }
+  return 0;
+}
+
+// ---- Net access for DL_CALL libraries ------------------------------------------------
+// The host-side net functions the reference's run-cu exports to the libraries
+// a DL_CALL names (src/hvm.cu:1842-1893, src/run.cu:102-285), over the device
+// net of the runtime running the IO loop. A failure records the error, makes
+// the DL_CALL fail and returns -1.
+
+namespace hvm_io {
+using namespace hvm;
+
+static hvm::Runtime& io_rt(hvm_gb300_io* io) { return *reinterpret_cast<hvm::Runtime*>(io); }
+static int io_fail(hvm::Runtime& rt, const char* msg) {
+  if (msg) rt.fail(msg);
+  rt.io_failed = true;
+  return -1;
+}
+}  // namespace hvm_io
+using hvm_io::io_rt;
+using hvm_io::io_fail;
+
+extern "C" int hvm_gb300_io_expand(hvm_gb300_io* io, uint32_t port, uint32_t* out) {
+  using namespace hvm;
+  if (!io || !out) return -1;
+  hvm::Runtime& rt = io_rt(io);
+  Port p;
+  if (rt.expand(port, &p)) return io_fail(rt, nullptr);
+  *out = p;
+  return 0;
+}
+
+extern "C" int hvm_gb300_io_node_load(hvm_gb300_io* io, uint32_t port, uint32_t* fst, uint32_t* snd) {
+  using namespace hvm;
+  if (!io || !fst || !snd) return -1;
+  hvm::Runtime& rt = io_rt(io);
+  const uint32_t tag = get_tag(port);
+  if (tag < CON || get_val(port) > rt.d.node_mask) return io_fail(rt, "hvm_gb300_io_node_load: not a node port");
+  const Pair n = rt.node_load(get_val(port));
+  *fst = get_fst(n);
+  *snd = get_snd(n);
+  return 0;
+}
+
+extern "C" int hvm_gb300_io_make_node(hvm_gb300_io* io, uint32_t tag, uint32_t fst, uint32_t snd, uint32_t* out) {
+  using namespace hvm;
+  if (!io || !out) return -1;
+  hvm::Runtime& rt = io_rt(io);
+  if (tag < CON || tag > SWI) return io_fail(rt, "hvm_gb300_io_make_node: not a node tag");
+  hvm::Runtime::Inject in;
+  const hvm::Runtime::LPort n = in.node(hvm::Runtime::ext(fst), hvm::Runtime::ext(snd));
+  Port p;
+  if (rt.commit(in, n, p)) return io_fail(rt, nullptr);
+  *out = new_port(tag, get_val(p));
+  return 0;
+}
+
+extern "C" int hvm_gb300_io_readback_tup(hvm_gb300_io* io, uint32_t port, uint32_t size, uint32_t* elems,
+                                         uint32_t* n) {
+  using namespace hvm;
+  if (!io || !elems || !n || size == 0) return -1;
+  hvm::Runtime& rt = io_rt(io);
+  std::vector<Port> tup;
+  if (rt.read_tup(port, size, tup)) return io_fail(rt, nullptr);
+  for (size_t i = 0; i < tup.size(); i++) elems[i] = tup[i];
+  *n = (uint32_t)tup.size();
+  return 0;
+}
+
+extern "C" int hvm_gb300_io_readback_bytes(hvm_gb300_io* io, uint32_t port, uint8_t* out, size_t cap, size_t* len) {
+  using namespace hvm;
+  if (!io || !len) return -1;
+  hvm::Runtime& rt = io_rt(io);
+  std::string b;
+  if (rt.read_bytes(port, b)) return io_fail(rt, nullptr);
+  *len = b.size();
+  if (out) {
+    if (cap < b.size()) return io_fail(rt, "hvm_gb300_io_readback_bytes: buffer too small");
+    memcpy(out, b.data(), b.size());
+  }
+  return 0;
+}
+
+extern "C" int hvm_gb300_io_inject_bytes(hvm_gb300_io* io, const uint8_t* bytes, size_t len, uint32_t* out) {
+  using namespace hvm;
+  if (!io || !out || (len && !bytes)) return -1;
+  hvm::Runtime& rt = io_rt(io);
+  Port p;
+  if (rt.inject_bytes(std::string((const char*)bytes, len), p)) return io_fail(rt, nullptr);
+  *out = p;
   return 0;
 }
 

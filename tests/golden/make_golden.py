@@ -18,7 +18,10 @@ reference sources exist; the fixtures travel, the reference does not).
                            in a scratch directory holding the files they
                            open, with the test harness's stdin
                            (tests/run.rs:79-96): printed lines, `Result:`,
-                           `- ITRS:`, and the snapshot's text.
+                           `- ITRS:`, and the snapshot's text; under "dl",
+                           DL_CALL programs calling the test library
+                           dl_test.c (the reference binary runs each
+                           function's C-runtime twin).
   configs.json             the same two fields for the seeded benchmark
                            workloads (lambdavm-rust_gb300/workloads.py), with
                            large results stored as a SHA-256 of their
@@ -26,7 +29,7 @@ reference sources exist; the fixtures travel, the reference does not).
                            evaluation counted by the oracle (-w), the
                            roofline numerator.
 
-Usage: python tests/golden/make_golden.py [--reference /root/reference] [--only-io | --only-batch]
+Usage: python tests/golden/make_golden.py [--reference /root/reference] [--only-io | --only-dl | --only-batch]
 """
 from __future__ import annotations
 
@@ -118,12 +121,14 @@ BIG_READ = ("@call ~ (d ((e 47) f))", "@call ~ (d ((e 20000) f))")
 IO_STDIN = "io from the tests\n"
 
 
-def run_ref_io(code: str) -> dict:
+def run_ref_io(code: str, dl_lib: str | None = None) -> dict:
     buf = H.book_from_text(code)
     with tempfile.TemporaryDirectory() as cwd:
         for name, text in IO_FILES.items():
             with open(os.path.join(cwd, name), "w") as f:
                 f.write(text)
+        if dl_lib:
+            build_dl_lib(os.path.join(cwd, dl_lib))
         path = os.path.join(cwd, "book.bin")
         buf.tofile(path)
         r = subprocess.run([REF_BIN, path], capture_output=True, text=True, timeout=600, cwd=cwd, input=IO_STDIN)
@@ -155,6 +160,79 @@ def make_io(ref: str) -> None:
             print(entry["name"], entry["itrs"], len(entry["printed"]))
     with open(os.path.join(HERE, "io_programs.json"), "w") as f:
         json.dump({"files": IO_FILES, "stdin": IO_STDIN, "programs": out}, f, indent=1)
+
+
+# DL_CALL programs: DL_OPEN the test library (dl_test.c), DL_CALL one of its
+# functions on an argument and return the result. The program around the
+# calls is the IO prelude of tests/programs/io/open1.hvm (IO/bind, call, the
+# String constructors); each symbol has a C-runtime twin (`*_c`) of the same
+# length that the reference binary calls, the `*_g` one is the GPU runtime's.
+DL_LIB = "libdltest.so"
+DL_CASES = [("inc", 41), ("greet", "abc"), ("nosuch", 0)]  # nosuch: no such symbol in either runtime
+
+
+def build_dl_lib(out: str) -> None:
+    subprocess.run(["gcc", "-O2", "-shared", "-fPIC", "-I", os.path.join(ROOT, "include"),
+                    os.path.join(HERE, "dl_test.c"), "-o", out], check=True)
+
+
+def hvm_string(name: str, text: str) -> str:
+    if not text:
+        return f"@{name} = @String/Nil\n"
+    lines = [f"@{name} = k0"]
+    for i, ch in enumerate(text):
+        tail = f"k{i + 1}" if i + 1 < len(text) else "@String/Nil"
+        lines.append(f"  & @String/Cons ~ ({ord(ch)} ({tail} k{i}))")
+    return "\n".join(lines) + "\n"
+
+
+def dl_program(prelude: str, symbol: str, arg) -> str:
+    arg_port = str(arg) if isinstance(arg, int) else "@s_arg"
+    code = prelude.rstrip() + "\n\n"
+    code += "@unwrap = (((* (a a)) b) b)\n\n"
+    code += ("@main = s\n  & @IO/bind ~ (o ((((p p) (@dl_step r)) r) s))\n"
+             "  & @call ~ (@s_open ((@s_path 0) o))\n\n")
+    code += ("@dl_step = (r s)\n  & @unwrap ~ (r h)\n"
+             "  & @IO/bind ~ (o ((((p p) (@IO/wrap q)) q) s))\n"
+             f"  & @call ~ (@s_call ((h (@s_sym {arg_port})) o))\n\n")
+    code += hvm_string("s_open", "DL_OPEN") + hvm_string("s_path", "./" + DL_LIB)
+    code += hvm_string("s_call", "DL_CALL") + hvm_string("s_sym", symbol)
+    if not isinstance(arg, int):
+        code += hvm_string("s_arg", arg)
+    return code
+
+
+def io_prelude(ref: str) -> str:
+    text = open(os.path.join(ref, "tests", "programs", "io", "open1.hvm")).read()
+    defs = re.split(r"\n(?=@)", text)
+    return "\n".join(d.rstrip() + "\n" for d in defs
+                     if not d.startswith("@main ") and not d.startswith("@test-io "))
+
+
+def make_dl(ref: str) -> None:
+    path = os.path.join(HERE, "io_programs.json")
+    data = json.load(open(path))
+    prelude = io_prelude(ref)
+    out = []
+    for fn, arg in DL_CASES:
+        sym_c, sym_g = (fn + "_x", fn + "_x") if fn == "nosuch" else (fn + "_c", fn + "_g")
+        code_c = dl_program(prelude, sym_c, arg)
+        entry = {"name": f"dl_call {fn}", "code": dl_program(prelude, sym_g, arg), **run_ref_io(code_c, DL_LIB)}
+        out.append(entry)
+        print(entry["name"], entry["itrs"], entry["result"][:80])
+    # pair_g has no C twin: its known answer is the inc program's with the Ok
+    # payload 42 replaced by the pair (41 42); the payload is never reduced,
+    # so the interaction count is the same.
+    inc = out[0]
+    pair = {"name": "dl_call pair (known answer)", "code": dl_program(prelude, "pair_g", 41),
+            "printed": inc["printed"], "result": inc["result"].replace("(((0 (42 ", "(((0 ((41 42) ", 1),
+            "itrs": inc["itrs"]}
+    assert pair["result"] != inc["result"]
+    out.append(pair)
+    data["dl_lib"] = DL_LIB
+    data["dl"] = out
+    with open(path, "w") as f:
+        json.dump(data, f, indent=1)
 
 
 def _batch_entry(item):
@@ -191,6 +269,7 @@ def main() -> None:
     ap.add_argument("--only-batch", action="store_true")
     ap.add_argument("--only-io", action="store_true")
     ap.add_argument("--only-counts", action="store_true")
+    ap.add_argument("--only-dl", action="store_true")
     args = ap.parse_args()
     if args.only_counts:
         subprocess.run(["make", "-C", os.path.join(ROOT, "oracle")], check=True)
@@ -199,11 +278,15 @@ def main() -> None:
     if args.only_batch:
         make_batch()
         return
+    if args.only_dl:
+        subprocess.run(["make", "-C", os.path.join(ROOT, "oracle"), "stage", "ref", f"REF_ROOT={args.reference}"], check=True)
+        make_dl(args.reference)
+        return
     if args.only_io:
-        subprocess.run(["make", "-C", os.path.join(ROOT, "oracle"), "ref", f"REF_SRC={args.reference}/src"], check=True)
+        subprocess.run(["make", "-C", os.path.join(ROOT, "oracle"), "stage", "ref", f"REF_ROOT={args.reference}"], check=True)
         make_io(args.reference)
         return
-    subprocess.run(["make", "-C", os.path.join(ROOT, "oracle"), "ref", f"REF_SRC={args.reference}/src"], check=True)
+    subprocess.run(["make", "-C", os.path.join(ROOT, "oracle"), "stage", "ref", f"REF_ROOT={args.reference}"], check=True)
     subprocess.run(["make", "-C", os.path.join(ROOT, "oracle")], check=True)
 
     progs = []
