@@ -126,6 +126,12 @@ EXPORTED_SYMBOLS = (
     "hvm_gb300_policy_grad",
     "hvm_gb300_policy_train",
     "hvm_gb300_atomic_peak",
+    "hvm_gb300_io_expand",
+    "hvm_gb300_io_node_load",
+    "hvm_gb300_io_make_node",
+    "hvm_gb300_io_readback_tup",
+    "hvm_gb300_io_readback_bytes",
+    "hvm_gb300_io_inject_bytes",
     "hvm_gb300_error",
     "hvm_gb300_destroy",
 )
