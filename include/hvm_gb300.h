@@ -114,6 +114,9 @@ typedef struct {
                                  src/hvm.cu:130-135, 1129-1174): fresh words of a turn in the block's
                                  shared memory, copied out to HBM when a global var would point at
                                  them and at the turn's end; 128-thread blocks, register caps 0/8 */
+  uint32_t persistent;        /* 1 = a normalisation runs its turns inside cooperative launches of up
+                                 to 4096 turns each, closed on the device (register caps 0 and 8, no
+                                 fast_calls/profile/local_nets); 0 = one launch per turn */
 } hvm_gb300_config;
 
 typedef struct {
@@ -335,11 +338,20 @@ int hvm_gb300_io_make_node(hvm_gb300_io* net, uint32_t tag, uint32_t fst, uint32
  * (gnet_readback_tup, src/run.cu:102-117). */
 int hvm_gb300_io_readback_tup(hvm_gb300_io* net, uint32_t port, uint32_t size, uint32_t* elems, uint32_t* n);
 /* Reads a lambda-encoded list of bytes; `out == NULL` queries the length
- * (gnet_readback_bytes, src/run.cu:124-163). */
+ * (gnet_readback_bytes, src/run.cu:124-163). Reading evaluates the list; a
+ * length query followed by the read of the same port, with no other net
+ * function between them, evaluates it once. */
 int hvm_gb300_io_readback_bytes(hvm_gb300_io* net, uint32_t port, uint8_t* out, size_t cap, size_t* len);
 /* Places a lambda-encoded list of bytes in the net (gnet_inject_bytes,
  * src/run.cu:267-285). */
 int hvm_gb300_io_inject_bytes(hvm_gb300_io* net, const uint8_t* bytes, size_t len, uint32_t* out);
+
+/* Self-test of the bounded wait that persistent launches use between turns
+ * (a block waiting for the turn's closing block): one GPU thread waits on a
+ * word that nothing writes, with a limit of `limit_ms` (1..10000) of the
+ * global timer. `*timed_out` = 1 once the limit ran out (the expected answer)
+ * and `*waited_ms` the time it waited. Returns 0, or -1 on a CUDA error. */
+int hvm_gb300_wait_probe(int32_t device, uint32_t limit_ms, uint32_t* timed_out, double* waited_ms);
 
 /* Last error message of `rt` ("" if none). */
 const char* hvm_gb300_error(const hvm_gb300_runtime* rt);

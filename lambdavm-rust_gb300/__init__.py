@@ -54,6 +54,7 @@ class Config(ctypes.Structure):
         ("rule_select", ctypes.c_uint32),
         ("fast_calls", ctypes.c_uint32),
         ("local_nets", ctypes.c_uint32),
+        ("persistent", ctypes.c_uint32),
     ]
 
 
@@ -132,6 +133,7 @@ EXPORTED_SYMBOLS = (
     "hvm_gb300_io_readback_tup",
     "hvm_gb300_io_readback_bytes",
     "hvm_gb300_io_inject_bytes",
+    "hvm_gb300_wait_probe",
     "hvm_gb300_error",
     "hvm_gb300_destroy",
 )
@@ -156,6 +158,7 @@ def lib() -> ctypes.CDLL:
     L.hvm_gb300_compile_calls.argtypes = [u32p, ctypes.c_size_t, ctypes.c_char_p, ctypes.c_size_t,
                                           ctypes.POINTER(ctypes.c_size_t), ctypes.c_char_p, ctypes.c_size_t]
     L.hvm_gb300_default_config.argtypes = [ctypes.POINTER(Config)]
+    L.hvm_gb300_wait_probe.argtypes = [ctypes.c_int32, ctypes.c_uint32, u32p, ctypes.POINTER(ctypes.c_double)]
     L.hvm_gb300_default_config.restype = None
     L.hvm_gb300_create.argtypes = [ctypes.POINTER(Config), ctypes.POINTER(ctypes.c_void_p)]
     L.hvm_gb300_load_book.argtypes = [ctypes.c_void_p, u32p, ctypes.c_size_t]
@@ -495,6 +498,16 @@ def atomic_peak(region_words: int = 1 << 24, device: int = 0) -> float:
     if lib().hvm_gb300_atomic_peak(device, region_words, ctypes.byref(v), err, 512):
         raise HvmError(err.value.decode())
     return v.value
+
+
+def wait_probe(limit_ms: int = 100, device: int = 0) -> tuple[bool, float]:
+    """Runs the persistent launches' bounded wait on a word nothing writes:
+    (whether the limit ran out, milliseconds waited)."""
+    out = ctypes.c_uint32()
+    ms = ctypes.c_double()
+    if lib().hvm_gb300_wait_probe(device, limit_ms, ctypes.byref(out), ctypes.byref(ms)):
+        raise HvmError("wait probe failed")
+    return bool(out.value), ms.value
 
 
 def run_text(code: str, device: int = 0, **cfg) -> tuple[str, RunStats]:

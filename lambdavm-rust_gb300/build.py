@@ -20,6 +20,9 @@ CSRC = os.path.join(PKG, "csrc")
 INCLUDE = os.path.join(ROOT, "include")
 BUILD = os.path.join(PKG, "_build")
 LIB = os.path.join(PKG, "libhvm_gb300.so")
+# The same runtime over 64-bit ports (HVM_PORT64: 128-bit node pairs, spaces
+# of up to 2^32 words); the front-end and the MLP kernels are shared objects.
+LIB64 = os.path.join(PKG, "libhvm_gb300_p64.so")
 CLI = os.path.join(PKG, "hvm")
 
 NVCC = os.environ.get("NVCC", "nvcc")
@@ -47,14 +50,15 @@ def _headers() -> list[str]:
     return hs + [os.path.join(INCLUDE, f) for f in os.listdir(INCLUDE) if f.endswith(".h")]
 
 
-def _compile(src: str) -> str:
+def _compile(src: str, port64: bool = False) -> str:
     path = os.path.join(CSRC, src)
-    obj = os.path.join(BUILD, src + ".o")
+    obj = os.path.join(BUILD, src + (".p64.o" if port64 else ".o"))
+    defs = ["-DHVM_PORT64"] if port64 else []
     if _stale(obj, [path] + _headers()):
         if src.endswith(".cu"):
-            _run([NVCC, *ARCH, "-lineinfo", *CXXFLAGS, "-Xcompiler", "-fPIC", "-c", path, "-o", obj])
+            _run([NVCC, *ARCH, "-lineinfo", *CXXFLAGS, *defs, "-Xcompiler", "-fPIC", "-c", path, "-o", obj])
         else:
-            _run([NVCC, *CXXFLAGS, "-Xcompiler", "-fPIC", "-c", path, "-o", obj])
+            _run([NVCC, *CXXFLAGS, *defs, "-Xcompiler", "-fPIC", "-c", path, "-o", obj])
     return obj
 
 
@@ -108,10 +112,16 @@ def build(verbose: bool = False) -> str:
     """Compiles the library and the CLI if any source changed; returns the library path."""
     os.makedirs(BUILD, exist_ok=True)
     _write_standalone()
-    with ThreadPoolExecutor(max_workers=max(2, len(LIB_SOURCES))) as ex:
-        objs = list(ex.map(_compile, LIB_SOURCES))
+    with ThreadPoolExecutor(max_workers=max(2, len(LIB_SOURCES) + 1)) as ex:
+        jobs = [ex.submit(_compile, src) for src in LIB_SOURCES]
+        job64 = ex.submit(_compile, "runtime.cu", True)
+        objs = [j.result() for j in jobs]
+        obj64 = job64.result()
     if _stale(LIB, objs):
         _run([NVCC, *ARCH, "-shared", "-o", LIB, *objs, "-lcudart"])
+    objs64 = [obj64 if o.endswith("runtime.cu.o") else o for o in objs]
+    if _stale(LIB64, objs64):
+        _run([NVCC, *ARCH, "-shared", "-o", LIB64, *objs64, "-lcudart"])
     cli_src = os.path.join(CSRC, "hvm_cli.cpp")
     if os.path.exists(cli_src) and _stale(CLI, [cli_src, LIB, STANDALONE_INC] + _headers()):
         _run([NVCC, *CXXFLAGS, "-I" + BUILD, "-o", CLI, cli_src, "-L" + PKG, "-lhvm_gb300",

@@ -21,7 +21,7 @@
 #include <stdint.h>
 #include "hvm_defs.h"
 
-namespace hvm {
+HVM_NS_BEGIN
 
 // Device status codes (0 = running / ok). Written once, first error wins.
 enum : uint32_t {
@@ -33,6 +33,7 @@ enum : uint32_t {
   ST_LINK_LIMIT = 5,    // a substitution chain exceeded the iteration bound
   ST_BAD_REF = 6,       // a REF to a definition the book does not have
   ST_DRAIN = 7,         // a turn's end could not make its local net global within the bound
+  ST_WAIT = 8,          // persistent launch: a block waited too long for a turn to close
 };
 
 // One book definition on the device. Pairs for a def are stored at
@@ -123,9 +124,15 @@ struct alignas(128) Ctl {
   TurnRecord* trace;                // per-turn records (null = off)
   unsigned int trace_cap;
   unsigned int policy_script_len;   // POLICY_SCRIPT: turns the script covers
+  // Persistent launches: the block that closes a turn writes `go` (whether
+  // the launch runs another turn) and then raises `epoch`, which the other
+  // blocks wait on.
+  unsigned int epoch;
+  unsigned int go;
+  unsigned int persist_ran;         // turns the last persistent launch closed
 };
 
-constexpr Pair NODE_MARK = ~0ull;
+constexpr Pair NODE_MARK = ~(Pair)0;
 
 // Node and var indices below LOCAL_WORDS name a block's local net (shared
 // memory) in the local-net kernel variant; the global allocator never hands
@@ -178,15 +185,51 @@ struct Dev {
 
 // ---- memory access -----------------------------------------------------------
 
+#ifdef HVM_PORT64
+// 128-bit node words: one 16-byte access each (a node is seen whole or not
+// at all, as the 64-bit words of the 32-bit build are), at gpu scope so that
+// no stale L1 line is read. Node indices are masked like var indices.
+__device__ __forceinline__ Pair ld_pair(const Pair* p) {
+  unsigned long long lo, hi;
+  asm volatile("{\n .reg .b128 d;\n ld.relaxed.gpu.global.b128 d, [%2];\n mov.b128 {%0, %1}, d;\n}"
+               : "=l"(lo), "=l"(hi) : "l"(p) : "memory");
+  return ((Pair)hi << 64) | lo;
+}
+__device__ __forceinline__ void st_pair(Pair* p, Pair v) {
+  asm volatile("{\n .reg .b128 s;\n mov.b128 s, {%1, %2};\n st.relaxed.gpu.global.b128 [%0], s;\n}"
+               :: "l"(p), "l"((unsigned long long)v), "l"((unsigned long long)(v >> 64)) : "memory");
+}
+__device__ __forceinline__ Pair nload(const Dev& d, uint32_t i) { return ld_pair(&d.node[i & d.node_mask]); }
+__device__ __forceinline__ void nstore(const Dev& d, uint32_t i, Pair p) { st_pair(&d.node[i & d.node_mask], p); }
+// Read-only words (the book): two 64-bit loads through the read-only cache.
+__device__ __forceinline__ Pair book_pair(const Pair* p) {
+  const unsigned long long* q = (const unsigned long long*)p;
+  return ((Pair)__ldg(q + 1) << 64) | __ldg(q);
+}
+// A redex of the ring, written in an earlier turn.
+__device__ __forceinline__ Pair ring_pair(const Pair* p) { return ld_pair(p); }
+__device__ __forceinline__ Port vload(const Dev& d, uint32_t i) {
+  return (Port)__ldcg((const unsigned long long*)&d.vars[i & d.vars_mask]);
+}
+__device__ __forceinline__ void vstore(const Dev& d, uint32_t i, Port p) {
+  __stcg((unsigned long long*)&d.vars[i & d.vars_mask], (unsigned long long)p);
+}
+__device__ __forceinline__ Port vexch(const Dev& d, uint32_t i, Port p) {
+  return (Port)atomicExch((unsigned long long*)&d.vars[i & d.vars_mask], (unsigned long long)p);
+}
+#else
 __device__ __forceinline__ Pair nload(const Dev& d, uint32_t i) {
   return (Pair)__ldcg((const unsigned long long*)&d.node[i]);
 }
 __device__ __forceinline__ void nstore(const Dev& d, uint32_t i, Pair p) {
   __stcg((unsigned long long*)&d.node[i], (unsigned long long)p);
 }
+__device__ __forceinline__ Pair book_pair(const Pair* p) { return (Pair)__ldg((const unsigned long long*)p); }
+__device__ __forceinline__ Pair ring_pair(const Pair* p) { return (Pair)__ldcg((const unsigned long long*)p); }
 __device__ __forceinline__ Port vload(const Dev& d, uint32_t i) { return __ldcg(&d.vars[i & d.vars_mask]); }
 __device__ __forceinline__ void vstore(const Dev& d, uint32_t i, Port p) { __stcg(&d.vars[i & d.vars_mask], p); }
 __device__ __forceinline__ Port vexch(const Dev& d, uint32_t i, Port p) { return atomicExch(&d.vars[i & d.vars_mask], p); }
+#endif
 
 __device__ __forceinline__ void set_status(const Dev& d, uint32_t code, uint32_t info) {
   if (atomicCAS(&d.ctl->status, 0u, code) == 0u) d.ctl->err_info = info;
@@ -272,7 +315,13 @@ __device__ __forceinline__ void v_store(const Dev& d, const TState& t, uint32_t 
 }
 template <bool LOCAL>
 __device__ __forceinline__ Port v_exch(const Dev& d, const TState& t, uint32_t i, Port p) {
-  if (LOCAL && i < LOCAL_WORDS) return atomicExch(&lvar_of(t)[i], p);
+  if (LOCAL && i < LOCAL_WORDS) {
+#ifdef HVM_PORT64
+    return (Port)atomicExch((unsigned long long*)&lvar_of(t)[i], (unsigned long long)p);
+#else
+    return atomicExch(&lvar_of(t)[i], p);
+#endif
+  }
   return vexch(d, i, p);
 }
 // Live-word accounting counts global words only (local ones end with the turn).
@@ -376,14 +425,31 @@ template <bool VARS>
 __device__ __forceinline__ uint32_t chunk_mask(const Dev& d, uint32_t base) {
   uint32_t m = 0;
   if (!VARS) {
+#ifdef HVM_PORT64
+    #pragma unroll
+    for (int k = 0; k < 16; k++) {  // two 16-byte nodes per 32-byte load
+      unsigned long long w0, w1, w2, w3;
+      ld_cg_v4(&d.node[base + 2 * k], w0, w1, w2, w3);
+      m |= ((w0 == 0 && w1 == 0) | (w2 == 0 && w3 == 0) << 1) << (2 * k);
+    }
+#else
     #pragma unroll
     for (int k = 0; k < 8; k++) {
       unsigned long long w0, w1, w2, w3;
       ld_cg_v4(&d.node[base + 4 * k], w0, w1, w2, w3);
       m |= ((w0 == 0) | (w1 == 0) << 1 | (w2 == 0) << 2 | (w3 == 0) << 3) << (4 * k);
     }
+#endif
     if (base + CHUNK > d.node_mask) m &= ~(1u << (d.node_mask - base));  // never the MARK word
   } else {
+#ifdef HVM_PORT64
+    #pragma unroll
+    for (int k = 0; k < 8; k++) {  // four 8-byte vars per 32-byte load
+      unsigned long long w0, w1, w2, w3;
+      ld_cg_v4(&d.vars[base + 4 * k], w0, w1, w2, w3);
+      m |= ((w0 == 0) | (w1 == 0) << 1 | (w2 == 0) << 2 | (w3 == 0) << 3) << (4 * k);
+    }
+#else
     #pragma unroll
     for (int k = 0; k < 4; k++) {
       unsigned long long w0, w1, w2, w3;
@@ -395,6 +461,7 @@ __device__ __forceinline__ uint32_t chunk_mask(const Dev& d, uint32_t base) {
       b8 |= ((uint32_t)w3 == 0) << 6 | ((uint32_t)(w3 >> 32) == 0) << 7;
       m |= b8 << (8 * k);
     }
+#endif
     if (base + CHUNK > d.vars_mask) m &= ~(1u << (d.vars_mask - base));  // ROOT
   }
   if (base == 0) m &= ~1u;
@@ -700,7 +767,7 @@ __device__ __forceinline__ void link_pair(const Dev& d, uint32_t gid, const Plan
       if (d.compiled && p.contig && compiled_call_link(p.fid, i, p.nbase, p.vbase, p.b, x, y)) break;
 #endif
       if (i < p.rbag_len) {
-        Pair q = __ldg((const unsigned long long*)&d.book[p.off + i]);
+        Pair q = book_pair(&d.book[p.off + i]);
         x = get_fst(q) == CALLER_PORT ? p.b : relocate(d, gid, p, get_fst(q));
         y = get_snd(q) == CALLER_PORT ? p.b : relocate(d, gid, p, get_snd(q));
       } else {
@@ -866,7 +933,7 @@ __device__ __forceinline__ int lockstep_round(const Dev& d, TState& t, bool has,
     const bool sw = fast_kind(p.fpad) == FAST_SWITCH && get_tag(get_fst(p.B)) == NUM;
     p.fast = sw ? (get_u24(get_val(get_fst(p.B))) == 0 ? 2u : 3u) : d.fast_calls >= 2 ? 1u : 0u;
     if (p.fast) {
-      const Pair q = __ldg((const unsigned long long*)&d.book[p.off + p.rbag_len + p.node_len + (sw ? 1 : 0)]);
+      const Pair q = book_pair(&d.book[p.off + p.rbag_len + p.node_len + (sw ? 1 : 0)]);
       p.f1 = get_fst(q);
       p.f2 = get_snd(q);
     }
@@ -1063,7 +1130,7 @@ __device__ __forceinline__ int lockstep_round(const Dev& d, TState& t, bool has,
             if (!p.contig) nstore(d, at, 0);  // taken (marked) one by one: give it back
             continue;
           }
-          Pair q = __ldg((const unsigned long long*)&nodes[i]);
+          Pair q = book_pair(&nodes[i]);
           n_store<LOCAL>(d, t, at, new_pair(relocate(d, t.gid, p, get_fst(q)), relocate(d, t.gid, p, get_snd(q))));
         }
         t.live_nodes -= __popc(skip);
@@ -1164,4 +1231,4 @@ __device__ __forceinline__ int lockstep_round(const Dev& d, TState& t, bool has,
   return rc;
 }
 
-}  // namespace hvm
+HVM_NS_END

@@ -18,12 +18,32 @@
 #define HVM_HD static inline
 #endif
 
-namespace hvm {
+// Port width: 32-bit ports (the reference's encoding) by default; a build
+// with HVM_PORT64 compiles the evaluator over 64-bit ports and 128-bit node
+// pairs. The two builds' symbols live in distinct inline namespaces, so that
+// one library can link 32-bit host code (the front-end) beside them.
+#ifdef HVM_PORT64
+#define HVM_NS_BEGIN namespace hvm { inline namespace p64 {
+#else
+#define HVM_NS_BEGIN namespace hvm { inline namespace p32 {
+#endif
+#define HVM_NS_END } }
+
+HVM_NS_BEGIN
 
 typedef uint8_t  Tag;
+#ifdef HVM_PORT64
+// 64-bit ports: a 61-bit val; a node is a 128-bit pair (fst in the low half).
+typedef uint64_t Val;
+typedef uint64_t Port;
+typedef unsigned __int128 Pair;
+constexpr int PORT_BITS = 64;
+#else
 typedef uint32_t Val;
 typedef uint32_t Port;
 typedef uint64_t Pair;
+constexpr int PORT_BITS = 32;
+#endif
 typedef uint32_t Numb;
 typedef uint8_t  Rule;
 
@@ -43,11 +63,20 @@ enum : uint32_t {
   FP_SHL = 0x14, OP_SHR = 0x15, FP_SHR = 0x16,
 };
 
-// Special ports (src/hvm.c:112-114). ROOT is the VAR whose index is 0x1FFFFFFF.
+// Special ports (src/hvm.c:112-114). ROOT is the VAR whose index is 0x1FFFFFFF
+// (with 64-bit ports, 0xFFFFFFFF: word indices stay 32-bit, and the ROOT var
+// is the last word of any var space either way); NONE is all ones.
+#ifdef HVM_PORT64
+constexpr Port FREE = 0;
+constexpr Val  ROOT_VAR = 0xFFFFFFFFull;
+constexpr Port ROOT = ROOT_VAR << 3;
+constexpr Port NONE = ~0ull;
+#else
 constexpr Port FREE = 0x00000000u;
 constexpr Port ROOT = 0xFFFFFFF8u;
 constexpr Port NONE = 0xFFFFFFFFu;
 constexpr Val  ROOT_VAR = 0x1FFFFFFFu;
+#endif
 
 // Book limits of the CPU runtime (src/hvm.c:135-136, 161): the GB300 runtime
 // accepts exactly what `hvm run-c` accepts, so both reject the same books.
@@ -60,9 +89,9 @@ constexpr uint32_t DEF_HEADER_WORDS = 1 + 64 + 5;
 HVM_HD Port new_port(Tag tag, Val val) { return (val << 3) | tag; }
 HVM_HD Tag  get_tag(Port p) { return (Tag)(p & 7); }
 HVM_HD Val  get_val(Port p) { return p >> 3; }
-HVM_HD Pair new_pair(Port fst, Port snd) { return ((uint64_t)snd << 32) | fst; }
-HVM_HD Port get_fst(Pair p) { return (Port)(p & 0xFFFFFFFFu); }
-HVM_HD Port get_snd(Pair p) { return (Port)(p >> 32); }
+HVM_HD Pair new_pair(Port fst, Port snd) { return ((Pair)snd << PORT_BITS) | fst; }
+HVM_HD Port get_fst(Pair p) { return (Port)p; }
+HVM_HD Port get_snd(Pair p) { return (Port)(p >> PORT_BITS); }
 HVM_HD bool is_nod(Port p) { return get_tag(p) >= CON; }
 HVM_HD bool is_var(Port p) { return get_tag(p) == VAR; }
 
@@ -265,4 +294,4 @@ HVM_HD Numb operate(Numb a, Numb b) {
   return new_u24(0);
 }
 
-}  // namespace hvm
+HVM_NS_END

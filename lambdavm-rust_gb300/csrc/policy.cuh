@@ -16,8 +16,9 @@
 // output).
 #pragma once
 #include <stdint.h>
+#include "hvm_defs.h"
 
-namespace hvm {
+HVM_NS_BEGIN
 
 constexpr int POLICY_IN = 16, POLICY_HID = 64, POLICY_OUT = 3;
 // Packed weights: W1[64][16] b1[64] W2[64][64] b2[64] W3[3][64] b3[3].
@@ -65,4 +66,4 @@ __device__ __forceinline__ void policy_infer_block(const float* __restrict__ w, 
   __syncthreads();
 }
 
-}  // namespace hvm
+HVM_NS_END

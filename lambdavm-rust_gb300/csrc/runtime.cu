@@ -38,7 +38,7 @@
 #include "policy.cuh"
 #include "hvm_gb300.h"
 
-namespace hvm {
+HVM_NS_BEGIN
 
 // Capacity of each thread's page list (pages of one space a thread may own).
 constexpr uint32_t MAX_PAGES = 64;
@@ -66,6 +66,7 @@ static const char* status_text(uint32_t s) {
     case ST_LINK_LIMIT: return "substitution chain too long";
     case ST_BAD_REF: return "reference to a missing definition";
     case ST_DRAIN: return "local net not drained at the turn's end";
+    case ST_WAIT: return "a persistent launch waited too long for a turn to close";
     default: return "unknown device error";
   }
 }
@@ -188,27 +189,44 @@ __device__ void apply_policy(Ctl* c, const float* o, unsigned long long pending,
 // per-phase clock counters (Ctl::prof) and LOCAL the block-local nets
 // (evaluator.cuh); each is kept out of the default variants because its code
 // alone costs the others registers.
-template <int MIN_BLOCKS_128, bool FAST, bool PROF, bool LOCAL>
-__global__ void __launch_bounds__(128, MIN_BLOCKS_128 > 0 ? MIN_BLOCKS_128 : 1) turn_kernel(Dev d, uint32_t cap) {
-  extern __shared__ unsigned long long smem_stack[];
+// The parameters of the turn about to run, read once per block so that every
+// thread of the block takes the same decisions. Returns whether the turn has
+// work (false: normal form reached, or a failure was recorded).
+struct TurnParams {
+  unsigned long long base, in_end;
+  uint32_t s, budget, stop_at;
+};
+__device__ __forceinline__ bool turn_begin(const Dev& d, TurnParams& tp) {
   Ctl* c = d.ctl;
-  // Turn parameters are read once per block so every thread of the block
-  // takes the same early-exit decision.
   __shared__ unsigned long long sh_base, sh_end;
-  __shared__ unsigned sh_run, sh_s, sh_budget, sh_stop_at, blk_dry;
+  __shared__ unsigned sh_run, sh_s, sh_budget, sh_stop_at;
   if (threadIdx.x == 0) {
     sh_base = ldcg64(&c->base);
     sh_end = ldcg64(&c->in_end);
-    sh_run = sh_base != sh_end && __ldcg(&c->status) == 0;  // else: normal form reached, or failed
+    sh_run = sh_base != sh_end && __ldcg(&c->status) == 0;
     sh_s = __ldcg(&c->static_per_thread);
     sh_budget = __ldcg(&c->budget);
     sh_stop_at = __ldcg(&c->stop_at);
-    blk_dry = 0;
   }
   __syncthreads();
-  if (!sh_run) return;
-  const unsigned long long base = sh_base, in_end = sh_end;
-  const uint32_t s = sh_s, budget = sh_budget, stop_at = sh_stop_at;
+  tp.base = sh_base;
+  tp.in_end = sh_end;
+  tp.s = sh_s;
+  tp.budget = sh_budget;
+  tp.stop_at = sh_stop_at;
+  const bool run = sh_run != 0;
+  __syncthreads();  // the shared words are rewritten by the next turn's call
+  return run;
+}
+
+// One turn's work for this block: static share of the input, rounds until
+// the budget or the stop flag, LIFO flush to the ring tail, counters.
+template <int MIN_BLOCKS_128, bool FAST, bool PROF, bool LOCAL>
+__device__ __forceinline__ void turn_work(const Dev& d, uint32_t cap, const TurnParams& tp) {
+  extern __shared__ unsigned long long smem_stack[];
+  Ctl* c = d.ctl;
+  const unsigned long long base = tp.base, in_end = tp.in_end;
+  const uint32_t s = tp.s, budget = tp.budget, stop_at = tp.stop_at;
 
   TState t;
   t.stk = (Pair*)smem_stack + threadIdx.x;
@@ -236,7 +254,7 @@ __global__ void __launch_bounds__(128, MIN_BLOCKS_128 > 0 ? MIN_BLOCKS_128 : 1) 
   for (uint32_t k = 0; k < s; k++) {
     unsigned long long at = base + t.gid + (unsigned long long)k * d.nthreads;
     if (at >= in_end) break;
-    push<LOCAL>(d, t, (Pair)__ldcg((const unsigned long long*)&d.ring[at & d.ring_mask]));
+    push<LOCAL>(d, t, ring_pair(&d.ring[at & d.ring_mask]));
   }
 
   const unsigned lane = threadIdx.x & 31;
@@ -282,7 +300,7 @@ __global__ void __launch_bounds__(128, MIN_BLOCKS_128 > 0 ? MIN_BLOCKS_128 : 1) 
       h = __shfl_sync(0xFFFFFFFFu, h, 0);
       unsigned k = __popc(empty & lt_mask);
       if (((empty >> lane) & 1) && h + k < in_end) {
-        push<LOCAL>(d, t, (Pair)__ldcg((const unsigned long long*)&d.ring[(h + k) & d.ring_mask]));
+        push<LOCAL>(d, t, ring_pair(&d.ring[(h + k) & d.ring_mask]));
       }
       ring_dry = h + __popc(empty) >= in_end;
     }
@@ -401,11 +419,46 @@ __global__ void __launch_bounds__(128, MIN_BLOCKS_128 > 0 ? MIN_BLOCKS_128 : 1) 
     atomicAdd(dst, blk_cnt[threadIdx.x]);
   }
 
-  // The last block to finish closes the turn and picks the next one.
+}
+
+__device__ __forceinline__ unsigned ld_acquire_u32(const unsigned* p) {
+  unsigned v;
+  asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+  return v;
+}
+__device__ __forceinline__ void st_release_u32(unsigned* p, unsigned v) {
+  asm volatile("st.release.gpu.global.u32 [%0], %1;" :: "l"(p), "r"(v) : "memory");
+}
+
+// The last block to finish closes the turn and picks the next one. In a
+// persistent launch (PERSIST) every block arrives, also one whose turn had
+// no work, and the closing block decides whether the launch goes on: turn
+// `k` of `turns`, while the pending count stays in [lo, hi) (outside it the
+// host switches kernel variants), no failure recorded and redexes left.
+template <bool PERSIST>
+__device__ __forceinline__ void turn_close(const Dev& d, uint32_t cap, const TurnParams& tp, bool ran, uint32_t k,
+                                           uint32_t turns, unsigned long long lo, unsigned long long hi) {
+  Ctl* c = d.ctl;
+  const unsigned long long in_end = tp.in_end;
   __shared__ unsigned sh_last;
   __shared__ float feat[POLICY_IN], h1[POLICY_HID], h2[POLICY_HID], outp[POLICY_OUT];
   __shared__ unsigned long long sh_pending, sh_prev, sh_nb, sh_tail;
   __syncthreads();
+  if (PERSIST && threadIdx.x == 0 && !ran) {
+    // Nothing ran in this block: arrive; the closing block (if it is this
+    // one) only lets the launch end.
+    __threadfence();
+    const unsigned prev = atomicAdd(&c->blocks_done, 1u);
+    if (prev == gridDim.x - 1) {
+      __threadfence();
+      c->go = 0;
+      c->persist_ran = k;
+      c->blocks_done = 0;
+      __threadfence();
+      st_release_u32(&c->epoch, c->epoch + 1);
+    }
+  }
+  if (PERSIST && !ran) return;
   if (threadIdx.x == 0) {
     __threadfence();
     unsigned prev = atomicAdd(&c->blocks_done, 1u);
@@ -473,6 +526,81 @@ __global__ void __launch_bounds__(128, MIN_BLOCKS_128 > 0 ? MIN_BLOCKS_128 : 1) 
     c->head = nb + (take < pending ? take : pending);
     c->blocks_done = 0;
     __threadfence();
+    if (PERSIST) {
+      c->go = c->status == 0 && pending != 0 && k + 1 < turns && pending >= lo && pending < hi;
+      c->persist_ran = k + 1;
+      __threadfence();
+      st_release_u32(&c->epoch, c->epoch + 1);
+    }
+  }
+}
+
+template <int MIN_BLOCKS_128, bool FAST, bool PROF, bool LOCAL>
+__global__ void __launch_bounds__(128, MIN_BLOCKS_128 > 0 ? MIN_BLOCKS_128 : 1) turn_kernel(Dev d, uint32_t cap) {
+  TurnParams tp;
+  if (!turn_begin(d, tp)) return;
+  turn_work<MIN_BLOCKS_128, FAST, PROF, LOCAL>(d, cap, tp);
+  turn_close<false>(d, cap, tp, true, 0, 0, 0, 0);
+}
+
+// Longest wait of a persistent launch's block for a turn to close; a turn is
+// bounded by its round budget and takes milliseconds.
+constexpr unsigned long long PERSIST_WAIT_NS = 2000000000ull;
+// Turns per persistent launch: the host polls between launches (progress
+// and turn-budget checks, kernel-variant switches).
+constexpr uint32_t PERSIST_TURNS = 4096;
+
+// Waits until *p differs from `v`, for at most `limit_ns` of the global
+// timer; returns false if the limit ran out.
+__device__ __forceinline__ bool wait_change(const unsigned* p, unsigned v, unsigned long long limit_ns) {
+  unsigned long long t0, now;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t0));
+  for (uint32_t spin = 0; ld_acquire_u32(p) == v; spin++) {
+    __nanosleep(200);
+    if ((spin & 1023) == 1023) {
+      asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(now));
+      if (now - t0 > limit_ns) return false;
+    }
+  }
+  return true;
+}
+
+// Self-test of the wait: one thread waits on a word that nothing writes and
+// reports (out[0]) whether the limit ran out and (out[1..2]) the time waited.
+__global__ void wait_probe_kernel(const unsigned* word, unsigned long long limit_ns, unsigned* out) {
+  unsigned long long t0, t1;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t0));
+  const bool changed = wait_change(word, *word, limit_ns);
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t1));
+  out[0] = changed ? 0u : 1u;
+  out[1] = (unsigned)((t1 - t0) & 0xFFFFFFFFu);
+  out[2] = (unsigned)((t1 - t0) >> 32);
+}
+
+// Persistent launch (cooperative, so every block is resident): up to `turns`
+// turns in one launch, each closed on the device as turn_kernel's are; the
+// blocks that did not close a turn wait for its epoch, with a time limit
+// after which they record ST_WAIT and return.
+template <int MIN_BLOCKS_128>
+__global__ void __launch_bounds__(128, MIN_BLOCKS_128 > 0 ? MIN_BLOCKS_128 : 1)
+    persistent_kernel(Dev d, uint32_t cap, uint32_t turns, unsigned long long lo, unsigned long long hi) {
+  Ctl* c = d.ctl;
+  __shared__ unsigned sh_go;
+  // No turn closes before every block has arrived at the first close, so
+  // every block reads the same starting epoch.
+  const unsigned e0 = ld_acquire_u32(&c->epoch);
+  for (uint32_t k = 0; k < turns; k++) {
+    TurnParams tp;
+    const bool ran = turn_begin(d, tp);
+    if (ran) turn_work<MIN_BLOCKS_128, false, false, false>(d, cap, tp);
+    turn_close<true>(d, cap, tp, ran, k, turns, lo, hi);
+    if (threadIdx.x == 0) {
+      const bool late = !wait_change(&c->epoch, e0 + k, PERSIST_WAIT_NS);
+      if (late) set_status(d, ST_WAIT, blockIdx.x);
+      sh_go = late ? 0u : __ldcg(&c->go);
+    }
+    __syncthreads();
+    if (!sh_go) return;
   }
 }
 
@@ -662,7 +790,7 @@ __global__ void gather_kernel(Dev d, Port root, Port* out, uint32_t* kids, uint3
       if (is_nod(p)) {
         uint32_t pos = atomicAdd(&next, 2u);
         if (pos + 2 > cap) { overflow = 1; continue; }
-        Pair nd = (Pair)__ldcg((const unsigned long long*)&d.node[get_val(p)]);
+        Pair nd = nload(d, (uint32_t)get_val(p));
         out[pos] = resolve(get_fst(nd));
         out[pos + 1] = resolve(get_snd(nd));
         kids[k] = pos;
@@ -690,7 +818,7 @@ __global__ void read_list_kernel(Dev d, Port p, uint32_t max, uint32_t* out, uin
     }
     return q;
   };
-  auto node = [&](Port q) -> Pair { return (Pair)__ldcg((const unsigned long long*)&d.node[get_val(q)]); };
+  auto node = [&](Port q) -> Pair { return nload(d, (uint32_t)get_val(q)); };
   uint32_t k = 0, host = 0;
   while (k < max) {
     const Port lam = peekp(p);
@@ -721,7 +849,8 @@ __global__ void read_list_kernel(Dev d, Port p, uint32_t max, uint32_t* out, uin
   if (k == max) host = 1;
   info[0] = k;
   info[1] = host;
-  info[2] = p;
+  info[2] = (uint32_t)p;  // the port where the host loop takes over, low and high words
+  info[3] = (uint32_t)((uint64_t)p >> 32);
 }
 
 // ---- host runtime ----------------------------------------------------------------
@@ -980,15 +1109,15 @@ static std::string compiled_calls_source(const std::vector<HostDef>& defs) {
     char b[64];
     if (q == CALLER_PORT) return "caller";
     const Tag t = get_tag(q);
-    if (t >= CON) snprintf(b, sizeof b, "new_port(%s, nb + %uu)", tags[t], get_val(q));
-    else if (t == VAR) snprintf(b, sizeof b, "new_port(VAR, vb + %uu)", get_val(q));
-    else snprintf(b, sizeof b, "0x%08xu", q);
+    if (t >= CON) snprintf(b, sizeof b, "new_port(%s, nb + %uu)", tags[t], (unsigned)get_val(q));
+    else if (t == VAR) snprintf(b, sizeof b, "new_port(VAR, vb + %uu)", (unsigned)get_val(q));
+    else snprintf(b, sizeof b, "0x%08xu", (unsigned)q);  // REF/ERA/NUM: below 2^32 in either width
     return b;
   };
   std::string o;
   char line[96];
   o += "\n// ---- compiled calls (hvm gen-cu --compiled) ----\n";
-  o += "namespace hvm {\n";
+  o += "HVM_NS_BEGIN\n";
   snprintf(line, sizeof line, "// %zu of %zu defs compiled (the recursive ones and their callees)\n", ndefs, defs.size());
   o += line;
   o += "__device__ __forceinline__ bool compiled_call_nodes(const Dev& d, uint32_t fid, uint32_t nb, uint32_t vb) {\n";
@@ -1023,7 +1152,7 @@ static std::string compiled_calls_source(const std::vector<HostDef>& defs) {
   snprintf(line, sizeof line, "uint64_t compiled_book_hash() { return 0x%016llxull; }\n",
            (unsigned long long)tables_hash(hdr, flat));
   o += line;
-  o += "}  // namespace hvm\n";
+  o += "HVM_NS_END\n";
   return o;
 }
 
@@ -1054,6 +1183,8 @@ class Runtime {
   // allocator state and CALL scratch are sized for the larger grid.
   struct Variant {
     void (*fn)(Dev, uint32_t) = nullptr;
+    // Persistent form (cfg.persistent): same register cap, cooperative launch.
+    void (*pfn)(Dev, uint32_t, uint32_t, unsigned long long, unsigned long long) = nullptr;
     uint32_t grid = 0, nthreads = 0;
   };
   Variant variants[2];
@@ -1133,6 +1264,8 @@ class Runtime {
     smem = (size_t)block * cap * sizeof(Pair);
     if (block > 128) return fail("threads_per_block must be <= 128");
     if (cfg.local_nets > 1) return fail("local_nets must be 0 or 1");
+    if (cfg.persistent > 1) return fail("persistent must be 0 or 1");
+    if (cfg.persistent && cfg.graph_turns) return fail("persistent and graph_turns are exclusive");
     if (cfg.local_nets) {
       // The block's local net (LOCAL_WORDS nodes and vars: a slice per lane) follows the deques.
       if (block * LOCAL_SLICE != LOCAL_WORDS) return fail("local_nets needs 128-thread blocks");
@@ -1148,6 +1281,15 @@ class Runtime {
       if ((prof || local) && reg_cap != 0 && reg_cap != 8)
         return fail("profile and local_nets need reg_cap_blocks / narrow_reg_cap 0 or 8");
       if (fast && reg_cap == 6) return fail("fast_calls needs reg_cap_blocks / narrow_reg_cap 0, 5 or 8");
+#ifdef HVM_PORT64
+      // The 64-bit port build compiles the default variants only.
+      if (fast || prof || local) return fail("fast_calls, profile and local_nets are not in the 64-bit port build");
+      switch (reg_cap) {
+        case 0: v.fn = turn_kernel<0, false, false, false>; break;
+        case 8: v.fn = turn_kernel<8, false, false, false>; break;
+        default: return fail("the 64-bit port build has register caps 0 and 8");
+      }
+#else
       switch (reg_cap) {
         case 0: v.fn = fast ? turn_kernel<0, true, false, false> : prof ? turn_kernel<0, false, true, false>
                      : local ? turn_kernel<0, false, false, true> : turn_kernel<0, false, false, false>; break;
@@ -1157,9 +1299,20 @@ class Runtime {
                      : local ? turn_kernel<8, false, false, true> : turn_kernel<8, false, false, false>; break;
         default: return fail("reg_cap_blocks / narrow_reg_cap must be 0, 5, 6 or 8");
       }
+#endif
       CK(cudaFuncSetAttribute(v.fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
       int per_sm = 0;
       CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, v.fn, (int)block, smem));
+      if (cfg.persistent) {
+        if (fast || prof || local) return fail("persistent is not compiled with fast_calls, profile or local_nets");
+        if (reg_cap == 0) v.pfn = persistent_kernel<0>;
+        else if (reg_cap == 8) v.pfn = persistent_kernel<8>;
+        else return fail("persistent needs reg_cap_blocks / narrow_reg_cap 0 or 8");
+        CK(cudaFuncSetAttribute(v.pfn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        int p_sm = 0;  // every block of a cooperative launch must be resident
+        CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&p_sm, v.pfn, (int)block, smem));
+        per_sm = std::min(per_sm, p_sm);
+      }
       if (per_sm <= 0) return fail("turn kernel does not fit on an SM with this block size / stack capacity");
       if (cfg.blocks_per_sm && (int)cfg.blocks_per_sm < per_sm) per_sm = (int)cfg.blocks_per_sm;
       v.grid = (uint32_t)(per_sm * sms);
@@ -1619,6 +1772,34 @@ class Runtime {
     return 0;
   }
 
+  // One cooperative launch of the current variant's persistent kernel: up
+  // to `turns` turns, ending early at the normal form, on a failure, or once
+  // the pending count leaves the variant's range (narrow_below).
+  int launch_persistent(uint32_t turns) {
+    unsigned long long lo = 0, hi = ~0ull;
+    if (cfg.narrow_below) {
+      if (cur_variant == 0) lo = cfg.narrow_below;
+      else hi = cfg.narrow_below;
+    }
+    if (events.size() < 2) {
+      for (int i = 0; i < 2; i++) {
+        cudaEvent_t e;
+        CK(cudaEventCreate(&e));
+        events.push_back(e);
+      }
+    }
+    marks_valid = false;
+    auto fn = variants[cur_variant].pfn;
+    void* args[] = {&d, &cap, &turns, &lo, &hi};
+    CK(cudaEventRecord(events[0]));
+    CK(cudaLaunchCooperativeKernel((const void*)fn, dim3(grid), dim3(block), args, smem, 0));
+    CK(cudaEventRecord(events[1]));
+    turn_launches++;
+    launches++;
+    timed_units = 1;
+    return 0;
+  }
+
   int collect_times() {
     for (uint32_t i = 0; i < timed_units; i++) {
       float ms = 0;
@@ -1638,9 +1819,18 @@ class Runtime {
     unsigned long long last_itrs = ~0ull, last_pending = ~0ull;
     Ctl h;
     for (;;) {
-      if (launch_turns(batch)) return -1;
-      turns_run += batch;
+      if (cfg.persistent) {
+        // A launch runs one turn past the budget, as a poll batch may, so
+        // that an exhausted budget is seen below.
+        uint64_t k = PERSIST_TURNS;
+        if (cfg.max_turns) k = std::min<uint64_t>(k, cfg.max_turns - std::min<uint64_t>(turns_run, cfg.max_turns) + 1);
+        if (launch_persistent((uint32_t)k)) return -1;
+      } else {
+        if (launch_turns(batch)) return -1;
+        turns_run += batch;
+      }
       if (read_ctl(h) || collect_times()) return -1;
+      if (cfg.persistent) turns_run += h.persist_ran;
       if (h.status) {
         std::string m = std::string("device error: ") + status_text(h.status) + " (info " + std::to_string(h.err_info) + ")";
         if (h.oom_space)
@@ -1655,7 +1845,8 @@ class Runtime {
       // A net whose interaction count stops moving while redexes remain is
       // stuck (e.g. a redex that never becomes available): report it.
       if (h.itrs == last_itrs && h.pending == last_pending) {
-        if (++stalled_turns > 4096) return fail("no progress: interaction count stalled with redexes pending");
+        if (++stalled_turns > (cfg.persistent ? 1u : 4096u))
+          return fail("no progress: interaction count stalled with redexes pending");
       } else {
         stalled_turns = 0;
       }
@@ -1774,7 +1965,9 @@ class Runtime {
   // become a number is complete (done[k] = host seconds, result[k] = port).
   // When every net is admitted and the ring is empty, the rest complete with
   // whatever their ROOT holds, after the readback expansion.
-  int run_stream(const double* arrival, uint32_t max_inflight, double live_frac, double* done, Port* result,
+  // `result` receives each net's result port: a number, so it fits 32 bits
+  // in either port width.
+  int run_stream(const double* arrival, uint32_t max_inflight, double live_frac, double* done, uint32_t* result,
                  uint32_t order = 0) {
     if (defs.empty() || net_main.size() != nroots) return fail("no batch loaded");
     if (reset_net()) return -1;
@@ -1878,7 +2071,7 @@ class Runtime {
         for (size_t i = 0; i < active.size(); i++) {
           if (get_tag(ports[i]) == NUM) {
             done[active[i]] = t;
-            result[active[i]] = ports[i];
+            result[active[i]] = (uint32_t)ports[i];
           } else {
             active[w++] = active[i];
           }
@@ -2070,7 +2263,7 @@ class Runtime {
     read_list_kernel<<<1, 1>>>(d, p, LIST_READ_MAX, list_buf, list_buf + LIST_READ_MAX);
     CK(cudaGetLastError());
     launches++;
-    uint32_t info[3];
+    uint32_t info[4];
     CK(cudaMemcpy(info, list_buf + LIST_READ_MAX, sizeof(info), cudaMemcpyDeviceToHost));
     if (info[0]) {
       std::vector<uint32_t> v(info[0]);
@@ -2079,7 +2272,7 @@ class Runtime {
     }
     d2h_bytes += sizeof(info) + (uint64_t)info[0] * sizeof(uint32_t);
     if (!info[1]) return 0;
-    p = info[2];
+    p = (Port)(((uint64_t)info[3] << 32) | info[2]);
     for (;;) {
       if (normalize()) return -1;
       Ctr c;
@@ -2108,6 +2301,11 @@ class Runtime {
   static FILE** io_files() { static FILE* files[256]; return files; }
   static void** io_dylibs() { static void* libs[256]; return libs; }
   bool io_failed = false;  // set by an hvm_gb300_io_* call that failed inside a DL_CALL
+  // The last byte-list readback of the current DL_CALL: a length query and
+  // the read that follows evaluate the list once.
+  bool io_bytes_valid = false;
+  Port io_bytes_port = 0;
+  std::string io_bytes;
 
   // One IO function call (src/run.c:430-770); `ret` receives its result.
   int io_call(const std::string& name, Port argm, Port& ret) {
@@ -2218,6 +2416,9 @@ class Runtime {
       return inject_ok(new_port(ERA, 0), ret);
     }
     if (name == "DL_CALL") {
+#ifdef HVM_PORT64
+      return inject_io_err_str("DL_CALL needs the 32-bit port build (its library ABI passes 32-bit ports)", ret);
+#endif
       // (handle, symbol, argument) (src/run.cu:795-813): the symbol is called
       // as `Port fn(net, arg)` with this runtime as the net handle (the
       // hvm_gb300_io_* functions read and extend the device net); the port it
@@ -2234,6 +2435,7 @@ class Runtime {
       if (e) return inject_io_err_str(e, ret);
       if (!f) return inject_io_err_str("symbol resolves to NULL", ret);
       io_failed = false;
+      io_bytes_valid = false;
       const Port r = reinterpret_cast<hvm_gb300_dl_fn>(f)(reinterpret_cast<hvm_gb300_io*>(this), tup[2]);
       if (io_failed) return -1;
       return inject_ok(r, ret);
@@ -2287,7 +2489,7 @@ class Runtime {
     launches++;
     uint32_t info[2];
     CK(cudaMemcpy(info, g_info, sizeof(info), cudaMemcpyDeviceToHost));
-    d2h_bytes += sizeof(info) + 2ull * info[0] * sizeof(uint32_t);
+    d2h_bytes += sizeof(info) + (uint64_t)info[0] * (sizeof(Port) + sizeof(uint32_t));
     if (info[1]) return fail("result tree larger than the readback buffer");
     std::vector<Port> out(info[0]);
     std::vector<uint32_t> kids(info[0]);
@@ -2318,7 +2520,7 @@ class Runtime {
           break;
         }
         case ERA: s += "*"; break;
-        case VAR: snprintf(buf, sizeof buf, "x%x", get_val(p)); s += buf; break;
+        case VAR: snprintf(buf, sizeof buf, "x%llx", (unsigned long long)get_val(p)); s += buf; break;
         case NUM: print_numb(get_val(p), s); break;
         case REF: {
           uint32_t fid = get_val(p) & 0xFFFFFFFu;
@@ -2380,7 +2582,7 @@ class Runtime {
   }
 };
 
-}  // namespace hvm
+HVM_NS_END
 
 // ---- C ABI ---------------------------------------------------------------------------
 
@@ -2431,6 +2633,7 @@ extern "C" void hvm_gb300_default_config(hvm_gb300_config* c) {
   c->rule_select = 1;
   c->fast_calls = 0;
   c->local_nets = 0;
+  c->persistent = 0;
 }
 
 extern "C" int hvm_gb300_create(const hvm_gb300_config* cfg, hvm_gb300_runtime** out) {
@@ -2505,7 +2708,11 @@ extern "C" int hvm_gb300_batch_roots(hvm_gb300_runtime* r, uint32_t* out, size_t
   if (!r) return -1;
   if (r->rt.roots.size() != r->rt.nroots) return r->rt.fail("no batch has run");
   if (cap < r->rt.roots.size()) return r->rt.fail("output too small");
-  memcpy(out, r->rt.roots.data(), r->rt.roots.size() * sizeof(uint32_t));
+  for (size_t i = 0; i < r->rt.roots.size(); i++) {
+    const hvm::Port p = r->rt.roots[i];
+    if ((uint64_t)p > 0xFFFFFFFFull) return r->rt.fail("a root port does not fit 32 bits (use hvm_gb300_batch_result)");
+    out[i] = (uint32_t)p;
+  }
   return 0;
 }
 
@@ -2601,6 +2808,8 @@ namespace hvm_io {
 using namespace hvm;
 
 static hvm::Runtime& io_rt(hvm_gb300_io* io) { return *reinterpret_cast<hvm::Runtime*>(io); }
+// The 64-bit port build calls no DL_CALL library, so these are never reached there.
+constexpr bool IO_PORTS_32 = hvm::PORT_BITS == 32;
 static int io_fail(hvm::Runtime& rt, const char* msg) {
   if (msg) rt.fail(msg);
   rt.io_failed = true;
@@ -2609,11 +2818,14 @@ static int io_fail(hvm::Runtime& rt, const char* msg) {
 }  // namespace hvm_io
 using hvm_io::io_rt;
 using hvm_io::io_fail;
+using hvm_io::IO_PORTS_32;
 
 extern "C" int hvm_gb300_io_expand(hvm_gb300_io* io, uint32_t port, uint32_t* out) {
+  if (!IO_PORTS_32) return -1;
   using namespace hvm;
   if (!io || !out) return -1;
   hvm::Runtime& rt = io_rt(io);
+  rt.io_bytes_valid = false;  // the net changes
   Port p;
   if (rt.expand(port, &p)) return io_fail(rt, nullptr);
   *out = p;
@@ -2621,6 +2833,7 @@ extern "C" int hvm_gb300_io_expand(hvm_gb300_io* io, uint32_t port, uint32_t* ou
 }
 
 extern "C" int hvm_gb300_io_node_load(hvm_gb300_io* io, uint32_t port, uint32_t* fst, uint32_t* snd) {
+  if (!IO_PORTS_32) return -1;
   using namespace hvm;
   if (!io || !fst || !snd) return -1;
   hvm::Runtime& rt = io_rt(io);
@@ -2633,9 +2846,11 @@ extern "C" int hvm_gb300_io_node_load(hvm_gb300_io* io, uint32_t port, uint32_t*
 }
 
 extern "C" int hvm_gb300_io_make_node(hvm_gb300_io* io, uint32_t tag, uint32_t fst, uint32_t snd, uint32_t* out) {
+  if (!IO_PORTS_32) return -1;
   using namespace hvm;
   if (!io || !out) return -1;
   hvm::Runtime& rt = io_rt(io);
+  rt.io_bytes_valid = false;  // the net changes
   if (tag < CON || tag > SWI) return io_fail(rt, "hvm_gb300_io_make_node: not a node tag");
   hvm::Runtime::Inject in;
   const hvm::Runtime::LPort n = in.node(hvm::Runtime::ext(fst), hvm::Runtime::ext(snd));
@@ -2647,9 +2862,11 @@ extern "C" int hvm_gb300_io_make_node(hvm_gb300_io* io, uint32_t tag, uint32_t f
 
 extern "C" int hvm_gb300_io_readback_tup(hvm_gb300_io* io, uint32_t port, uint32_t size, uint32_t* elems,
                                          uint32_t* n) {
+  if (!IO_PORTS_32) return -1;
   using namespace hvm;
   if (!io || !elems || !n || size == 0) return -1;
   hvm::Runtime& rt = io_rt(io);
+  rt.io_bytes_valid = false;  // the net changes
   std::vector<Port> tup;
   if (rt.read_tup(port, size, tup)) return io_fail(rt, nullptr);
   for (size_t i = 0; i < tup.size(); i++) elems[i] = tup[i];
@@ -2658,11 +2875,17 @@ extern "C" int hvm_gb300_io_readback_tup(hvm_gb300_io* io, uint32_t port, uint32
 }
 
 extern "C" int hvm_gb300_io_readback_bytes(hvm_gb300_io* io, uint32_t port, uint8_t* out, size_t cap, size_t* len) {
+  if (!IO_PORTS_32) return -1;
   using namespace hvm;
   if (!io || !len) return -1;
   hvm::Runtime& rt = io_rt(io);
-  std::string b;
-  if (rt.read_bytes(port, b)) return io_fail(rt, nullptr);
+  if (!rt.io_bytes_valid || rt.io_bytes_port != port) {
+    rt.io_bytes_valid = false;
+    if (rt.read_bytes(port, rt.io_bytes)) return io_fail(rt, nullptr);
+    rt.io_bytes_valid = true;
+    rt.io_bytes_port = port;
+  }
+  const std::string& b = rt.io_bytes;
   *len = b.size();
   if (out) {
     if (cap < b.size()) return io_fail(rt, "hvm_gb300_io_readback_bytes: buffer too small");
@@ -2672,13 +2895,33 @@ extern "C" int hvm_gb300_io_readback_bytes(hvm_gb300_io* io, uint32_t port, uint
 }
 
 extern "C" int hvm_gb300_io_inject_bytes(hvm_gb300_io* io, const uint8_t* bytes, size_t len, uint32_t* out) {
+  if (!IO_PORTS_32) return -1;
   using namespace hvm;
   if (!io || !out || (len && !bytes)) return -1;
   hvm::Runtime& rt = io_rt(io);
+  rt.io_bytes_valid = false;  // the net changes
   Port p;
   if (rt.inject_bytes(std::string((const char*)bytes, len), p)) return io_fail(rt, nullptr);
   *out = p;
   return 0;
+}
+
+extern "C" int hvm_gb300_wait_probe(int32_t device, uint32_t limit_ms, uint32_t* timed_out, double* waited_ms) {
+  if (!timed_out || !waited_ms || limit_ms == 0 || limit_ms > 10000) return -1;
+  if (cudaSetDevice(device) != cudaSuccess) return -1;
+  unsigned* buf = nullptr;
+  if (cudaMalloc((void**)&buf, 4 * sizeof(unsigned)) != cudaSuccess) return -1;
+  int rc = cudaMemset(buf, 0, 4 * sizeof(unsigned)) == cudaSuccess ? 0 : -1;
+  if (rc == 0) {
+    hvm::wait_probe_kernel<<<1, 1>>>(buf, (unsigned long long)limit_ms * 1000000ull, buf + 1);
+    unsigned out[3] = {0, 0, 0};
+    rc = cudaGetLastError() == cudaSuccess && cudaMemcpy(out, buf + 1, sizeof(out), cudaMemcpyDeviceToHost) == cudaSuccess
+             ? 0 : -1;
+    *timed_out = out[0];
+    *waited_ms = (double)(((unsigned long long)out[2] << 32) | out[1]) / 1e6;
+  }
+  cudaFree(buf);
+  return rc;
 }
 
 // Drop-in for the reference's CUDA entry point (src/hvm.cu:2320-2397): loads
@@ -2736,7 +2979,7 @@ extern "C" void hvm_cu(const uint32_t* book_buffer) {
 // (cudaGetSymbolAddress) with that device current; make that first call
 // before any stream capture.
 
-namespace hvm {
+HVM_NS_BEGIN
 namespace noalloc {
 
 // Fixed capacities of the arena. The grid is fixed (16 blocks of 128 threads,
@@ -2764,13 +3007,13 @@ constexpr size_t OFF_CTL = OFF_INFO + 256;
 constexpr size_t ARENA_BYTES = OFF_CTL + align256(sizeof(Ctl));
 
 }  // namespace noalloc
-}  // namespace hvm
+HVM_NS_END
 
 // The arena. In host code this name is a host-side stand-in, not a device
 // address: only the address from cudaGetSymbolAddress may be given to kernels.
 static __device__ __align__(256) unsigned char g_noalloc_arena[hvm::noalloc::ARENA_BYTES];
 
-namespace hvm {
+HVM_NS_BEGIN
 namespace noalloc {
 
 constexpr int MAX_DEVICES = 64;
@@ -2956,7 +3199,7 @@ static int validate(Ctx& x, const uint32_t* w, size_t words) {
 }
 
 }  // namespace noalloc
-}  // namespace hvm
+HVM_NS_END
 
 extern "C" int hvm_gb300_run_noalloc(const uint32_t* book, size_t words, uint32_t* out_ports, uint32_t* out_kids,
                                      size_t out_cap, size_t* out_len, uint64_t* out_itrs, char* err, size_t err_cap) {
@@ -2965,6 +3208,7 @@ extern "C" int hvm_gb300_run_noalloc(const uint32_t* book, size_t words, uint32_
   Ctx x{};
   x.err = err;
   x.err_cap = err_cap;
+  if (PORT_BITS != 32) return failf(x, "hvm_gb300_run_noalloc returns 32-bit ports: not in the 64-bit port build");
   if (err && err_cap) err[0] = 0;
   int dev = 0;
   if (cuda_ok(x, cudaGetDevice(&dev))) return -1;

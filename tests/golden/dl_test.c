@@ -71,7 +71,7 @@ uint32_t greet_g(hvm_gb300_io* net, uint32_t arg) {
  * tuple and node readbacks: exercises the remaining GB300 net functions. The
  * reference binary exports no node constructor for a library to call, so
  * this one has no C twin; its test compares with a known answer. */
-uint32_t pair_g(hvm_gb300_io* net, uint32_t arg) {
+uint32_t two_g(hvm_gb300_io* net, uint32_t arg) {
   uint32_t a = 0, out = 0;
   if (hvm_gb300_io_expand(net, arg, &a)) return 0;
   if (hvm_gb300_io_make_node(net, 4u /* CON */, a, succ_u24(a), &out)) return 0;

@@ -220,11 +220,11 @@ def make_dl(ref: str) -> None:
         entry = {"name": f"dl_call {fn}", "code": dl_program(prelude, sym_g, arg), **run_ref_io(code_c, DL_LIB)}
         out.append(entry)
         print(entry["name"], entry["itrs"], entry["result"][:80])
-    # pair_g has no C twin: its known answer is the inc program's with the Ok
-    # payload 42 replaced by the pair (41 42); the payload is never reduced,
-    # so the interaction count is the same.
+    # two_g has no C twin: its known answer is the inc program's with the Ok
+    # payload 42 replaced by the pair (41 42); the payload is never reduced
+    # and the symbol names have one length, so the interaction count is the same.
     inc = out[0]
-    pair = {"name": "dl_call pair (known answer)", "code": dl_program(prelude, "pair_g", 41),
+    pair = {"name": "dl_call pair (known answer)", "code": dl_program(prelude, "two_g", 41),
             "printed": inc["printed"], "result": inc["result"].replace("(((0 (42 ", "(((0 ((41 42) ", 1),
             "itrs": inc["itrs"]}
     assert pair["result"] != inc["result"]

@@ -4,6 +4,7 @@ numbers) and identical interaction count. All calls go through the C ABI."""
 from __future__ import annotations
 
 import hashlib
+import importlib
 import re
 import subprocess
 
@@ -82,9 +83,11 @@ def test_kernel_variant_switching(hvm, workloads, config_goldens, cfg):
 
 @pytest.mark.parametrize("cfg", [dict(fast_calls=1), dict(fast_calls=2), dict(fast_calls=2, rule_select=0),
                                  dict(fast_calls=1, reg_cap_blocks=0), dict(rule_select=2), dict(local_nets=1),
-                                 dict(local_nets=1, reg_cap_blocks=0, narrow_below=0)],
+                                 dict(local_nets=1, reg_cap_blocks=0, narrow_below=0), dict(persistent=1),
+                                 dict(persistent=1, narrow_below=0), dict(persistent=1, reg_cap_blocks=0, narrow_below=0)],
                          ids=["fast_switch", "fast_switch_anni", "fast_all_lanes", "fast_uncapped", "rule_per_round",
-                              "local_nets", "local_nets_uncapped"])
+                              "local_nets", "local_nets_uncapped", "persistent", "persistent_one_variant",
+                              "persistent_uncapped"])
 def test_scheduling_options(hvm, workloads, config_goldens, ref_programs, cfg):
     # CALL-time fast paths (the reference's compiled-mode short-cuts, adding
     # by hand the interactions they perform), the per-round rule selection
@@ -105,6 +108,32 @@ def test_scheduling_options(hvm, workloads, config_goldens, ref_programs, cfg):
             res, st = run(r, prog["code"])
             assert st.itrs == prog["itrs"], prog["name"]
             assert hvm.canonical(res) == hvm.canonical(prog["result"]), prog["name"]
+
+
+def test_persistent_launch_count(hvm, workloads, config_goldens):
+    # A persistent normalisation closes its turns on the device: a handful of
+    # launches for a net that runs tens of turns, the same result.
+    code = workloads.bitonic_sort(12)
+    with hvm.Runtime(device=0, persistent=1) as r:
+        res, st = run(r, code)
+        assert st.itrs == config_goldens["bitonic_sort_2p12"]["itrs"]
+        assert st.turns > 8
+        assert st.turn_launches <= 4
+        # The learned scheduler's inference runs in the closing block as well.
+        train = importlib.import_module("lambdavm-rust_gb300.train_policy")
+        r.set_policy(hvm.POLICY_LEARNED, weights=train.load_weights())
+        res2, st2 = run(r, code)
+        assert st2.itrs == st.itrs and hvm.canonical(res2) == hvm.canonical(res)
+
+
+def test_persistent_wait_limit(hvm, rt, workloads):
+    # The bounded wait of persistent launches, on a word nothing writes: the
+    # limit runs out, the kernel returns, and the context still runs a net.
+    timed_out, ms = hvm.wait_probe(limit_ms=100)
+    assert timed_out
+    assert 90.0 <= ms < 5000.0
+    res, st = run(rt, workloads.tree_sum(8))
+    assert res == "256"
 
 
 def test_repeat_runs_identical(hvm, rt, workloads):
