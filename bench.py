@@ -54,6 +54,7 @@ REF_CU_UNAVAILABLE = ("the reference CUDA runtime never finished the bitonic-sor
                       "it, so it is not run on them")
 
 BATCH_GOLDEN = os.path.join(ROOT, "tests", "golden", "batch_mixed_4096.json")
+SERVING_GOLDEN = os.path.join(ROOT, "tests", "golden", "serving_pool.json")
 
 WORKLOADS = {
     # name: (golden key, generator, description)
@@ -65,6 +66,8 @@ WORKLOADS = {
     "batch_mixed_4096": (None, None, "4096 independent nets (1/3 tree sums d 8..18, 1/3 bitonic sorts of 2^6..2^12 "
                                      "keys then summed, 1/3 countdowns 10..1e5), continuous batching"),
     "serving": (None, None, "Poisson arrivals of nets drawn from the 4096-net mixed pool, continuous batching"),
+    "serving_2p22": (None, None, "Poisson arrivals of nets sized log-uniform up to 2^22 nodes (serving pool), "
+                                 "64-bit ports, 64 GB arena, continuous batching"),
     "compiled_calls": (None, None, "standalone `hvm gen-cu --compiled` programs against `hvm gen-cu` ones "
                                    "(bitonic 2^16, tree sum d=20, skewed fold 2^18, countdown 1e5)"),
 }
@@ -281,6 +284,43 @@ def bench_serving(hvm, W, rates=(1e2, 1e3, 1e4, 1e5), seconds: float = 2.0, max_
                     "parity": bool(ok and st.itrs == itrs_expected)})
     rt.close()
     return {"rates": out}
+
+
+# Serving at its stated scale: request nets up to 2^22 nodes in a 64 GB arena
+# of the 64-bit port build (2^31 node words of 16 B + 2^32 var words of 8 B),
+# admission while the live words stay under half of each space.
+SERVING_ARENA = {"port64": True, "node_log2": 31, "vars_log2": 32}
+SERVING_LIVE_FRAC = 0.5
+
+
+def bench_serving_scaled(hvm, W, rates=(1e2, 1e3, 1e4, 1e5), seconds: float = 2.0, max_requests: int = 1000) -> dict:
+    """Serving with the serving pool (96 templates of the three families,
+    sizes log-uniform from 2^8 to 2^22 nodes) in the 64 GB arena: Poisson
+    arrivals at each rate for about `seconds` (at most `max_requests`);
+    latency = completion - arrival on the host clock; every response and the
+    interaction total checked against the reference's per-template results."""
+    gold = json.load(open(SERVING_GOLDEN))
+    nets = W.serving_pool(gold["count"])
+    books = [hvm.book_from_text(code) for code, _ in nets]
+    out = []
+    with hvm.Runtime(device=0, **SERVING_ARENA) as rt:
+        for rate in rates:
+            n = int(min(max_requests, max(50, rate * seconds)))
+            arrivals, tmpl = W.serving_requests(n, rate, pool=gold["count"])
+            rt.load_batch(books)
+            rt.set_requests(tmpl)
+            t0 = time.perf_counter()
+            st, done, res = rt.run_stream(arrival_s=arrivals, max_inflight=BATCH_INFLIGHT, live_frac=SERVING_LIVE_FRAC)
+            wall = time.perf_counter() - t0
+            lat = sorted(float(d - a) for d, a in zip(done, arrivals))
+            ok = all(numb_u24(p) == int(gold["nets"][t]["result"]) for p, t in zip(res, tmpl))
+            itrs_expected = sum(gold["nets"][t]["itrs"] for t in tmpl)
+            out.append({"rate_per_s": rate, "requests": n, "wall_s": wall, "itrs": st.itrs,
+                        "itrs_per_s": st.itrs / wall, "p50_latency_s": lat[len(lat) // 2],
+                        "p99_latency_s": lat[min(len(lat) - 1, int(len(lat) * 0.99))],
+                        "parity": bool(ok and st.itrs == itrs_expected)})
+    return {"arena": {**SERVING_ARENA, "bytes": (16 << 31) + (8 << 32), "live_frac": SERVING_LIVE_FRAC},
+            "pool": {"templates": gold["count"], "max_log2_nodes": 22}, "rates": out}
 
 
 def dist_env():
@@ -747,7 +787,7 @@ def main():
     ap.add_argument("--impl", choices=["gb300", "reference"], default="gb300")
     ap.add_argument("--workload", choices=sorted(WORKLOADS), default="bitonic_sort_2p16")
     ap.add_argument("--no-batch", action="store_true",
-                    help="skip the 4096-net batch, scheduler and reference-CUDA reports of the default line")
+                    help="skip the 4096-net batch, scheduler, serving and reference-CUDA reports of the default line")
     ap.add_argument("--profile-case", choices=["bitonic", "tree_sum", "skewed"],
                     help="evaluate one small case for a profiler instead of benchmarking (see profile_case)")
     ap.add_argument("--log2n", type=int, default=14, help="--profile-case: keys / depth / elements (log2)")
@@ -786,7 +826,7 @@ def main():
                 "config": {"workload": desc, **cc}}
         print(json.dumps(line), flush=True)
         return
-    if args.workload in ("batch_mixed_4096", "serving"):
+    if args.workload in ("batch_mixed_4096", "serving", "serving_2p22"):
         if args.impl == "reference" or rank != 0:
             if rank == 0:
                 print(json.dumps({"impl": "reference", "unavailable": "the CPU arm runs the single-net workloads"}))
@@ -811,7 +851,7 @@ def main():
                     "scaling": "weak", "vs_baseline": None, "dtype": "u32", "data": "synthetic",
                     "config": {"workload": desc, **{k: v for k, v in b.items() if k not in ("value", "unit")}}}
         else:
-            sv = bench_serving(hvm, W)
+            sv = bench_serving(hvm, W) if args.workload == "serving" else bench_serving_scaled(hvm, W)
             best = max(r["itrs_per_s"] for r in sv["rates"])
             line = {"metric": METRIC, "value": best, "unit": UNIT, "n_gpus": 1, "steps": 1, "warmup": 0,
                     "ms_per_step": None, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
@@ -830,6 +870,7 @@ def main():
             line["config4"] = config4_report(line["batched"], line["batched_learned"], line["batched_tuned"])
             line["scheduler"] = bench_scheduler(hvm, W)
         if line is not None and not args.no_batch:
+            line["serving"] = bench_serving_scaled(hvm, W)
             line["reference_cuda"] = bench_reference_cuda(hvm, W)
     finally:
         dist.close()

@@ -77,8 +77,9 @@ typedef struct {
   uint32_t threads_per_block; /* multiple of 32, at most 128 */
   uint32_t stack_cap;         /* redexes per thread in the shared-memory LIFO */
   uint32_t blocks_per_sm;     /* 0 = as many as fit */
-  uint32_t node_log2;         /* node space 2^k words (k <= 29, the port width) */
-  uint32_t vars_log2;         /* var space 2^k words (k <= 29) */
+  uint32_t node_log2;         /* node space 2^k words (k <= 29 with 32-bit ports, <= 32 in the 64-bit
+                                 port library libhvm_gb300_p64.so) */
+  uint32_t vars_log2;         /* var space 2^k words (same bounds) */
   uint32_t ring_log2;         /* global redex ring 2^k entries */
   uint32_t max_turns;         /* 0 = unbounded; else fail after this many turns */
   uint32_t stop_frac_q8;      /* a turn ends once busy threads < (1 - f/256) x initially busy */
@@ -117,6 +118,9 @@ typedef struct {
   uint32_t persistent;        /* 1 = a normalisation runs its turns inside cooperative launches of up
                                  to 4096 turns each, closed on the device (register caps 0 and 8, no
                                  fast_calls/profile/local_nets); 0 = one launch per turn */
+  uint32_t upper_half;        /* 1 = the allocator hands out words from the upper half of each space
+                                 only (every fresh word has a high index: with 64-bit ports and 2^32-word
+                                 spaces, indices beyond the 32-bit port's range) */
 } hvm_gb300_config;
 
 typedef struct {

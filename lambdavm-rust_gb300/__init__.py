@@ -20,9 +20,13 @@ import numpy as np
 
 PKG_DIR = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(PKG_DIR, "libhvm_gb300.so")
+# The same runtime over 64-bit ports (128-bit node pairs, spaces of up to
+# 2^32 words each): Runtime(port64=True).
+LIB64_PATH = os.path.join(PKG_DIR, "libhvm_gb300_p64.so")
 CLI_PATH = os.path.join(PKG_DIR, "hvm")
 
 _lib = None
+_lib64 = None
 
 
 class HvmError(RuntimeError):
@@ -55,6 +59,7 @@ class Config(ctypes.Structure):
         ("fast_calls", ctypes.c_uint32),
         ("local_nets", ctypes.c_uint32),
         ("persistent", ctypes.c_uint32),
+        ("upper_half", ctypes.c_uint32),
     ]
 
 
@@ -142,12 +147,24 @@ EXPORTED_SYMBOLS = (
 def lib() -> ctypes.CDLL:
     """Loads libhvm_gb300.so (built in-tree by build.py); raises if absent."""
     global _lib
-    if _lib is not None:
-        return _lib
-    if not os.path.exists(LIB_PATH):
-        raise HvmError(f"{LIB_PATH} is missing: build it with `python lambdavm-rust_gb300/build.py` "
+    if _lib is None:
+        _lib = _load(LIB_PATH)
+    return _lib
+
+
+def lib64() -> ctypes.CDLL:
+    """Loads libhvm_gb300_p64.so, the 64-bit port build; raises if absent."""
+    global _lib64
+    if _lib64 is None:
+        _lib64 = _load(LIB64_PATH)
+    return _lib64
+
+
+def _load(path: str) -> ctypes.CDLL:
+    if not os.path.exists(path):
+        raise HvmError(f"{path} is missing: build it with `python lambdavm-rust_gb300/build.py` "
                        "or `python -c 'import __graft_entry__ as g; g.build()'`")
-    L = ctypes.CDLL(LIB_PATH)
+    L = ctypes.CDLL(path)
     u32p = ctypes.POINTER(ctypes.c_uint32)
     L.hvm_cu.argtypes = [u32p]
     L.hvm_cu.restype = None
@@ -197,7 +214,6 @@ def lib() -> ctypes.CDLL:
     L.hvm_gb300_error.restype = ctypes.c_char_p
     L.hvm_gb300_destroy.argtypes = [ctypes.c_void_p]
     L.hvm_gb300_destroy.restype = None
-    _lib = L
     return L
 
 
@@ -277,8 +293,9 @@ class RunStats:
 class Runtime:
     """One GPU net (include/hvm_gb300.h handle API)."""
 
-    def __init__(self, device: int = 0, **overrides):
-        L = lib()
+    def __init__(self, device: int = 0, port64: bool = False, **overrides):
+        L = lib64() if port64 else lib()
+        self._L = L
         cfg = Config()
         L.hvm_gb300_default_config(ctypes.byref(cfg))
         cfg.device = device
@@ -297,19 +314,19 @@ class Runtime:
 
     def _check(self, rc: int) -> None:
         if rc:
-            raise HvmError(lib().hvm_gb300_error(self._h).decode())
+            raise HvmError(self._L.hvm_gb300_error(self._h).decode())
 
     def load(self, book) -> None:
         if isinstance(book, str):
             book = book_from_text(book)
         buf = np.ascontiguousarray(np.asarray(book, dtype=np.uint32))
         self._book = buf
-        self._check(lib().hvm_gb300_load_book(self._h, buf.ctypes.data_as(ctypes.POINTER(ctypes.c_uint32)),
+        self._check(self._L.hvm_gb300_load_book(self._h, buf.ctypes.data_as(ctypes.POINTER(ctypes.c_uint32)),
                                               buf.size))
 
     def run(self) -> RunStats:
         st = _Stats()
-        self._check(lib().hvm_gb300_run(self._h, ctypes.byref(st)))
+        self._check(self._L.hvm_gb300_run(self._h, ctypes.byref(st)))
         return self._stats(st)
 
     @staticmethod
@@ -329,17 +346,17 @@ class Runtime:
         u32p = ctypes.POINTER(ctypes.c_uint32)
         ptrs = (u32p * len(bufs))(*[b.ctypes.data_as(u32p) for b in bufs])
         sizes = (ctypes.c_size_t * len(bufs))(*[b.size for b in bufs])
-        self._check(lib().hvm_gb300_load_batch(self._h, ptrs, sizes, len(bufs)))
+        self._check(self._L.hvm_gb300_load_batch(self._h, ptrs, sizes, len(bufs)))
 
     def run_batch(self) -> RunStats:
         st = _Stats()
-        self._check(lib().hvm_gb300_run_batch(self._h, ctypes.byref(st)))
+        self._check(self._L.hvm_gb300_run_batch(self._h, ctypes.byref(st)))
         return self._stats(st)
 
     def set_requests(self, templates) -> None:
         """Makes request r a copy of loaded net templates[r] (serving)."""
         t = np.ascontiguousarray(templates, dtype=np.uint32)
-        self._check(lib().hvm_gb300_set_requests(self._h, t.ctypes.data_as(ctypes.POINTER(ctypes.c_uint32)), t.size))
+        self._check(self._L.hvm_gb300_set_requests(self._h, t.ctypes.data_as(ctypes.POINTER(ctypes.c_uint32)), t.size))
         self._batch = [None] * t.size
 
     def run_stream(self, arrival_s=None, max_inflight: int = 0, live_frac: float = 0.25, order: int = 0):
@@ -349,7 +366,7 @@ class Runtime:
         done = np.zeros(n, dtype=np.float64)
         res = np.zeros(n, dtype=np.uint32)
         st = _Stats()
-        self._check(lib().hvm_gb300_run_stream(self._h, arr.ctypes.data_as(ctypes.POINTER(ctypes.c_double)),
+        self._check(self._L.hvm_gb300_run_stream(self._h, arr.ctypes.data_as(ctypes.POINTER(ctypes.c_double)),
                                                max_inflight, live_frac, order,
                                                done.ctypes.data_as(ctypes.POINTER(ctypes.c_double)),
                                                res.ctypes.data_as(ctypes.POINTER(ctypes.c_uint32)),
@@ -358,38 +375,38 @@ class Runtime:
 
     def batch_roots(self) -> np.ndarray:
         out = np.zeros(len(self._batch), dtype=np.uint32)
-        self._check(lib().hvm_gb300_batch_roots(self._h, out.ctypes.data_as(ctypes.POINTER(ctypes.c_uint32)),
+        self._check(self._L.hvm_gb300_batch_roots(self._h, out.ctypes.data_as(ctypes.POINTER(ctypes.c_uint32)),
                                                 out.size))
         return out
 
     def batch_result(self, net: int) -> str:
         n = ctypes.c_size_t()
-        self._check(lib().hvm_gb300_batch_result(self._h, net, None, 0, ctypes.byref(n)))
+        self._check(self._L.hvm_gb300_batch_result(self._h, net, None, 0, ctypes.byref(n)))
         out = ctypes.create_string_buffer(n.value + 1)
-        self._check(lib().hvm_gb300_batch_result(self._h, net, out, n.value + 1, ctypes.byref(n)))
+        self._check(self._L.hvm_gb300_batch_result(self._h, net, out, n.value + 1, ctypes.byref(n)))
         return out.value.decode()
 
     def result(self) -> str:
         n = ctypes.c_size_t()
-        self._check(lib().hvm_gb300_result(self._h, None, 0, ctypes.byref(n)))
+        self._check(self._L.hvm_gb300_result(self._h, None, 0, ctypes.byref(n)))
         out = ctypes.create_string_buffer(n.value + 1)
-        self._check(lib().hvm_gb300_result(self._h, out, n.value + 1, ctypes.byref(n)))
+        self._check(self._L.hvm_gb300_result(self._h, out, n.value + 1, ctypes.byref(n)))
         return out.value.decode()
 
     def count_live(self) -> dict:
         out = (ctypes.c_uint64 * 5)()
-        self._check(lib().hvm_gb300_count_live(self._h, out))
+        self._check(self._L.hvm_gb300_count_live(self._h, out))
         return {"nodes": out[0], "vars": out[1], "marked": out[2], "node_pages": out[3], "var_pages": out[4]}
 
     def reset_counters(self) -> None:
-        lib().hvm_gb300_reset_counters(self._h)
+        self._L.hvm_gb300_reset_counters(self._h)
 
     def trace(self) -> list[dict]:
         """Per-turn records of the last run (needs trace_cap > 0)."""
         n = ctypes.c_size_t()
-        self._check(lib().hvm_gb300_trace(self._h, None, 0, ctypes.byref(n)))
+        self._check(self._L.hvm_gb300_trace(self._h, None, 0, ctypes.byref(n)))
         arr = (Turn * max(1, n.value))()
-        self._check(lib().hvm_gb300_trace(self._h, arr, n.value, ctypes.byref(n)))
+        self._check(self._L.hvm_gb300_trace(self._h, arr, n.value, ctypes.byref(n)))
         out = []
         for i in range(n.value):
             r = {k: getattr(arr[i], k) for k, _ in Turn._fields_}
@@ -407,11 +424,11 @@ class Runtime:
         turn (the decision at the close of turn k; -1 or later turns: fixed)."""
         w = _floats(weights) if weights is not None else None
         c = _floats(constants) if constants is not None else None
-        self._check(lib().hvm_gb300_set_policy(self._h, mode, w, len(w) if w is not None else 0, c))
+        self._check(self._L.hvm_gb300_set_policy(self._h, mode, w, len(w) if w is not None else 0, c))
 
     def close(self) -> None:
         if getattr(self, "_h", None):
-            lib().hvm_gb300_destroy(self._h)
+            self._L.hvm_gb300_destroy(self._h)
             self._h = None
 
     def __enter__(self):

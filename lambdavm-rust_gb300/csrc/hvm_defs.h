@@ -86,7 +86,13 @@ constexpr uint32_t MAX_DEFS     = 0x4000;
 // Each def header in the buffer: fid, name[64], safe, rbag_len, node_len, vars_len, root.
 constexpr uint32_t DEF_HEADER_WORDS = 1 + 64 + 5;
 
+#ifdef HVM_PORT64
+// A number keeps the 29-bit Numb a 32-bit port holds: the reference's u24
+// arithmetic wraps where (numb << 3) leaves the 32-bit word.
+HVM_HD Port new_port(Tag tag, Val val) { return ((tag == NUM ? val & 0x1FFFFFFFull : val) << 3) | tag; }
+#else
 HVM_HD Port new_port(Tag tag, Val val) { return (val << 3) | tag; }
+#endif
 HVM_HD Tag  get_tag(Port p) { return (Tag)(p & 7); }
 HVM_HD Val  get_val(Port p) { return p >> 3; }
 HVM_HD Pair new_pair(Port fst, Port snd) { return ((Pair)snd << PORT_BITS) | fst; }

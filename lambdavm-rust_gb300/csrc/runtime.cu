@@ -238,12 +238,13 @@ __device__ __forceinline__ void turn_work(const Dev& d, uint32_t cap, const Turn
   alloc_load<false>(d.nspace, t.gid, t.na);
   alloc_load<true>(d.vspace, t.gid, t.va);
   t.base = base;
-  t.itrs = t.leak = t.retries = 0;
+  t.leak = t.retries = 0;
   t.live_nodes = t.live_vars = 0;
   t.dirty = false;
-  for (int i = 0; i < 8; i++) t.hist[i] = 0;
   t.dead = false;
   t.waited = 0;
+  if (threadIdx.x < 8) s_hist[threadIdx.x] = 0;
+  __syncthreads();
   if (LOCAL) {
     // Each lane clears its own slice of the block's local net (128-thread blocks).
     for (uint32_t i = 0; i < LOCAL_SLICE; i++) { lnode_of(t)[lbase_of() + i] = 0; lvar_of(t)[lbase_of() + i] = 0; }
@@ -330,7 +331,7 @@ __device__ __forceinline__ void turn_work(const Dev& d, uint32_t cap, const Turn
     }
     const bool has = go;
     const Pair r = has ? pop(t) : 0;
-    lockstep_round<FAST, LOCAL, MIN_BLOCKS_128 != 8>(d, t, has, r, prof_on ? &prof : nullptr);
+    lockstep_round<FAST, LOCAL>(d, t, has, r, prof_on ? &prof : nullptr);
     if (__any_sync(0xFFFFFFFFu, t.dead)) break;
     if (LOCAL && __any_sync(0xFFFFFFFFu, ovf_len_of(t) > OVF_HIGH)) break;  // end the turn before an overflow fills
     // The stop flag is tested one round after it was loaded, so its L2
@@ -356,7 +357,7 @@ __device__ __forceinline__ void turn_work(const Dev& d, uint32_t cap, const Turn
       }
       const Pair r = has ? pop(t) : 0;
       if (has && !local_pair(r)) { ring_put(d, t, r); has = false; }
-      lockstep_round<FAST, LOCAL, MIN_BLOCKS_128 != 8>(d, t, has, r, nullptr, true);
+      lockstep_round<FAST, LOCAL>(d, t, has, r, nullptr, true);
       if (__any_sync(0xFFFFFFFFu, t.dead)) break;
     }
   }
@@ -405,12 +406,11 @@ __device__ __forceinline__ void turn_work(const Dev& d, uint32_t cap, const Turn
   if (threadIdx.x < 11) blk_cnt[threadIdx.x] = 0;
   __syncthreads();
   unsigned long long v;
-  v = warp_sum(t.itrs);    if (lane == 0 && v) atomicAdd(&blk_cnt[0], v);
   v = warp_sum(t.leak);    if (lane == 0 && v) atomicAdd(&blk_cnt[1], v);
   v = warp_sum(t.retries); if (lane == 0 && v) atomicAdd(&blk_cnt[2], v);
-  for (int i = 0; i < 8; i++) {
-    v = warp_sum(t.hist[i]);
-    if (lane == 0 && v) atomicAdd(&blk_cnt[3 + i], v);
+  if (threadIdx.x < 8) {
+    blk_cnt[3 + threadIdx.x] = s_hist[threadIdx.x];
+    if (threadIdx.x != LINK) atomicAdd(&blk_cnt[0], (unsigned long long)s_hist[threadIdx.x]);
   }
   __syncthreads();
   if (threadIdx.x < 11 && blk_cnt[threadIdx.x]) {
@@ -610,15 +610,15 @@ __global__ void reset_alloc_kernel(Dev d) {
   uint32_t g = blockIdx.x * blockDim.x + threadIdx.x;
   if (g < d.nthreads) {
     for (const PagedSpace* sp : {&d.nspace, &d.vspace}) {
-      sp->lists[(size_t)g * sp->max_pages] = g + reserved_pages(sp->page_log2);
+      sp->lists[(size_t)g * sp->max_pages] = g + (sp == &d.nspace ? d.npool_base : d.vpool_base);
       sp->counts[g] = 1;
       sp->pos[g] = 0;
       sp->off[g] = 0;
     }
   }
   if (g == 0) {
-    d.ctl->npool_next = d.nthreads + reserved_pages(d.nspace.page_log2);
-    d.ctl->vpool_next = d.nthreads + reserved_pages(d.vspace.page_log2);
+    d.ctl->npool_next = d.nthreads + d.npool_base;
+    d.ctl->vpool_next = d.nthreads + d.vpool_base;
   }
 }
 
@@ -1259,8 +1259,11 @@ class Runtime {
     cap = cfg.stack_cap;
     if (block == 0 || block % 32 || block > 128) return fail("threads_per_block must be a multiple of 32 in [32, 128]");
     if (cap < 2 || (cap & (cap - 1))) return fail("stack_cap must be a power of two >= 2");
-    if (cfg.node_log2 < 10 || cfg.node_log2 > 29 || cfg.vars_log2 < 10 || cfg.vars_log2 > 29)
-      return fail("node_log2/vars_log2 must be in [10, 29]");
+    // Word indices are 32-bit; 32-bit ports address 2^29 words.
+    const uint32_t max_log2 = PORT_BITS == 64 ? 32 : 29;
+    if (cfg.node_log2 < 10 || cfg.node_log2 > max_log2 || cfg.vars_log2 < 10 || cfg.vars_log2 > max_log2)
+      return fail(PORT_BITS == 64 ? "node_log2/vars_log2 must be in [10, 32]" : "node_log2/vars_log2 must be in [10, 29]");
+    if (cfg.upper_half > 1) return fail("upper_half must be 0 or 1");
     smem = (size_t)block * cap * sizeof(Pair);
     if (block > 128) return fail("threads_per_block must be <= 128");
     if (cfg.local_nets > 1) return fail("local_nets must be 0 or 1");
@@ -1447,6 +1450,11 @@ class Runtime {
         return fail("node/var space too small for the thread count");
       d.npool_end = nfull - hn;
       d.vpool_end -= hv;
+      // upper_half: the pools start at the middle of each space.
+      d.npool_base = reserved_pages(d.nspace.page_log2) + (cfg.upper_half ? d.npool_end / 2 : 0);
+      d.vpool_base = reserved_pages(d.vspace.page_log2) + (cfg.upper_half ? d.vpool_end / 2 : 0);
+      if (d.npool_base + nthreads_max >= d.npool_end || d.vpool_base + nthreads_max >= d.vpool_end)
+        return fail("node/var space too small for the thread count");
       host_lo[0] = d.npool_end << d.nspace.page_log2;
       host_hi[0] = (uint32_t)std::min<uint64_t>((uint64_t)(d.npool_end + hn) << d.nspace.page_log2, d.node_mask);
       host_lo[1] = d.vpool_end << d.vspace.page_log2;
@@ -1810,6 +1818,26 @@ class Runtime {
     return 0;
   }
 
+  // Pages of a pool in lanes' hands: handed out (next - base) minus those
+  // waiting on the free-page ring (tail - head); 0 before the first turn.
+  static double pages_held(uint32_t next, uint32_t base, uint32_t ftail, uint32_t fhead) {
+    if (next < base) return 0;
+    const double out = (double)(next - base), free = ftail > fhead ? (double)(ftail - fhead) : 0.0;
+    return out > free ? out - free : 0.0;
+  }
+
+  // The message of a failed turn, with the allocator's state on out-of-memory.
+  std::string device_error(const Ctl& h) const {
+    std::string m = std::string("device error: ") + status_text(h.status) + " (info " + std::to_string(h.err_info) + ")";
+    if (h.oom_space)
+      m += " [" + std::string(h.oom_space == 2 ? "var" : "node") + " pages owned " + std::to_string(h.oom_pages) +
+           ", dry chunks " + std::to_string(h.oom_dry) + ", pool " + (h.oom_pool_dry ? "empty" : "not empty") +
+           ", pools at " + std::to_string(h.npool_next) + "/" + std::to_string(d.npool_end) + " and " +
+           std::to_string(h.vpool_next) + "/" + std::to_string(d.vpool_end) + ", live words " +
+           std::to_string(h.live_nodes) + " and " + std::to_string(h.live_vars) + "]";
+    return m;
+  }
+
   // Runs turns until the ring is empty (src/hvm.cu:1810-1839).
   int normalize() {
     result_valid = false;  // the net changes
@@ -1831,15 +1859,7 @@ class Runtime {
       }
       if (read_ctl(h) || collect_times()) return -1;
       if (cfg.persistent) turns_run += h.persist_ran;
-      if (h.status) {
-        std::string m = std::string("device error: ") + status_text(h.status) + " (info " + std::to_string(h.err_info) + ")";
-        if (h.oom_space)
-          m += " [" + std::string(h.oom_space == 2 ? "var" : "node") + " pages owned " + std::to_string(h.oom_pages) +
-               ", dry chunks " + std::to_string(h.oom_dry) + ", pool " + (h.oom_pool_dry ? "empty" : "not empty") +
-               ", pools at " + std::to_string(h.npool_next) + "/" + std::to_string(d.npool_end) + " and " +
-               std::to_string(h.vpool_next) + "/" + std::to_string(d.vpool_end) + "]";
-        return fail(m);
-      }
+      if (h.status) return fail(device_error(h));
       if (h.base == h.in_end) break;
       if (cfg.max_turns && turns_run >= cfg.max_turns) return fail("turn budget exhausted before normal form");
       // A net whose interaction count stops moving while redexes remain is
@@ -2027,8 +2047,13 @@ class Runtime {
                          [&](uint32_t x, uint32_t y) { return weight[x] < weight[y]; });
       }
       admit.clear();
+      // Pages in lanes' hands (handed out by a pool, not back on its free
+      // ring) also bound admission: lanes keep partly used pages, so a pool
+      // can run dry while the live words are well under their limit.
+      const bool pages_ok = pages_held(h.npool_next, d.npool_base, h.nf_tail, h.nf_head) < 0.6 * (d.npool_end - d.npool_base) &&
+                            pages_held(h.vpool_next, d.vpool_base, h.vf_tail, h.vf_head) < 0.6 * (d.vpool_end - d.vpool_base);
       while (ready_head < ready.size() && active.size() + admit.size() < max_inflight &&
-             h.live_nodes < node_limit && h.live_vars < var_limit && admit.size() < 4096)
+             h.live_nodes < node_limit && h.live_vars < var_limit && pages_ok && admit.size() < 4096)
         admit.push_back(ready[ready_head++]);
       if (!admit.empty()) {
         CK(cudaMemcpy(dact, admit.data(), admit.size() * sizeof(uint32_t), cudaMemcpyHostToDevice));
@@ -2053,7 +2078,7 @@ class Runtime {
       // A few turns, then the control block.
       if (launch_turns(4)) return -1;
       if (read_ctl(h) || collect_times()) return -1;
-      if (h.status) return fail(std::string("device error: ") + status_text(h.status));
+      if (h.status) return fail(device_error(h));
       if (pick_variant(h)) return -1;
       // Completions.
       if (!active.empty()) {
@@ -2634,6 +2659,7 @@ extern "C" void hvm_gb300_default_config(hvm_gb300_config* c) {
   c->fast_calls = 0;
   c->local_nets = 0;
   c->persistent = 0;
+  c->upper_half = 0;
 }
 
 extern "C" int hvm_gb300_create(const hvm_gb300_config* cfg, hvm_gb300_runtime** out) {
@@ -3243,6 +3269,8 @@ extern "C" int hvm_gb300_run_noalloc(const uint32_t* book, size_t words, uint32_
     sp->pos = lw; lw += NTHREADS;
     sp->off = lw; lw += NTHREADS;
   }
+  d.npool_base = reserved_pages(PAGE_LOG2);
+  d.vpool_base = reserved_pages(PAGE_LOG2);
   d.npool_end = 1u << (NODE_LOG2 - PAGE_LOG2);
   d.vpool_end = 1u << (VARS_LOG2 - PAGE_LOG2);
   d.nloc = nullptr;  // every def fits one chunk: the scratch tables are never used

@@ -219,6 +219,33 @@ def mixed_batch(count: int = 4096, seed: int = 0x4D495845) -> list[tuple[str, di
     return nets
 
 
+def serving_pool(count: int = 96, seed: int = 0x53525645) -> list[tuple[str, dict]]:
+    """Request templates of the serving workload at its stated scale: the
+    mixed batch's three families, each net's size log-uniform from 2^8 to
+    2^22 nodes -- tree sums of 2^7..2^21 leaves (about twice as many nodes),
+    bitonic sums of the most keys n with n log2(n)^2 / 2 within the size
+    (2^6..2^14), countdown loops of size/4 steps (10..1e5). Returns
+    [(code, description)]."""
+    rng = PCG32(seed, PCG_DEFAULT_SEQ)
+    nets = []
+    for i in range(count):
+        kind = i % 3
+        lg = 8 + rng.uniform() * 14  # log2 of the size in nodes
+        if kind == 0:
+            d = min(21, max(7, int(round(lg)) - 1))
+            nets.append((tree_sum(d), {"family": "tree_sum", "depth": d, "log2_size": lg}))
+        elif kind == 1:
+            k = 6
+            while k < 14 and (1 << (k + 1)) * (k + 1) ** 2 / 2 <= 2 ** lg:
+                k += 1
+            s = rng.next() | (rng.next() << 32)
+            nets.append((bitonic_sum(k, s), {"family": "bitonic", "log2n": k, "seed": s, "log2_size": lg}))
+        else:
+            length = int(min(1e5, max(10, round(2 ** lg / 4))))
+            nets.append((countdown(length), {"family": "countdown", "length": length, "log2_size": lg}))
+    return nets
+
+
 def poisson_arrivals(count: int, rate: float, seed: int = 0x5E21E) -> list[float]:
     """Arrival times (seconds) of a Poisson process of `rate` requests/s."""
     rng = PCG32(seed, PCG_DEFAULT_SEQ)

@@ -13,6 +13,9 @@ reference sources exist; the fixtures travel, the reference does not).
   batch_mixed_4096.json    per net of the 4096-net mixed batch
                            (workloads.mixed_batch): its family and size, the
                            reference C runtime's interaction count and result.
+  serving_pool.json        the same for the serving workload's request
+                           templates (workloads.serving_pool: sizes up to
+                           2^22 nodes).
   io_programs.json         the reference's IO programs (tests/programs/io,
                            examples/demo_io) run by the reference C runtime
                            in a scratch directory holding the files they
@@ -29,7 +32,8 @@ reference sources exist; the fixtures travel, the reference does not).
                            evaluation counted by the oracle (-w), the
                            roofline numerator.
 
-Usage: python tests/golden/make_golden.py [--reference /root/reference] [--only-io | --only-dl | --only-batch]
+Usage: python tests/golden/make_golden.py [--reference /root/reference] [--only-io | --only-dl | --only-batch |
+                                          --only-serving]
 """
 from __future__ import annotations
 
@@ -252,6 +256,17 @@ def make_batch(count: int = 4096, workers: int = 4) -> None:
     print("batch", count, sum(e["itrs"] for e in out))
 
 
+def make_serving(count: int = 96, workers: int = 4) -> None:
+    import multiprocessing as mp
+    nets = W.serving_pool(count)
+    items = [(i, code, info) for i, (code, info) in enumerate(nets)]
+    with mp.get_context("spawn").Pool(workers) as pool:
+        out = pool.map(_batch_entry, items, chunksize=1)
+    with open(os.path.join(HERE, "serving_pool.json"), "w") as f:
+        json.dump({"count": count, "nets": out}, f, indent=0)
+    print("serving pool", count, sum(e["itrs"] for e in out))
+
+
 def snapshot_result(ref: str, rel: str) -> str | None:
     key = rel.replace("tests/programs/", "").replace("examples/", "").replace("/", "__")
     for snap in glob.glob(os.path.join(ref, "tests", "snapshots", "*.snap")):
@@ -270,6 +285,7 @@ def main() -> None:
     ap.add_argument("--only-io", action="store_true")
     ap.add_argument("--only-counts", action="store_true")
     ap.add_argument("--only-dl", action="store_true")
+    ap.add_argument("--only-serving", action="store_true")
     args = ap.parse_args()
     if args.only_counts:
         subprocess.run(["make", "-C", os.path.join(ROOT, "oracle")], check=True)
@@ -277,6 +293,10 @@ def main() -> None:
         return
     if args.only_batch:
         make_batch()
+        return
+    if args.only_serving:
+        subprocess.run(["make", "-C", os.path.join(ROOT, "oracle"), "stage", "ref", f"REF_ROOT={args.reference}"], check=True)
+        make_serving()
         return
     if args.only_dl:
         subprocess.run(["make", "-C", os.path.join(ROOT, "oracle"), "stage", "ref", f"REF_ROOT={args.reference}"], check=True)

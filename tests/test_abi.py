@@ -74,3 +74,20 @@ def test_ctypes_mirrors_match_the_header(hvm, tmp_path):
     got = [int(x) for x in subprocess.run([str(exe)], capture_output=True, text=True, check=True).stdout.split()]
     assert got == [ctypes.sizeof(hvm.Config), hvm.Config.turn_budget_cap.offset, ctypes.sizeof(hvm._Stats),
                    ctypes.sizeof(hvm.Turn), hvm.Turn.outputs.offset]
+
+
+def test_port64_library_exports_and_refuses_32bit_calls(hvm):
+    # The 64-bit port build exports the same C ABI; the no-alloc entry point,
+    # whose output ports are 32-bit, refuses before touching a device.
+    L = hvm.lib64()
+    nm = subprocess.run(["nm", "-D", "--defined-only", hvm.LIB64_PATH], capture_output=True, text=True).stdout
+    assert declared_functions() <= set(re.findall(r" T (\w+)$", nm, re.M))
+    import numpy as np
+    book = hvm.book_from_text("@main = 1\n")
+    out = np.zeros(16, dtype=np.uint32)
+    err = ctypes.create_string_buffer(256)
+    n, itrs = ctypes.c_size_t(), ctypes.c_uint64()
+    u32p = ctypes.POINTER(ctypes.c_uint32)
+    rc = L.hvm_gb300_run_noalloc(book.ctypes.data_as(u32p), book.size, out.ctypes.data_as(u32p),
+                                 out.ctypes.data_as(u32p), 8, ctypes.byref(n), ctypes.byref(itrs), err, 256)
+    assert rc == -1 and b"64-bit" in err.value
