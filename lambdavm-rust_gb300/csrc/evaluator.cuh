@@ -249,12 +249,6 @@ struct Alloc {
 
 // ---- per-thread state ----------------------------------------------------------
 
-// The running turn's interactions per rule for the block, in shared memory:
-// each warp round adds its lanes' counts with one atomic per rule it ran
-// (the interaction count is the sum over the counted rules; entry LINK counts
-// the local-net variant's LEAK copies, which are not interactions).
-__shared__ unsigned s_hist[8];
-
 struct TState {
   Pair* stk;                  // this thread's deque in shared memory (stride = blockDim.x)
   uint32_t stride;
@@ -262,9 +256,10 @@ struct TState {
   uint32_t gid;
   Alloc na, va;               // node / var allocators
   unsigned long long base;    // ring index of this turn's first input (overflow check)
-  uint32_t leak, retries;     // this turn's counts: budget-bounded, so 32 bits suffice
+  uint32_t itrs, leak, retries;  // this turn's counts: budget-bounded, so 32 bits suffice
   int live_nodes, live_vars;  // words taken minus words freed in this turn
   bool dirty;                 // wrote fresh words not yet ordered by a fence
+  uint32_t hist[8];
   bool dead;                  // set after a fatal status: stop interacting
   uint32_t waited;            // rounds this lane's next redex has waited for its rule class
 };
@@ -909,8 +904,13 @@ __device__ __forceinline__ void ring_put(const Dev& d, TState& t, Pair r) {
 }
 
 // `drain` (local-net variant, at a turn's end): every redex given is made
-// global (LEAK or GLOBALIZE) instead of interacting.
-template <bool FAST, bool LOCAL>
+// global (LEAK or GLOBALIZE) instead of interacting. HREG selects how the
+// per-rule counters are indexed: by constant indices (the thread state then
+// lives in registers), or by the rule (which keeps the thread state in local
+// memory) -- measured faster for the 64-register variant, whose registers
+// cannot hold the state. (Per-block counters in shared memory, added once per
+// warp round, measured slower than either.)
+template <bool FAST, bool LOCAL, bool HREG = true>
 __device__ __forceinline__ int lockstep_round(const Dev& d, TState& t, bool has, Pair r, WarpProf* wp,
                                               bool drain = false) {
   long long c0 = wp ? clock64() : 0;
@@ -1208,18 +1208,26 @@ __device__ __forceinline__ int lockstep_round(const Dev& d, TState& t, bool has,
     wp->v[PROF_CYC_LINK] += c4 - c3;
   }
   if (has && rc == IR_RETRY) { push<LOCAL>(d, t, r); t.retries++; }
-  // Counts: the lanes that ran one rule add to its entry through one lane.
-  const bool done = has && rc == IR_DONE;
-  const uint32_t key = done && p.counted ? rule : (LOCAL && done && rule == LEAK_RULE) ? (uint32_t)LINK : 0xFFu;
-  const unsigned grp = __match_any_sync(0xFFFFFFFFu, key);
-  if (key != 0xFFu && (threadIdx.x & 31) == (unsigned)(__ffs(grp) - 1)) atomicAdd(&s_hist[key], (unsigned)__popc(grp));
-  if (FAST) {  // the interactions a fast path performs in place (src/cmp.rs:147, 191, 220, 253)
-    const bool fp = done && p.counted && p.fast;
-    const unsigned anni = __reduce_add_sync(0xFFFFFFFFu, fp ? (p.fast == 1 ? 1u : 2u) : 0u);
-    const unsigned swit = __reduce_add_sync(0xFFFFFFFFu, fp && p.fast >= 2 ? 1u : 0u);
-    if ((threadIdx.x & 31) == 0) {
-      if (anni) atomicAdd(&s_hist[ANNI], anni);
-      if (swit) atomicAdd(&s_hist[SWIT], swit);
+  if (LOCAL && has && rc == IR_DONE && rule == LEAK_RULE) t.hist[LINK]++;  // LEAK copies (not interactions)
+  if (has && rc == IR_DONE && p.counted) {
+    t.itrs++;
+    if (!HREG) {
+      t.hist[rule]++;
+    } else {
+      switch (rule) {
+        case CALL: t.hist[CALL]++; break;
+        case VOID: t.hist[VOID]++; break;
+        case ERAS: t.hist[ERAS]++; break;
+        case ANNI: t.hist[ANNI]++; break;
+        case COMM: t.hist[COMM]++; break;
+        case OPER: t.hist[OPER]++; break;
+        default: t.hist[SWIT]++; break;
+      }
+    }
+    if (FAST && p.fast) {  // the interactions a fast path performs in place (src/cmp.rs:147, 191, 220, 253)
+      t.itrs += p.fast == 1 ? 1 : 3;
+      t.hist[ANNI] += p.fast == 1 ? 1 : 2;
+      if (p.fast >= 2) t.hist[SWIT]++;
     }
   }
   return rc;

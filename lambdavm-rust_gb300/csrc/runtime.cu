@@ -238,13 +238,12 @@ __device__ __forceinline__ void turn_work(const Dev& d, uint32_t cap, const Turn
   alloc_load<false>(d.nspace, t.gid, t.na);
   alloc_load<true>(d.vspace, t.gid, t.va);
   t.base = base;
-  t.leak = t.retries = 0;
+  t.itrs = t.leak = t.retries = 0;
   t.live_nodes = t.live_vars = 0;
   t.dirty = false;
+  for (int i = 0; i < 8; i++) t.hist[i] = 0;
   t.dead = false;
   t.waited = 0;
-  if (threadIdx.x < 8) s_hist[threadIdx.x] = 0;
-  __syncthreads();
   if (LOCAL) {
     // Each lane clears its own slice of the block's local net (128-thread blocks).
     for (uint32_t i = 0; i < LOCAL_SLICE; i++) { lnode_of(t)[lbase_of() + i] = 0; lvar_of(t)[lbase_of() + i] = 0; }
@@ -331,7 +330,7 @@ __device__ __forceinline__ void turn_work(const Dev& d, uint32_t cap, const Turn
     }
     const bool has = go;
     const Pair r = has ? pop(t) : 0;
-    lockstep_round<FAST, LOCAL>(d, t, has, r, prof_on ? &prof : nullptr);
+    lockstep_round<FAST, LOCAL, MIN_BLOCKS_128 != 8>(d, t, has, r, prof_on ? &prof : nullptr);
     if (__any_sync(0xFFFFFFFFu, t.dead)) break;
     if (LOCAL && __any_sync(0xFFFFFFFFu, ovf_len_of(t) > OVF_HIGH)) break;  // end the turn before an overflow fills
     // The stop flag is tested one round after it was loaded, so its L2
@@ -357,7 +356,7 @@ __device__ __forceinline__ void turn_work(const Dev& d, uint32_t cap, const Turn
       }
       const Pair r = has ? pop(t) : 0;
       if (has && !local_pair(r)) { ring_put(d, t, r); has = false; }
-      lockstep_round<FAST, LOCAL>(d, t, has, r, nullptr, true);
+      lockstep_round<FAST, LOCAL, MIN_BLOCKS_128 != 8>(d, t, has, r, nullptr, true);
       if (__any_sync(0xFFFFFFFFu, t.dead)) break;
     }
   }
@@ -406,11 +405,12 @@ __device__ __forceinline__ void turn_work(const Dev& d, uint32_t cap, const Turn
   if (threadIdx.x < 11) blk_cnt[threadIdx.x] = 0;
   __syncthreads();
   unsigned long long v;
+  v = warp_sum(t.itrs);    if (lane == 0 && v) atomicAdd(&blk_cnt[0], v);
   v = warp_sum(t.leak);    if (lane == 0 && v) atomicAdd(&blk_cnt[1], v);
   v = warp_sum(t.retries); if (lane == 0 && v) atomicAdd(&blk_cnt[2], v);
-  if (threadIdx.x < 8) {
-    blk_cnt[3 + threadIdx.x] = s_hist[threadIdx.x];
-    if (threadIdx.x != LINK) atomicAdd(&blk_cnt[0], (unsigned long long)s_hist[threadIdx.x]);
+  for (int i = 0; i < 8; i++) {
+    v = warp_sum(t.hist[i]);
+    if (lane == 0 && v) atomicAdd(&blk_cnt[3 + i], v);
   }
   __syncthreads();
   if (threadIdx.x < 11 && blk_cnt[threadIdx.x]) {
