@@ -27,6 +27,7 @@ import json
 import math
 import os
 import re
+import signal
 import statistics
 import subprocess
 import sys
@@ -437,8 +438,7 @@ def run_oracle(book, threads: int) -> tuple[int, float, str]:
         book.tofile(f.name)
         path = f.name
     try:
-        out = subprocess.run([ORACLE, "-t", str(threads), "-n", path], capture_output=True, text=True,
-                             check=True).stdout
+        out = run_bounded([ORACLE, "-t", str(threads), "-n", path], 600)
     finally:
         os.unlink(path)
     itrs = int(re.search(r"^- ITRS: (\d+)$", out, re.M).group(1))
@@ -447,12 +447,29 @@ def run_oracle(book, threads: int) -> tuple[int, float, str]:
     return itrs, ns / 1e9, res
 
 
-def run_reference_c(path: str) -> tuple[int, float, str]:
+def run_bounded(cmd: list[str], timeout: float) -> str:
+    """Runs a reference binary with no standard input, in its own process
+    group, killed as a group once `timeout` seconds pass (subprocess's own
+    timeout kills only the child and then waits for its pipes)."""
+    proc = subprocess.Popen(cmd, stdin=subprocess.DEVNULL, stdout=subprocess.PIPE, stderr=subprocess.PIPE,
+                            text=True, start_new_session=True)
+    try:
+        out, err = proc.communicate(timeout=timeout)
+    except subprocess.TimeoutExpired:
+        os.killpg(proc.pid, signal.SIGKILL)
+        proc.communicate()
+        raise
+    if proc.returncode != 0:
+        raise subprocess.CalledProcessError(proc.returncode, cmd, out, err)
+    return out
+
+
+def run_reference_c(path: str, timeout: float = 300) -> tuple[int, float, str]:
     """The reference's own C runtime (`hvm run-c`: src/run.c + src/hvm.c built
     by oracle/Makefile) on a book file. Seconds = its own TIME (boot,
     normalise, readback and print, src/hvm.c:1759-1779), taken at full
     precision from its MIPS line."""
-    out = subprocess.run([REF_C, path], capture_output=True, text=True, check=True, timeout=1800).stdout
+    out = run_bounded([REF_C, path], timeout)
     itrs = int(re.search(r"^- ITRS: (\d+)$", out, re.M).group(1))
     mips = float(re.search(r"^- MIPS: ([0-9.]+)$", out, re.M).group(1))
     res = re.search(r"^Result: (.*)$", out, re.M).group(1)
@@ -560,7 +577,7 @@ def run_reference_cu(path: str, timeout: float = 120) -> tuple[int, float, str]:
     """The reference's own CUDA runtime (src/run.cu + src/hvm.cu rebuilt for
     sm_103a by oracle/Makefile) on a book file: interaction count, wall time
     of the hvm_cu call (the driver's `- WALL`), printed result."""
-    out = subprocess.run([REF_CU, path], capture_output=True, text=True, check=True, timeout=timeout).stdout
+    out = run_bounded([REF_CU, path], timeout)
     itrs = int(re.search(r"^- ITRS: (\d+)$", out, re.M).group(1))
     wall = float(re.search(r"^- WALL: ([0-9.]+)s$", out, re.M).group(1))
     res = re.search(r"^Result: (.*)$", out, re.M)
@@ -734,7 +751,10 @@ def bench_gpu(args, hvm, book, golden, desc, ws, rank, local, dist):
                            "frac_of_2gb_region": ach / peak_far if ach else None,
                            "atomics_per_interaction": api, "peak_source": "measured by hvm_gb300_atomic_peak"}
     # CPU baseline: the reference's run-c on this host's cores, one full evaluation.
-    cpu = time_cpu_reference(book, golden, hvm.canonical, 1)
+    try:
+        cpu = time_cpu_reference(book, golden, hvm.canonical, 1)
+    except (subprocess.TimeoutExpired, subprocess.CalledProcessError) as e:
+        cpu = {"unavailable": f"the reference C runtime did not complete ({type(e).__name__})"}
     cpu.pop("seconds")
     return {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
@@ -807,7 +827,10 @@ def main():
         # loads the repository's library.
         W = importlib.import_module("lambdavm-rust_gb300.workloads")
         golden = json.load(open(GOLDEN))[key]
-        line = bench_reference(args, make(W), golden, desc, ws, rank, oracle_module().canonical)
+        try:
+            line = bench_reference(args, make(W), golden, desc, ws, rank, oracle_module().canonical)
+        except (subprocess.TimeoutExpired, subprocess.CalledProcessError) as e:
+            line = {"impl": "reference", "unavailable": f"the reference C runtime did not complete ({type(e).__name__})"}
         if line:
             print(json.dumps(line), flush=True)
         return

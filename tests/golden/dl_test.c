@@ -4,7 +4,8 @@
  *   *_c  the reference C runtime's signature, Port fn(Net*, Book*, Port)
  *        (src/run.c:681-698), using the net functions of the reference
  *        binary (readback_bytes / inject_bytes, src/run.c:123-161, 224-246;
- *        the binary is linked with -rdynamic so that this library sees them);
+ *        binary built with -rdynamic, oracle/Makefile ref-dl, so that this
+ *        library sees them);
  *   *_g  the GB300 runtime's hvm_gb300_dl_fn, using hvm_gb300_io_*.
  * The golden script runs the *_c programs through the reference binary, the
  * GPU tests the *_g programs through `hvm run-cu`.

@@ -125,6 +125,9 @@ BIG_READ = ("@call ~ (d ((e 47) f))", "@call ~ (d ((e 20000) f))")
 IO_STDIN = "io from the tests\n"
 
 
+REF_DL_BIN = os.path.join(ROOT, "oracle", "_ref", "hvm_ref_dl")
+
+
 def run_ref_io(code: str, dl_lib: str | None = None) -> dict:
     buf = H.book_from_text(code)
     with tempfile.TemporaryDirectory() as cwd:
@@ -135,7 +138,8 @@ def run_ref_io(code: str, dl_lib: str | None = None) -> dict:
             build_dl_lib(os.path.join(cwd, dl_lib))
         path = os.path.join(cwd, "book.bin")
         buf.tofile(path)
-        r = subprocess.run([REF_BIN, path], capture_output=True, text=True, timeout=600, cwd=cwd, input=IO_STDIN)
+        r = subprocess.run([REF_DL_BIN if dl_lib else REF_BIN, path], capture_output=True, text=True, timeout=600,
+                           cwd=cwd, input=IO_STDIN)
     res = re.search(r"^Result: (.*)$", r.stdout, re.M)
     itrs = re.search(r"^- ITRS: (\d+)$", r.stdout, re.M)
     if r.returncode != 0 or not res or not itrs:
@@ -167,7 +171,8 @@ def make_io(ref: str) -> None:
 
 
 # DL_CALL programs: DL_OPEN the test library (dl_test.c), DL_CALL one of its
-# functions on an argument and return the result. The program around the
+# functions on an argument and return the result (run by the reference binary
+# built with its functions exported, oracle/Makefile ref-dl). The program around the
 # calls is the IO prelude of tests/programs/io/open1.hvm (IO/bind, call, the
 # String constructors); each symbol has a C-runtime twin (`*_c`) of the same
 # length that the reference binary calls, the `*_g` one is the GPU runtime's.
@@ -299,7 +304,8 @@ def main() -> None:
         make_serving()
         return
     if args.only_dl:
-        subprocess.run(["make", "-C", os.path.join(ROOT, "oracle"), "stage", "ref", f"REF_ROOT={args.reference}"], check=True)
+        subprocess.run(["make", "-C", os.path.join(ROOT, "oracle"), "stage", "ref-dl", f"REF_ROOT={args.reference}"],
+                       check=True)
         make_dl(args.reference)
         return
     if args.only_io:
