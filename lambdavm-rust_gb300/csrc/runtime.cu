@@ -1818,14 +1818,6 @@ class Runtime {
     return 0;
   }
 
-  // Pages of a pool in lanes' hands: handed out (next - base) minus those
-  // waiting on the free-page ring (tail - head); 0 before the first turn.
-  static double pages_held(uint32_t next, uint32_t base, uint32_t ftail, uint32_t fhead) {
-    if (next < base) return 0;
-    const double out = (double)(next - base), free = ftail > fhead ? (double)(ftail - fhead) : 0.0;
-    return out > free ? out - free : 0.0;
-  }
-
   // The message of a failed turn, with the allocator's state on out-of-memory.
   std::string device_error(const Ctl& h) const {
     std::string m = std::string("device error: ") + status_text(h.status) + " (info " + std::to_string(h.err_info) + ")";
@@ -2036,7 +2028,7 @@ class Runtime {
     memset(&h, 0, sizeof(h));
     auto t0 = std::chrono::steady_clock::now();
     auto now_s = [&]() { return std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count(); };
-    uint64_t polls = 0;
+    uint64_t polls = 0, stalled_polls = 0;
     for (;;) {
       double now = now_s();
       // Arrivals join the ready queue; admission takes from it.
@@ -2047,14 +2039,12 @@ class Runtime {
                          [&](uint32_t x, uint32_t y) { return weight[x] < weight[y]; });
       }
       admit.clear();
-      // Pages in lanes' hands (handed out by a pool, not back on its free
-      // ring) also bound admission: lanes keep partly used pages, so a pool
-      // can run dry while the live words are well under their limit.
-      const bool pages_ok = pages_held(h.npool_next, d.npool_base, h.nf_tail, h.nf_head) < 0.6 * (d.npool_end - d.npool_base) &&
-                            pages_held(h.vpool_next, d.vpool_base, h.vf_tail, h.vf_head) < 0.6 * (d.vpool_end - d.vpool_base);
       while (ready_head < ready.size() && active.size() + admit.size() < max_inflight &&
-             h.live_nodes < node_limit && h.live_vars < var_limit && pages_ok && admit.size() < 4096)
+             h.live_nodes < node_limit && h.live_vars < var_limit && admit.size() < 4096)
         admit.push_back(ready[ready_head++]);
+      // Progress: with nothing in flight, a waiting net is admitted whatever
+      // the counters say (so the stream cannot stop with nets still queued).
+      if (admit.empty() && active.empty() && ready_head < ready.size()) admit.push_back(ready[ready_head++]);
       if (!admit.empty()) {
         CK(cudaMemcpy(dact, admit.data(), admit.size() * sizeof(uint32_t), cudaMemcpyHostToDevice));
         h2d_bytes += admit.size() * sizeof(uint32_t);
@@ -2081,6 +2071,7 @@ class Runtime {
       if (h.status) return fail(device_error(h));
       if (pick_variant(h)) return -1;
       // Completions.
+      const size_t active_before = active.size();
       if (!active.empty()) {
         CK(cudaMemcpy(dlive, active.data(), active.size() * sizeof(uint32_t), cudaMemcpyHostToDevice));
         active_roots_kernel<<<((uint32_t)active.size() + 255) / 256, 256>>>(d, dlive, (Port*)mem_roots,
@@ -2106,6 +2097,12 @@ class Runtime {
       polls++;
       const bool quiet = h.base == h.in_end;
       if (quiet && admitted_total == nroots) break;
+      // A quiet ring with nothing admitted, nothing completed and no arrival
+      // still to come cannot change: fail instead of polling forever.
+      const bool progressed = !admit.empty() || active.size() != active_before;
+      const bool arrival_due = next < nroots && arrival[next] > now_s();
+      stalled_polls = quiet && !progressed && !arrival_due ? stalled_polls + 1 : 0;
+      if (stalled_polls > 64) return fail("stream stalled: the ring is empty and no net completes or can be admitted");
       if (quiet && active.empty() && ready_head == ready.size() && next < nroots && arrival[next] > now_s()) {
         // Idle until the next arrival.
         while (arrival[next] > now_s()) {}
