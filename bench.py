@@ -887,14 +887,20 @@ def main():
     try:
         line = bench_gpu(args, hvm, book, golden, desc, ws, rank, local, dist)
         if line is not None and not args.no_batch:
-            line["batched"] = bench_batch(hvm, W, args)
-            line["batched_learned"] = bench_batch(hvm, W, args, plain_sample=0, policy="learned")
-            line["batched_tuned"] = bench_batch_tuned(hvm, W, args)
-            line["config4"] = config4_report(line["batched"], line["batched_learned"], line["batched_tuned"])
-            line["scheduler"] = bench_scheduler(hvm, W)
-        if line is not None and not args.no_batch:
-            line["serving"] = bench_serving_scaled(hvm, W)
-            line["reference_cuda"] = bench_reference_cuda(hvm, W)
+            # The reports beside the headline: one that fails records its
+            # error under its own key instead of losing the line.
+            def report(key, fn):
+                try:
+                    line[key] = fn()
+                except Exception as e:  # noqa: BLE001 -- recorded in the line
+                    line[key] = {"error": f"{type(e).__name__}: {e}"[:300]}
+            report("batched", lambda: bench_batch(hvm, W, args))
+            report("batched_learned", lambda: bench_batch(hvm, W, args, plain_sample=0, policy="learned"))
+            report("batched_tuned", lambda: bench_batch_tuned(hvm, W, args))
+            report("config4", lambda: config4_report(line["batched"], line["batched_learned"], line["batched_tuned"]))
+            report("scheduler", lambda: bench_scheduler(hvm, W))
+            report("serving", lambda: bench_serving_scaled(hvm, W))
+            report("reference_cuda", lambda: bench_reference_cuda(hvm, W))
     finally:
         dist.close()
     if line:
