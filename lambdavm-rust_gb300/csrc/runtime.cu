@@ -2827,21 +2827,15 @@ extern "C" int hvm_gb300_result(hvm_gb300_runtime* r, char* out, size_t cap, siz
 // net of the runtime running the IO loop. A failure records the error, makes
 // the DL_CALL fail and returns -1.
 
-namespace hvm_io {
-using namespace hvm;
-
 static hvm::Runtime& io_rt(hvm_gb300_io* io) { return *reinterpret_cast<hvm::Runtime*>(io); }
-// The 64-bit port build calls no DL_CALL library, so these are never reached there.
+// The ports these functions exchange are 32-bit: the 64-bit port build calls
+// no DL_CALL library, so there they refuse.
 constexpr bool IO_PORTS_32 = hvm::PORT_BITS == 32;
 static int io_fail(hvm::Runtime& rt, const char* msg) {
   if (msg) rt.fail(msg);
   rt.io_failed = true;
   return -1;
 }
-}  // namespace hvm_io
-using hvm_io::io_rt;
-using hvm_io::io_fail;
-using hvm_io::IO_PORTS_32;
 
 extern "C" int hvm_gb300_io_expand(hvm_gb300_io* io, uint32_t port, uint32_t* out) {
   if (!IO_PORTS_32) return -1;

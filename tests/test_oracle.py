@@ -126,3 +126,24 @@ def test_gen_c_compiled_mode_matches_run_c(hvm, workloads, ref_programs, config_
     assert len(rows) >= 30
     for name, t, itrs_ok, nf_ok in rows:
         assert itrs_ok and nf_ok, (name, t)
+
+
+def test_oracle_matches_serving_pool_goldens(hvm, oracle, workloads):
+    # The serving pool's fixture came from the reference C runtime; the
+    # oracle restatement reproduces every template it can finish in seconds
+    # (72 of the 96, about 15 M interactions together).
+    import json
+    import os
+    from conftest import GOLDEN
+    with open(os.path.join(GOLDEN, "serving_pool.json")) as f:
+        gold = json.load(f)
+    nets = workloads.serving_pool(gold["count"])
+    checked = 0
+    for (code, info), g in zip(nets, gold["nets"]):
+        if g["itrs"] >= 2_000_000:
+            continue
+        out = oracle(code, threads=2)
+        assert out["itrs"] == g["itrs"], info
+        assert out["result"] == g["result"], info
+        checked += 1
+    assert checked >= 64
