@@ -455,7 +455,7 @@ __device__ __forceinline__ void turn_close(const Dev& d, uint32_t cap, const Tur
       c->persist_ran = k;
       c->blocks_done = 0;
       __threadfence();
-      st_release_u32(&c->epoch, c->epoch + 1);
+      st_release_u32(&c->epoch, ld_acquire_u32(&c->epoch) + 1);
     }
   }
   if (PERSIST && !ran) return;
@@ -530,7 +530,7 @@ __device__ __forceinline__ void turn_close(const Dev& d, uint32_t cap, const Tur
       c->go = c->status == 0 && pending != 0 && k + 1 < turns && pending >= lo && pending < hi;
       c->persist_ran = k + 1;
       __threadfence();
-      st_release_u32(&c->epoch, c->epoch + 1);
+      st_release_u32(&c->epoch, ld_acquire_u32(&c->epoch) + 1);
     }
   }
 }
