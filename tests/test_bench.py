@@ -39,3 +39,28 @@ def test_reference_arm_runs_the_reference_without_the_library():
     golden = json.load(open(bench.GOLDEN))["tree_sum_d20"]
     assert line["config"] == bench.arm_config(bench.WORKLOADS["tree_sum_d20"][2], golden)
     assert line["value"] > 0 and line["e2e"]["h2d_bytes_per_step"] == 0
+
+
+def test_reference_binaries_run_bounded(tmp_path):
+    # A reference binary that hangs -- here one that sleeps and leaves a
+    # background child holding its output pipe -- ends the bench's call after
+    # the timeout, its whole process group killed, instead of blocking it.
+    sys.path.insert(0, ROOT)
+    import time
+    import bench
+    fake = tmp_path / "hangs.sh"
+    fake.write_text("#!/bin/sh\nsleep 60 &\nsleep 60\n")
+    fake.chmod(0o755)
+    t0 = time.monotonic()
+    with pytest.raises(subprocess.TimeoutExpired):
+        bench.run_bounded([str(fake)], timeout=1)
+    assert time.monotonic() - t0 < 10
+    ok = tmp_path / "ok.sh"
+    ok.write_text("#!/bin/sh\necho '- ITRS: 7'\n")
+    ok.chmod(0o755)
+    assert bench.run_bounded([str(ok)], timeout=10).strip() == "- ITRS: 7"
+    bad = tmp_path / "fails.sh"
+    bad.write_text("#!/bin/sh\nexit 3\n")
+    bad.chmod(0o755)
+    with pytest.raises(subprocess.CalledProcessError):
+        bench.run_bounded([str(bad)], timeout=10)

@@ -175,3 +175,18 @@ def test_workloads_never_divide(workloads):
     texts += [code for code, _ in workloads.mixed_batch(64)]
     for code in texts:
         assert not re.search(r"\[:?[/%]", code)
+
+
+def test_serving_pool_sizes(workloads):
+    # The serving workload's templates: the three families in turn, sizes
+    # log-uniform in 2^8..2^22 nodes, reproducible from the seed; tree sums of
+    # at most 2^21 leaves, bitonic sums of at most 2^14 keys, countdowns of
+    # at most 1e5 steps.
+    pool = workloads.serving_pool(96)
+    assert pool == workloads.serving_pool(96)
+    fams = [info["family"] for _, info in pool]
+    assert fams == ["tree_sum", "bitonic", "countdown"] * 32
+    assert all(8 <= info["log2_size"] <= 22 for _, info in pool)
+    assert max(info["depth"] for _, info in pool if info["family"] == "tree_sum") <= 21
+    assert max(info["log2n"] for _, info in pool if info["family"] == "bitonic") <= 14
+    assert all(10 <= info["length"] <= 100_000 for _, info in pool if info["family"] == "countdown")
