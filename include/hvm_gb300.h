@@ -115,9 +115,10 @@ typedef struct {
                                  src/hvm.cu:130-135, 1129-1174): fresh words of a turn in the block's
                                  shared memory, copied out to HBM when a global var would point at
                                  them and at the turn's end; 128-thread blocks, register caps 0/8 */
-  uint32_t persistent;        /* 1 = a normalisation runs its turns inside cooperative launches of up
-                                 to 4096 turns each, closed on the device (register caps 0 and 8, no
-                                 fast_calls/profile/local_nets); 0 = one launch per turn */
+  uint32_t persistent;        /* 1 = a normalisation (single net or batch) runs its turns inside
+                                 cooperative launches of up to 4096 turns each, closed on the device
+                                 (register caps 0 and 8, no fast_calls/profile/local_nets; streams keep
+                                 one launch per turn); 0 = one launch per turn (default) */
   uint32_t upper_half;        /* 1 = the allocator hands out words from the upper half of each space
                                  only (every fresh word has a high index: with 64-bit ports and 2^32-word
                                  spaces, indices beyond the 32-bit port's range) */
